@@ -1,0 +1,287 @@
+/*
+ * sph_gb300.h — C ABI of the GB300 SPH interaction engine.
+ *
+ * The engine computes the three per-step pair interactions of the FDPS-based
+ * SPH stellar-collision code yamauchi1132/Research_Codes (sph_yamauchi/run):
+ *   - the density sum with the fixed 3-pass smoothing-length iteration and the
+ *     grad-h / div v / |rot v| pass            (hdr_density.hpp:246-366)
+ *   - the hydro force: pressure gradient, Balsara-switched artificial
+ *     viscosity, du/dt, conduction signal, v_sig max and the gravity
+ *     softening correction                     (hdr_hydro.hpp:312-424)
+ *   - the softened tree-gravity sum over particles and monopoles
+ *                                              (hdr_gravity.hpp:286-342)
+ * on sm_103a CUDA cores.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (SPH_OK == 0).  Structs named sph_<Name> reproduce the reference's FDPS
+ * particle/force classes byte for byte (offsets are asserted in the library
+ * and reported by sph_abi_layout()), so arrays built for the reference's
+ * functors can be passed unchanged.
+ *
+ * Threading: a context owns one CUDA stream and its device buffers; calls on
+ * one context must not overlap.  Different contexts may be used from
+ * different host threads.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes.  The reference has no error channel (void functors,
+ * Dispatch/Retrieve return 0, limits are assert()s: hdr_densityGPU.cu:503,
+ * 521-522); these replace the asserts and never abort the process.          */
+enum sph_status {
+    SPH_OK                   = 0,
+    SPH_ERR_INVALID_ARGUMENT = 1,  /* null pointer, negative count, bad enum  */
+    SPH_ERR_CAPACITY         = 2,  /* walk / i / j count beyond the capacity  */
+    SPH_ERR_CUDA             = 3,  /* a CUDA runtime call failed              */
+    SPH_ERR_NONFINITE        = 4,  /* NaN/Inf found in an output              */
+    SPH_ERR_NOT_CONVERGED    = 5,  /* search-radius expansion hit its cap     */
+    SPH_ERR_STATE            = 6,  /* e.g. Retrieve without a Dispatch        */
+    SPH_ERR_NO_DEVICE        = 7   /* no CUDA device / unsupported device     */
+};
+
+/* Arithmetic of the pair kernels. */
+enum sph_precision {
+    /* FP32 pair arithmetic on positions/velocities taken relative to each
+     * i-group's centre, compensated (Kahan) accumulation; per-particle
+     * scalars (h update, Omega, write-back) in FP64.                        */
+    SPH_PREC_FP32C = 0,
+    /* Plain FP64 pair arithmetic on global coordinates. */
+    SPH_PREC_FP64  = 1
+};
+
+/* ------------------------------------------------------------------------ */
+/* Reference POD layouts (FDPS EPI / EPJ / SPJ / Force classes).             */
+
+/* DensityEPI, hdr_density.hpp:33-58 (80 bytes). */
+typedef struct sph_DensityEPI {
+    int32_t id;
+    double  mass;
+    double  pos[3];
+    double  vel[3];
+    double  ksr;   /* kernel support radius h used as the first guess */
+    double  rs;    /* search radius the j-list was built with          */
+} sph_DensityEPI;
+
+/* DensityEPJ, hdr_density.hpp:60-78 (64 bytes). */
+typedef struct sph_DensityEPJ {
+    int32_t id;
+    double  mass;
+    double  pos[3];
+    double  vel[3];
+} sph_DensityEPJ;
+
+/* Density (force), hdr_density.hpp:4-22 (56 bytes). */
+typedef struct sph_Density {
+    double  dens;
+    double  divv;
+    double  rotv;
+    double  grdh;  /* Omega = 1 / (1 + h/(3 rho) d rho/dh) */
+    double  ksr;
+    int64_t np;    /* neighbour count of the last h pass */
+    bool    itr;   /* final h exceeds the search radius rs */
+} sph_Density;
+
+/* HydroEPI, hdr_hydro.hpp:28-75 (144 bytes). */
+typedef struct sph_HydroEPI {
+    int64_t id;
+    double  pos[3];
+    double  vel[3];
+    double  ksr;
+    double  hinv;
+    double  pres;
+    double  presc;  /* P * Omega / rho^2 */
+    double  bswt;   /* 0.5 * Balsara switch */
+    double  dens;
+    double  vsnd;
+    double  alph;
+    double  alphu;
+    double  thrm;   /* max(u - umin, 0) */
+    double  eta;    /* gravity-softening correction coefficient */
+} sph_HydroEPI;
+
+/* HydroEPJ, hdr_hydro.hpp:77-126 (152 bytes). */
+typedef struct sph_HydroEPJ {
+    int64_t id;
+    double  mass;
+    double  pos[3];
+    double  vel[3];
+    double  ksr;
+    double  hinv;
+    double  pres;
+    double  presc;
+    double  bswt;
+    double  dens;
+    double  vsnd;
+    double  alph;
+    double  alphu;
+    double  thrm;
+    double  eta;
+} sph_HydroEPJ;
+
+/* Hydro (force), hdr_hydro.hpp:3-17 (72 bytes). */
+typedef struct sph_Hydro {
+    double acch[3];
+    double accg[3];
+    double udot;
+    double vsmx;
+    double diffu;
+} sph_Hydro;
+
+/* GravityEPI, hdr_gravity.hpp:130-155 (32 bytes). */
+typedef struct sph_GravityEPI {
+    double pos[3];
+    double eps2;
+} sph_GravityEPI;
+
+/* GravityEPJ, hdr_gravity.hpp:157-192 (40 bytes). */
+typedef struct sph_GravityEPJ {
+    double mass;
+    double pos[3];
+    double eps2;
+} sph_GravityEPJ;
+
+/* PS::GravitySPJ, hdr_gravity.hpp:63-91 (40 bytes). */
+typedef struct sph_GravitySPJ {
+    double mass;
+    double pos[3];
+    double eps2;
+} sph_GravitySPJ;
+
+/* Gravity (force), hdr_gravity.hpp:95-105 (40 bytes). */
+typedef struct sph_Gravity {
+    double acc[3];
+    double pot;
+    double eta;
+} sph_Gravity;
+
+/* ------------------------------------------------------------------------ */
+/* Context.                                                                  */
+
+typedef struct sph_params {
+    int32_t device;      /* CUDA device ordinal                                */
+    int32_t precision;   /* enum sph_precision                                 */
+    double  eta;         /* h = eta * ksrh * (m/rho)^(1/3); reference: 1.6
+                            (hdr_kernel.hpp:218)                              */
+    double  ksr_max;     /* KernelSupportRadiusMaximum clamp of h; 0 disables
+                            the clamp, matching ksrmax=+inf                   */
+    int32_t max_walks;   /* walks per dispatch (reference N_WALK_LIMIT=1000,
+                            use_gpu.hpp:20-26)                                */
+    int64_t max_i;       /* i-particles per dispatch (NI_LIMIT = 1e6)          */
+    int64_t max_j;       /* j entries per dispatch   (NJ_LIMIT = 1e7)          */
+    int32_t check_finite;/* non-zero: scan outputs, return SPH_ERR_NONFINITE   */
+} sph_params;
+
+typedef struct sph_context sph_context;
+
+/* Fills *p with defaults: device 0, FP32C, eta 1.6, no clamp, the reference's
+ * buffer limits, finite check on. */
+void sph_params_default(sph_params *p);
+
+/* Creates a context on p->device with one stream and buffers sized by the
+ * capacities in *p.  No counterpart call in the reference: its buffers are
+ * file-static and allocated on the first Dispatch (hdr_densityGPU.cu:486-511). */
+int  sph_context_create(const sph_params *p, sph_context **out);
+int  sph_context_destroy(sph_context *ctx);
+
+/* Updates eta / ksr_max / precision between calls (the reference re-uploads
+ * ksrmax to constant memory on every dispatch, hdr_densityGPU.cu:581). */
+int  sph_context_set_eta(sph_context *ctx, double eta);
+int  sph_context_set_ksr_max(sph_context *ctx, double ksr_max);
+int  sph_context_set_precision(sph_context *ctx, int32_t precision);
+
+/* Human-readable text for a status code (static storage). */
+const char *sph_status_string(int status);
+/* Detail text of the last failure on this context (copied into buf). */
+int  sph_context_last_error(const sph_context *ctx, char *buf, size_t n);
+
+/* ------------------------------------------------------------------------ */
+/* Single-group functors: the FDPS interaction-functor signature
+ *   operator()(const EPI *epi, S32 n_i, const EPJ *epj, S32 n_j, Force *f)
+ * with the context in front.  Synchronous.                                  */
+
+/* calcDensity::operator(), hdr_density.hpp:248-252.  Assigns force[0..n_i). */
+int sph_calc_density(sph_context *ctx,
+                     const sph_DensityEPI *epi, int32_t n_i,
+                     const sph_DensityEPJ *epj, int32_t n_j,
+                     sph_Density *force);
+
+/* calcHydro::operator(), hdr_hydro.hpp:314-318.  Assigns force[0..n_i). */
+int sph_calc_hydro(sph_context *ctx,
+                   const sph_HydroEPI *epi, int32_t n_i,
+                   const sph_HydroEPJ *epj, int32_t n_j,
+                   sph_Hydro *force);
+
+/* calcGravity<GravityEPJ>::operator(), hdr_gravity.hpp:289-293.
+ * ACCUMULATES into force[0..n_i) like the reference; clear it first. */
+int sph_calc_gravity_ep(sph_context *ctx,
+                        const sph_GravityEPI *epi, int32_t n_i,
+                        const sph_GravityEPJ *epj, int32_t n_j,
+                        sph_Gravity *force);
+
+/* calcGravity<PS::GravitySPJ>::operator() (the same template, called for the
+ * superparticles, hdr_gravity.hpp:400-402).  Accumulates. */
+int sph_calc_gravity_sp(sph_context *ctx,
+                        const sph_GravityEPI *epi, int32_t n_i,
+                        const sph_GravitySPJ *spj, int32_t n_j,
+                        sph_Gravity *force);
+
+/* ------------------------------------------------------------------------ */
+/* Batched multiwalk pairs (use_gpu.hpp:28-64).  Dispatch copies the walks to
+ * the device and launches; it returns before the kernel finishes.  Retrieve
+ * waits and writes force[w][0..n_i[w]).  Density/Hydro/Gravity results are
+ * ASSIGNED (the reference's Retrieve* assign, hdr_gravityGPU.cu:484-489).
+ * tag is accepted for signature parity; one dispatch may be outstanding per
+ * context and interaction kind. */
+
+/* DispatchKernel_Dens / RetrieveKernel_Dens, hdr_densityGPU.cu:496-621 */
+int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_walk,
+                         const sph_DensityEPI **epi, const int32_t *n_epi,
+                         const sph_DensityEPJ **epj, const int32_t *n_epj);
+int sph_retrieve_density(sph_context *ctx, int32_t tag, int32_t n_walk,
+                         const int32_t *n_i, sph_Density **force);
+
+/* DispatchKernel_HydroForce / RetrieveKernel_HydroForce,
+ * hdr_hydroGPU.cu:371-507 */
+int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
+                       const sph_HydroEPI **epi, const int32_t *n_epi,
+                       const sph_HydroEPJ **epj, const int32_t *n_epj);
+int sph_retrieve_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
+                       const int32_t *n_i, sph_Hydro **force);
+
+/* DispatchKernel_Gravity / RetrieveKernel_Gravity,
+ * hdr_gravityGPU.cu:383-495.  The j-list of walk w is its EPJ followed by its
+ * SPJ, as the reference appends them (hdr_gravityGPU.cu:445-453). */
+int sph_dispatch_gravity(sph_context *ctx, int32_t tag, int32_t n_walk,
+                         const sph_GravityEPI **epi, const int32_t *n_epi,
+                         const sph_GravityEPJ **epj, const int32_t *n_epj,
+                         const sph_GravitySPJ **spj, const int32_t *n_spj);
+int sph_retrieve_gravity(sph_context *ctx, int32_t tag, int32_t n_walk,
+                         const int32_t *n_i, sph_Gravity **force);
+
+/* ------------------------------------------------------------------------ */
+/* ABI self-description, used by the tests to check the struct layouts.
+ * Writes up to n int64 values: for each struct in the order DensityEPI,
+ * DensityEPJ, Density, HydroEPI, HydroEPJ, Hydro, GravityEPI, GravityEPJ,
+ * GravitySPJ, Gravity: sizeof followed by the byte offset of every field in
+ * declaration order.  Returns the number of values available. */
+int64_t sph_abi_layout(int64_t *out, int64_t n);
+
+/* Library version string. */
+const char *sph_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

@@ -1,0 +1,88 @@
+/*
+ * sph_oracle.h — CPU oracle for the SPH interaction path (TEST INFRASTRUCTURE).
+ *
+ * Plain scalar FP64 C restatement of the reference's CPU functors
+ * (yamauchi1132/Research_Codes, sph_yamauchi/run, USE_HELMHOLTZ build without
+ * USE_INTRINSICS).  Only the tests, the smoke check and the CPU-baseline leg of
+ * bench.py use it, always as the checker or the timed CPU reference; the
+ * product library never links it.
+ *
+ * Parity of this restatement is pinned against the reference's own functors
+ * compiled from their source (oracle/Makefile target `ref`, see ref_bridge.cpp)
+ * through the golden vectors under tests/golden/.
+ */
+#ifndef SPH_ORACLE_H
+#define SPH_ORACLE_H
+
+#include <stdint.h>
+#include "../include/sph_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Wendland C2 3-D constants, hdr_kernel.hpp:218-227. */
+#define ORACLE_KSRH  1.936492
+#define ORACLE_CEFF0 3.342253804929802286e+00
+#define ORACLE_CEFF1 1.336901521971920914e+01
+
+/* calcDensity (hdr_density.hpp:246-366).  ksr_max <= 0 disables the clamp. */
+void oracle_density(const sph_DensityEPI *epi, int32_t ni,
+                    const sph_DensityEPJ *epj, int32_t nj,
+                    sph_Density *out, double eta, double ksr_max);
+
+/* calcHydro (hdr_hydro.hpp:312-424). */
+void oracle_hydro(const sph_HydroEPI *epi, int32_t ni,
+                  const sph_HydroEPJ *epj, int32_t nj, sph_Hydro *out);
+
+/* calcGravity<TJ> (hdr_gravity.hpp:286-342), accumulating into out. */
+void oracle_gravity_ep(const sph_GravityEPI *epi, int32_t ni,
+                       const sph_GravityEPJ *epj, int32_t nj, sph_Gravity *out);
+void oracle_gravity_sp(const sph_GravityEPI *epi, int32_t ni,
+                       const sph_GravitySPJ *spj, int32_t nj, sph_Gravity *out);
+
+/* Many walks at once, OpenMP over walks (the CPU baseline's threading).
+ * Walk w owns epi[i_off[w] .. i_off[w+1]) and epj[j_off[w] .. j_off[w+1]).
+ * Gravity assigns: out is cleared per walk before the sum (as Retrieve does).
+ * nthreads <= 0 uses the OpenMP default.  Returns the thread count used. */
+int oracle_density_walks(int32_t n_walk, const int64_t *i_off, const int64_t *j_off,
+                         const sph_DensityEPI *epi, const sph_DensityEPJ *epj,
+                         sph_Density *out, double eta, double ksr_max, int nthreads);
+int oracle_hydro_walks(int32_t n_walk, const int64_t *i_off, const int64_t *j_off,
+                       const sph_HydroEPI *epi, const sph_HydroEPJ *epj,
+                       sph_Hydro *out, int nthreads);
+int oracle_gravity_walks(int32_t n_walk, const int64_t *i_off, const int64_t *j_off,
+                         const sph_GravityEPI *epi, const sph_GravityEPJ *epj,
+                         sph_Gravity *out, int nthreads);
+
+/* ---- per-particle step glue (FP64), arrays of length n ---------------- */
+
+/* Ideal-gas EOS with n = 1.5 (hdr_hgas.hpp:318-344):
+ * P = rho u / n, c = sqrt((1 + 1/n) P / rho). */
+void oracle_eos(int64_t n, const double *dens, const double *uene,
+                double *pres, double *vsnd);
+
+/* Balsara switch (hdr_sph.hpp:79-89). */
+void oracle_balsara(int64_t n, const double *divv, const double *rotv,
+                    const double *vsnd, const double *ksr, double *bswt);
+
+/* alpha / alpha_u time derivatives (hdr_hgas.hpp:750-762) with umin = 0 and
+ * EpsilonOfInternalEnergy = eps_u. */
+void oracle_alpha_dot(int64_t n, const double *divv, const double *alph,
+                      const double *alphu, const double *vsnd, const double *ksr,
+                      const double *uene, const double *diffu,
+                      double alpha_max, double alpha_min,
+                      double alphu_max, double alphu_min, double eps_u,
+                      double *adot, double *adotu);
+
+/* Per-particle time step (hdr_hgas.hpp:477-488); returns the minimum of
+ * dt_max and all particles' limits. */
+double oracle_timestep_min(int64_t n, const double *ksr, const double *vsmx,
+                           const double *divv, const double *accg,  /* n*3 */
+                           double c_dt, double dt_max);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
