@@ -1,0 +1,115 @@
+// sph_device.cuh — device helpers shared by the pair kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+// 32-byte aligned FP64 quadruple (one 256-bit load on sm_103a).
+typedef double4_32a dbl4;
+__host__ __device__ __forceinline__ dbl4 make_dbl4(double x, double y, double z, double w) {
+    return make_double4_32a(x, y, z, w);
+}
+
+namespace sphk {
+
+// Wendland C2 (3-D) constants of the reference, hdr_kernel.hpp:218-227.
+constexpr double KSRH = 1.936492;
+constexpr double CEFF0 = 3.342253804929802286e+00;
+constexpr double CEFF1 = 1.336901521971920914e+01;
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// A unit of work for the persistent pair kernels: up to 32 consecutive
+// i-particles of one walk (i-group), processed by one warp against the walk's
+// whole j-list.  x = walk, y = index of the first i-particle in the i arrays,
+// z = number of i-particles (1..32), w = cost estimate (pairs) for ordering.
+typedef int4 WorkItem;
+
+template <bool F64>
+struct Real;
+template <>
+struct Real<false> {
+    typedef float T;
+    typedef float4 T4;
+    __device__ static __forceinline__ float4 make4(float a, float b, float c, float d) {
+        return make_float4(a, b, c, d);
+    }
+};
+template <>
+struct Real<true> {
+    typedef double T;
+    typedef dbl4 T4;
+    __device__ static __forceinline__ dbl4 make4(double a, double b, double c, double d) {
+        return make_dbl4(a, b, c, d);
+    }
+};
+
+// 1/sqrt in the working precision.  FP32 uses the hardware approximation
+// (rsqrt.approx, relative error ~2^-23); FP64 the library's double rsqrt.
+__device__ __forceinline__ float rsqrt_r(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_r(double x) { return rsqrt(x); }
+
+// 1/x: FP32 via rcp.approx.ftz.f32 (relative error <= 2^-23), FP64 exact.
+__device__ __forceinline__ float rcp_r(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ double rcp_r(double x) { return 1.0 / x; }
+
+__device__ __forceinline__ float max0(float x) { return fmaxf(x, 0.0f); }
+__device__ __forceinline__ double max0(double x) { return fmax(x, 0.0); }
+
+// Compensated accumulator.  In FP32 mode a warp lane sums the pairs of one
+// 32-wide j-tile in plain FP32 and folds the tile's partial sum into a Kahan
+// pair (s, c); in FP64 mode it is a plain FP64 sum.
+template <bool F64>
+struct Acc;
+template <>
+struct Acc<false> {
+    float s, c;
+    __device__ __forceinline__ Acc() : s(0.0f), c(0.0f) {}
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <>
+struct Acc<true> {
+    double s;
+    __device__ __forceinline__ Acc() : s(0.0) {}
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+// Sum / max over the `tpi` consecutive lanes that share one i-particle
+// (tpi is a power of two <= 32; every lane of the warp must call it).
+__device__ __forceinline__ double seg_sum(double v, int tpi) {
+    for (int o = tpi >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+__device__ __forceinline__ long long seg_sum(long long v, int tpi) {
+    for (int o = tpi >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+__device__ __forceinline__ double seg_max(double v, int tpi) {
+    for (int o = tpi >> 1; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+
+// Lanes per i-particle for a work item of n_i i-particles: the largest power
+// of two with n_i * tpi <= 32.
+__device__ __forceinline__ int lanes_per_i(int n_i) {
+    int tpi = 1;
+    while (tpi < 32 && 2 * tpi * n_i <= 32) tpi <<= 1;
+    return tpi;
+}
+
+__device__ __forceinline__ int ilog2_pow2(int x) { return __ffs(x) - 1; }
+
+}  // namespace sphk

@@ -1,0 +1,61 @@
+"""C ABI checks that need no GPU: the library builds and loads, exports every
+function include/sph_gb300.h declares, and its struct layouts equal both the
+numpy mirrors and the reference classes' sizes."""
+import ctypes
+
+import pytest
+
+from research_codes_gb300 import _lib, abi
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def test_exports_every_header_function(lib):
+    names = _lib.header_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_layout_matches_numpy_mirrors(lib):
+    n = lib.sph_abi_layout(None, 0)
+    buf = (ctypes.c_int64 * n)()
+    assert lib.sph_abi_layout(buf, n) == n
+    assert list(buf) == abi.layout_vector()
+    for name, dt in abi.LAYOUT_ORDER:
+        assert dt.itemsize == abi.EXPECTED_SIZES[name], name
+
+
+def test_status_strings(lib):
+    assert lib.sph_status_string(0) == b"ok"
+    assert b"capacity" in lib.sph_status_string(abi.SPH_ERR_CAPACITY)
+    assert lib.sph_version().startswith(b"sph_gb300")
+
+
+def test_params_default(lib):
+    p = _lib.Params()
+    lib.sph_params_default(ctypes.byref(p))
+    assert (p.eta, p.max_walks, p.max_i, p.max_j) == (1.6, 1000, 1_000_000, 10_000_000)
+
+
+def test_invalid_arguments_rejected_without_device(lib):
+    h = ctypes.c_void_p()
+    p = _lib.Params()
+    lib.sph_params_default(ctypes.byref(p))
+    p.eta = -1.0
+    assert lib.sph_context_create(ctypes.byref(p), ctypes.byref(h)) == abi.SPH_ERR_INVALID_ARGUMENT
+    assert lib.sph_context_create(ctypes.byref(p), None) == abi.SPH_ERR_INVALID_ARGUMENT
+    assert lib.sph_context_destroy(None) == abi.SPH_ERR_INVALID_ARGUMENT
+    assert lib.sph_calc_density(None, None, 0, None, 0, None) == abi.SPH_ERR_INVALID_ARGUMENT
+
+
+def test_no_device_is_reported_cleanly(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert lib.sph_context_create(None, ctypes.byref(h)) == abi.SPH_ERR_NO_DEVICE
+    assert not h.value
