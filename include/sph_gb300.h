@@ -270,6 +270,106 @@ int sph_retrieve_gravity(sph_context *ctx, int32_t tag, int32_t n_walk,
                          const int32_t *n_i, sph_Gravity **force);
 
 /* ------------------------------------------------------------------------ */
+/* Device-resident particle system: the whole calcSPHKernel step on the GPU.
+ *
+ * Replaces the reference's per-step driver around the functors:
+ *   loopSimulation (hdr_hgas.hpp:1469-1542): calcTimestep (main.cpp:242-273),
+ *   predict (hdr_hgas.hpp:646-657), calcSPHKernel (main.cpp:300-358) =
+ *   calcDensityKernel (hdr_density.hpp:372-415) -> EOS (hdr_hgas.hpp:318-344)
+ *   -> Balsara (hdr_sph.hpp:79-89) -> gravity (hdr_gravity.hpp:351-423) ->
+ *   hydro -> sumAcceleration / calcAlphaDot / ksrmax (hdr_util.hpp:489-527),
+ *   correct (hdr_hgas.hpp:659-665).
+ * The tree, the i-groups and the interaction lists that FDPS builds for the
+ * reference are built on the GPU (Morton-sorted binary radix tree).  Particle
+ * state stays in HBM in Morton order between calls; uploads and downloads
+ * use the caller's (upload) order.  A step can be captured as a CUDA graph.  */
+
+typedef struct sph_system sph_system;
+
+typedef struct sph_system_params {
+    int32_t n_group;     /* max i-particles per walk (FDPS n_group, main.cpp:380: 256) */
+    int32_t n_leaf;      /* particle bucket of the tree walk (FDPS n_leaf: 8)           */
+    double  theta;       /* gravity opening angle (main.cpp:394: 0.5)                   */
+    double  G;           /* gravitational constant in code units (hdr_heos.hpp:102)     */
+    double  c_dt;        /* CoefficientOfTimestep (0.1)                                 */
+    double  dt_max;      /* MaximumTimestep (hdr_hgas.hpp:1240: 10)                     */
+    double  dt_min;      /* MinimumTimestep (1e-16)                                     */
+    double  alpha_max, alpha_min, alphu_max, alphu_min;  /* .head run parameters       */
+    int32_t ksr_max_mode;/* 0: the context's fixed ksr_max; 1: the reference rule —
+                            star-centre separation at start (hdr_hgas.hpp:1335), then
+                            the density-weighted rms radius about star 0's centre of
+                            mass after every force evaluation (hdr_util.hpp:489-527)   */
+    int32_t max_density_iterations; /* cap on search-radius expansions              */
+    int32_t use_graph;   /* capture sph_system_step's body as a CUDA graph              */
+} sph_system_params;
+
+/* Fields for sph_system_download / sph_system_download_sorted. */
+enum sph_field {
+    SPH_F_POS = 0, SPH_F_VEL = 1, SPH_F_ACC = 2, SPH_F_ACCH = 3, SPH_F_ACCG1 = 4,
+    SPH_F_ACCG2 = 5,                                  /* 3 doubles per particle */
+    SPH_F_MASS = 10, SPH_F_DENS = 11, SPH_F_PRES = 12, SPH_F_VSND = 13, SPH_F_KSR = 14,
+    SPH_F_DIVV = 15, SPH_F_ROTV = 16, SPH_F_BSWT = 17, SPH_F_GRDH = 18, SPH_F_UENE = 19,
+    SPH_F_UDOT = 20, SPH_F_ALPH = 21, SPH_F_ALPHU = 22, SPH_F_POT = 23, SPH_F_ETA = 24,
+    SPH_F_VSMX = 25, SPH_F_DIFFU = 26, SPH_F_NP = 27, SPH_F_ADOT = 28, SPH_F_ADOTU = 29,
+    SPH_F_ID = 30, SPH_F_ISTAR = 31                    /* 1 double per particle */
+};
+
+typedef struct sph_system_stats {
+    double  time, dt, ksr_max;
+    double  e_kin, e_thm, e_pot, e_tot;   /* FP64 sums, sum m(v^2/2), m u, m pot/2 */
+    int64_t n_groups;
+    int64_t density_iterations;           /* walks of the last density evaluation */
+    int64_t pairs_density;                /* sum over walks of n_i * n_j          */
+    int64_t pairs_hydro;
+    int64_t pairs_gravity;                /* particles + monopoles                */
+    int64_t list_density, list_hydro, list_gravity;  /* list entries            */
+    int64_t steps;
+    int32_t last_status;
+} sph_system_stats;
+
+void sph_system_params_default(sph_system_params *p);
+
+/* Allocates a system of n particles on the context's device. */
+int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p,
+                      sph_system **out);
+int sph_system_destroy(sph_system *sys);
+
+/* Host -> device copy of the particle state (arrays of n, pos/vel n*3).
+ * alph / alphu / istar may be null (1.0 / 0.0 / 0).  Resets time to t0. */
+int sph_system_upload(sph_system *sys, double t0, const int64_t *id, const int32_t *istar,
+                      const double *mass, const double *pos, const double *vel,
+                      const double *uene, const double *ksr, const double *alph,
+                      const double *alphu);
+
+/* calcSPHKernel on the current state (the force evaluation of
+ * startSimulation, hdr_hgas.hpp:1378): density, EOS, gravity, hydro,
+ * accelerations, alpha derivatives, ksrmax.  Fills the stats' pair counts. */
+int sph_system_compute_forces(sph_system *sys);
+
+/* n_steps iterations of the reference's loop body: time step, predict,
+ * calcSPHKernel, correct. */
+int sph_system_step(sph_system *sys, int32_t n_steps);
+
+/* Device -> host copy of one field in upload order (3 or 1 doubles each). */
+int sph_system_download(sph_system *sys, int32_t field, double *out);
+/* The same in the system's current (Morton) order, matching the lists. */
+int sph_system_download_sorted(sph_system *sys, int32_t field, double *out);
+
+int sph_system_get_stats(sph_system *sys, sph_system_stats *out);
+
+/* Interaction lists of the last force evaluation (kind 0 density — the last
+ * search-radius expansion —, 1 hydro, 2 gravity), in Morton order:
+ * walk w has i-particles [i_first[w], i_first[w] + i_count[w]) and list
+ * entries j_idx[j_off[w] .. j_off[w+1]); for gravity an entry >= n is tree
+ * node entry - n (see sph_system_get_nodes).  Call with null arrays to get
+ * *n_walk and *n_entries first. */
+int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t *n_entries,
+                         int32_t *i_first, int32_t *i_count, int64_t *j_off, int32_t *j_idx);
+
+/* Monopoles of the 2n-1 tree nodes: mom[4*k..] = (x, y, z, mass), eps2[k]. */
+int sph_system_get_nodes(sph_system *sys, double *mom, double *eps2);
+
+/* ------------------------------------------------------------------------ */
 /* ABI self-description, used by the tests to check the struct layouts.
  * Writes up to n int64 values: for each struct in the order DensityEPI,
  * DensityEPJ, Density, HydroEPI, HydroEPJ, Hydro, GravityEPI, GravityEPJ,

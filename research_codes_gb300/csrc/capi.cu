@@ -521,6 +521,7 @@ extern "C" int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_wal
         a.j_pm = ks.a4[2].p; a.j_vel = ks.a4[3].p; a.j_id = ks.id[1].p;
         a.items = (const WorkItem *)(d + L.off_items);
         a.n_items = (int)ks.items.size();
+        a.n_items_dev = nullptr;
         a.j_off = (const int *)(d + L.off_joff);
         a.j_idx = nullptr;
         a.queue = ctx->d_queue + K_DENS;
@@ -528,6 +529,7 @@ extern "C" int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_wal
         a.o_ksr = ks.o[4].p; a.o_np = ks.o_np.p; a.o_itr = ks.o_itr.p;
         a.eta_ksrh = ctx->prm.eta * sphk::KSRH;
         a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
+        a.ksr_max_dev = nullptr;
         launch_density(a, ctx->prm.precision, pair_grid(ctx, K_DENS, ctx->prm.precision, a.n_items), ctx->stream);
     }
     if (ni > 0)
@@ -588,6 +590,7 @@ extern "C" int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
         a.j_h1 = ks.a4[6].p; a.j_h2 = ks.a4[7].p; a.j_h3 = ks.a2[1].p;
         a.items = (const WorkItem *)(d + L.off_items);
         a.n_items = (int)ks.items.size();
+        a.n_items_dev = nullptr;
         a.j_off = (const int *)(d + L.off_joff);
         a.j_idx = nullptr;
         a.queue = ctx->d_queue + K_HYDRO;
@@ -655,6 +658,7 @@ extern "C" int sph_dispatch_gravity(sph_context *ctx, int32_t tag, int32_t n_wal
         a.n_split = 0x7fffffff;
         a.items = (const WorkItem *)(d + L.off_items);
         a.n_items = (int)ks.items.size();
+        a.n_items_dev = nullptr;
         a.j_off = (const int *)(d + L.off_joff);
         a.j_idx = nullptr;
         a.queue = ctx->d_queue + K_GRAV;

@@ -39,6 +39,7 @@ struct DensityArgs {
     // work
     const WorkItem *items;
     int n_items;
+    const int *n_items_dev; // when set, the item count is read from device memory
     const int *j_off;       // per walk: [j_off[w], j_off[w+1]) in j index space
     const int *j_idx;       // null: entries are j indices themselves
     int *queue;             // item counter, 0 at launch
@@ -48,6 +49,7 @@ struct DensityArgs {
     unsigned char *o_itr;
     double eta_ksrh;        // eta * ksrh
     double ksr_max;         // clamp of h (+inf disables)
+    const double *ksr_max_dev;  // when set, the clamp is read from device memory
 };
 
 template <bool F64, int WARPS>
@@ -60,12 +62,13 @@ density_kernel(const DensityArgs a) {
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
+    const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
 
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.queue, 1);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= a.n_items) return;
+        if (item >= n_items) return;
         const WorkItem it = a.items[item];
         const int jb = a.j_off[it.x];
         const int nj = a.j_off[it.x + 1] - jb;
@@ -89,6 +92,7 @@ density_kernel(const DensityArgs a) {
         const R vxi = (R)(vi.x - cvx), vyi = (R)(vi.y - cvy), vzi = (R)(vi.z - cvz);
         const long long idi = a.i_id[ii];
         const double rs_i = a.i_rs[ii];
+        const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
         double h = a.i_ksr[ii];
         double rho = 0.0;
         long long np = 0;
@@ -128,7 +132,7 @@ density_kernel(const DensityArgs a) {
             const long long c = seg_sum((long long)cnt, tpi);
             rho = CEFF0 * hinv_d * hinv_d * hinv_d * sum;
             double hn = a.eta_ksrh * cbrt(pi.w / rho);
-            hn = (hn < a.ksr_max) ? hn : a.ksr_max;
+            hn = (hn < ksr_max) ? hn : ksr_max;
             np = c;
             itr = hn > rs_i;
             h = hn;
@@ -223,6 +227,7 @@ struct HydroArgs {
     const double2 *j_h3;
     const WorkItem *items;
     int n_items;
+    const int *n_items_dev;
     const int *j_off;
     const int *j_idx;
     int *queue;
@@ -245,12 +250,13 @@ hydro_kernel(const HydroArgs a) {
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
+    const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
 
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.queue, 1);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= a.n_items) return;
+        if (item >= n_items) return;
         const WorkItem it = a.items[item];
         const int jb = a.j_off[it.x];
         const int nj = a.j_off[it.x + 1] - jb;
@@ -394,6 +400,7 @@ struct GravityArgs {
     int n_split;
     const WorkItem *items;
     int n_items;
+    const int *n_items_dev;
     const int *j_off;
     const int *j_idx;
     int *queue;
@@ -410,12 +417,13 @@ gravity_kernel(const GravityArgs a) {
     __shared__ R s_e[WARPS][32];    // eps2
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
+    const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
 
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.queue, 1);
         item = __shfl_sync(FULL, item, 0);
-        if (item >= a.n_items) return;
+        if (item >= n_items) return;
         const WorkItem it = a.items[item];
         const int jb = a.j_off[it.x];
         const int nj = a.j_off[it.x + 1] - jb;

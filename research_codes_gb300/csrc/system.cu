@@ -1,0 +1,1297 @@
+// system.cu — the device-resident particle system: the reference's step loop
+// (calcTimestep -> predict -> calcSPHKernel -> correct) entirely on the GPU,
+// with the tree / list builder of tree.cuh standing in for FDPS and the pair
+// kernels of pair_kernels.cuh doing the interactions.  Every launch reads its
+// counts from device memory, so a whole step can be captured as a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <vector>
+
+#include <cub/cub.cuh>
+
+#include "../../include/sph_gb300.h"
+#include "capi_internal.h"
+#include "pair_kernels.cuh"
+#include "tree.cuh"
+
+using sphk::WorkItem;
+using sphrt::DevBuf;
+using sphrt::HostBuf;
+
+namespace {
+
+constexpr double KSRH = sphk::KSRH;
+constexpr int RED_BLOCKS = 296;   // 2 x 148..152 SMs; fixed for deterministic sums
+constexpr int RED_THREADS = 256;
+constexpr int MAX_RED = 8;
+
+// int scalars
+enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_NI };
+// double scalars
+enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
+       D_R2, D_DN, D_NI };
+// 64-bit counters
+enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_NI };
+// error bits
+enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
+
+inline int grid_for(long long n, int threads = 256) {
+    long long b = (n + threads - 1) / threads;
+    return (int)std::max(1LL, std::min(b, 8192LL));
+}
+
+#define GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+// ---------------------------------------------------------------- reductions
+// Two-stage deterministic reduction: RED_BLOCKS partials in a fixed order,
+// then one block adds them in index order.
+template <class F>
+__global__ void __launch_bounds__(RED_THREADS) reduce_stage1(int n, F f, double *partial) {
+    __shared__ double sh[MAX_RED][RED_THREADS];
+    double acc[MAX_RED];
+    for (int k = 0; k < F::K; ++k) acc[k] = F::identity();
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) f(p, acc);
+    for (int k = 0; k < F::K; ++k) sh[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int k = 0; k < F::K; ++k) sh[k][threadIdx.x] = F::op(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x < F::K) partial[blockIdx.x * MAX_RED + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+template <class F>
+__global__ void reduce_stage2(const double *partial, int nb, double *out) {
+    const int k = threadIdx.x;
+    if (k >= F::K) return;
+    double a = F::identity();
+    for (int b = 0; b < nb; ++b) a = F::op(a, partial[b * MAX_RED + k]);
+    out[k] = a;
+}
+
+struct SumOp {
+    __device__ static double identity() { return 0.0; }
+    __device__ static double op(double a, double b) { return a + b; }
+};
+struct MinOp {
+    __device__ static double identity() { return 1.0e300; }
+    __device__ static double op(double a, double b) { return fmin(a, b); }
+};
+
+// centre of mass of star 0 (hdr_util.hpp:8-34 with istar = 0)
+struct Star0Com : SumOp {
+    static constexpr int K = 4;
+    const dbl4 *pos;
+    const int *istar;
+    __device__ void operator()(int p, double *a) const {
+        if (istar[p] != 0) return;
+        const dbl4 x = pos[p];
+        a[0] += x.w * x.x;
+        a[1] += x.w * x.y;
+        a[2] += x.w * x.z;
+        a[3] += x.w;
+    }
+};
+
+// density-weighted r^2 about star 0's centre, over all particles (hdr_util.hpp:497-505)
+struct KsrMaxSums : SumOp {
+    static constexpr int K = 2;
+    const dbl4 *pos;
+    const double *dens;
+    const double *xc;   // D_XC.. (already divided by mass)
+    __device__ void operator()(int p, double *a) const {
+        const dbl4 x = pos[p];
+        const double dx = x.x - xc[0], dy = x.y - xc[1], dz = x.z - xc[2];
+        a[0] += dens[p] * (dx * dx + dy * dy + dz * dz);
+        a[1] += dens[p];
+    }
+};
+
+// per-particle time step, hdr_hgas.hpp:477-488
+struct TimestepMin : MinOp {
+    static constexpr int K = 1;
+    const double *ksr, *vsmx, *divv, *accg1, *accg2;
+    double c_dt, dt_max;
+    __device__ void operator()(int p, double *a) const {
+        const double dth = c_dt * ksr[p] / (vsmx[p] * KSRH);
+        const double dtd = (divv[p] < 0.0) ? (-c_dt / divv[p]) : dt_max;
+        const double gx = accg1[3 * p] + accg2[3 * p], gy = accg1[3 * p + 1] + accg2[3 * p + 1],
+                     gz = accg1[3 * p + 2] + accg2[3 * p + 2];
+        const double dtg = c_dt * sqrt(ksr[p] / sqrt(gx * gx + gy * gy + gz * gz));
+        const double d = fmin(fmin(dth, dt_max), fmin(dtg, dtd));
+        a[0] = fmin(a[0], d);
+    }
+};
+
+// energy parts, hdr_hgas.hpp:630-634
+struct Energy : SumOp {
+    static constexpr int K = 3;
+    const dbl4 *pos, *vel;
+    const double *uene, *pot;
+    __device__ void operator()(int p, double *a) const {
+        const double m = pos[p].w;
+        const dbl4 v = vel[p];
+        a[0] += 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
+        a[1] += m * uene[p];
+        a[2] += 0.5 * m * pot[p];
+    }
+};
+
+struct UeneMin : MinOp {
+    static constexpr int K = 1;
+    const double *uene;
+    __device__ void operator()(int p, double *a) const { a[0] = fmin(a[0], uene[p]); }
+};
+
+struct StarComs : SumOp {    // both stars' centres (calcSystemSize, hdr_util.hpp:95-113)
+    static constexpr int K = 8;
+    const dbl4 *pos;
+    const int *istar;
+    __device__ void operator()(int p, double *a) const {
+        const dbl4 x = pos[p];
+        const int o = istar[p] == 0 ? 0 : 4;
+        if (istar[p] > 1) return;
+        a[o + 0] += x.w * x.x;
+        a[o + 1] += x.w * x.y;
+        a[o + 2] += x.w * x.z;
+        a[o + 3] += x.w;
+    }
+};
+
+// ---------------------------------------------------------------- small kernels
+__global__ void bbox_stage1(const dbl4 *pos, int n, double *partial) {
+    __shared__ double sh[6][RED_THREADS];
+    double b[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const dbl4 x = pos[p];
+        b[0] = fmin(b[0], x.x); b[1] = fmin(b[1], x.y); b[2] = fmin(b[2], x.z);
+        b[3] = fmax(b[3], x.x); b[4] = fmax(b[4], x.y); b[5] = fmax(b[5], x.z);
+    }
+    for (int k = 0; k < 6; ++k) sh[k][threadIdx.x] = b[k];
+    __syncthreads();
+    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] = fmin(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
+            for (int k = 3; k < 6; ++k) sh[k][threadIdx.x] = fmax(sh[k][threadIdx.x], sh[k][threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) partial[blockIdx.x * MAX_RED + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void bbox_stage2(const double *partial, int nb, double *box) {
+    const int k = threadIdx.x;
+    if (k >= 6) return;
+    double a = (k < 3) ? 1e300 : -1e300;
+    for (int b = 0; b < nb; ++b) a = (k < 3) ? fmin(a, partial[b * MAX_RED + k]) : fmax(a, partial[b * MAX_RED + k]);
+    box[k] = a;
+}
+
+struct Persist {          // state carried across steps (permuted on each re-sort)
+    dbl4 *pos, *vel, *vel2;
+    long long *id;
+    int *istar, *orig;
+    double *uene, *uene2, *alph, *alph2, *alphu, *alphu2, *ksr;
+};
+
+__global__ void permute(int n, const int *idx, Persist src, Persist dst) {
+    GRID_STRIDE(p, n) {
+        const int q = idx[p];
+        dst.pos[p] = src.pos[q];
+        dst.vel[p] = src.vel[q];
+        dst.vel2[p] = src.vel2[q];
+        dst.id[p] = src.id[q];
+        dst.istar[p] = src.istar[q];
+        dst.orig[p] = src.orig[q];
+        dst.uene[p] = src.uene[q];
+        dst.uene2[p] = src.uene2[q];
+        dst.alph[p] = src.alph[q];
+        dst.alph2[p] = src.alph2[q];
+        dst.alphu[p] = src.alphu[q];
+        dst.alphu2[p] = src.alphu2[q];
+        dst.ksr[p] = src.ksr[q];
+    }
+}
+
+__global__ void eps2_from_h(int n, const double *h, double *eps2) {
+    GRID_STRIDE(p, n) { eps2[p] = (h[p] / KSRH) * (h[p] / KSRH); }
+}
+
+// compact group roots: position-indexed flags -> group arrays
+__global__ void compact_groups(int n, const int *flag, const int *scan, const int *root_at,
+                               sphtree::Nodes t, int *group_node, int *group_first, int *group_count,
+                               int *scal) {
+    GRID_STRIDE(p, n) {
+        if (flag[p]) {
+            const int g = scan[p];
+            const int v = root_at[p];
+            group_node[g] = v;
+            group_first[g] = p;
+            group_count[g] = t.count[v];
+        }
+        if (p == n - 1) scal[S_NGROUPS] = scan[p] + flag[p];
+    }
+}
+
+// one warp per group: max rs over the members that are still iterating
+__global__ void group_rs_max(const int *scal, const int *group_first, const int *group_count,
+                             const double *rs, double *rmax, int *active_flag) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    const int ng = scal[S_NGROUPS];
+    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < ng; g += warps) {
+        double m = 0.0;
+        for (int k = lane; k < group_count[g]; k += 32) m = fmax(m, rs[group_first[g] + k]);
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) {
+            rmax[g] = m;
+            active_flag[g] = m > 0.0 ? 1 : 0;
+        }
+    }
+}
+
+__global__ void compact_active(int n, const int *scal, const int *flag, const int *scan,
+                               const int *group_node, const int *group_first, const int *group_count,
+                               const double *rmax, int *a_node, int *a_first, int *a_count, double *a_r,
+                               int *scal_out) {
+    const int ng = scal[S_NGROUPS];
+    GRID_STRIDE(g, n) {
+        if (g < ng && flag[g]) {
+            const int k = scan[g];
+            a_node[k] = group_node[g];
+            a_first[k] = group_first[g];
+            a_count[k] = group_count[g];
+            a_r[k] = rmax[g];
+        }
+        if (g == n - 1) scal_out[S_NACTIVE] = scan[g] + flag[g];
+    }
+}
+
+__global__ void set_int(int *p, int v) { *p = v; }
+__global__ void copy_int(const int *src, int *dst) { *dst = *src; }
+
+// list totals: offset[n-1] + count[n-1] (counts beyond the walk count are 0)
+__global__ void list_total(int n, const int *cnt, const int *off, long long cap, int *scal, long long *lscal,
+                           int lslot) {
+    const long long tot = (long long)off[n - 1] + cnt[n - 1];
+    scal[S_TOTAL] = (int)min(tot, (long long)0x7fffffff);
+    lscal[lslot] = tot;
+    if (tot > cap) atomicOr(&scal[S_ERROR], E_LISTCAP);
+}
+
+// work items: walk k gets ceil(n_i/32) items
+__global__ void item_counts(int n, const int *n_walks, const int *i_count, int *c) {
+    const int nw = *n_walks;
+    GRID_STRIDE(k, n) { c[k] = (k < nw) ? (i_count[k] + 31) / 32 : 0; }
+}
+
+__global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count,
+                           const int *item_off, const int *item_cnt, const int *j_off, const int *j_cnt,
+                           WorkItem *items, int *n_items, long long *pairs) {
+    const int nw = *n_walks;
+    long long local = 0;
+    GRID_STRIDE(k, n) {
+        if (k < nw) {
+            const int base = item_off[k];
+            const int ni = i_count[k];
+            const int nj = j_cnt[k];
+            for (int c = 0; c < item_cnt[k]; ++c) {
+                const int chunk = min(32, ni - 32 * c);
+                items[base + c] = make_int4(k, i_first[k] + 32 * c, chunk, nj * chunk);
+            }
+            local += (long long)ni * nj;
+        }
+        if (k == n - 1) *n_items = item_off[k] + item_cnt[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd((unsigned long long *)pairs, (unsigned long long)local);
+}
+
+__global__ void init_rs(int n, const double *ksr, double *rs) {
+    GRID_STRIDE(p, n) { rs[p] = 1.1 * ksr[p]; }   // hdr_density.hpp:376-379
+}
+
+struct DensOut {
+    double *dens, *divv, *rotv, *grdh, *ksr;
+    long long *np;
+    unsigned char *itr;
+};
+
+// hdr_density.hpp:401-411: converged particles take the result and get rs = 0,
+// the others expand rs by 1.1 and stay in the iteration.
+__global__ void commit_density(int n, double *rs, DensOut tmp, DensOut st, int *scal) {
+    int local = 0;
+    GRID_STRIDE(p, n) {
+        if (rs[p] != 0.0) {
+            if (tmp.itr[p]) {
+                rs[p] *= 1.1;
+                local = 1;
+            } else {
+                rs[p] = 0.0;
+                st.dens[p] = tmp.dens[p];
+                st.divv[p] = tmp.divv[p];
+                st.rotv[p] = tmp.rotv[p];
+                st.grdh[p] = tmp.grdh[p];
+                st.ksr[p] = tmp.ksr[p];
+                st.np[p] = tmp.np[p];
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, local) && (threadIdx.x & 31) == 0) atomicAdd(&scal[S_UNCONV], 1);
+}
+
+__global__ void iteration_end(int *scal, int max_it, int it) {
+    if (scal[S_UNCONV] > 0) {
+        scal[S_ITERS] = it + 2;
+        if (it + 1 >= max_it) atomicOr(&scal[S_ERROR], E_NOTCONV);
+    }
+    scal[S_UNCONV] = 0;
+}
+
+// EOS (hdr_hgas.hpp:339-342), Balsara (hdr_sph.hpp:79-81), softening eps^2
+__global__ void post_density(int n, const dbl4 *pos, const double *dens, const double *uene,
+                             const double *divv, const double *rotv, const double *ksr, double *pres,
+                             double *vsnd, double *bswt, double *eps2, dbl4 *pe) {
+    const double ninv = 1.0 / 1.5;
+    GRID_STRIDE(p, n) {
+        const double P = ninv * dens[p] * uene[p];
+        const double c = sqrt((1.0 + ninv) * P / dens[p]);
+        pres[p] = P;
+        vsnd[p] = c;
+        const double ad = fabs(divv[p]);
+        bswt[p] = ad / (ad + fabs(rotv[p]) + 1e-4 * c * KSRH / ksr[p]);
+        const double e2 = (ksr[p] / KSRH) * (ksr[p] / KSRH);
+        eps2[p] = e2;
+        const dbl4 x = pos[p];
+        pe[p] = make_dbl4(x.x, x.y, x.z, e2);
+    }
+}
+
+// Gravity write-back, hdr_gravity.hpp:107-113
+__global__ void gravity_writeback(int n, double G, const double *acc, const double *pot, const double *etas,
+                                  const double *ksr, const double *grdh, const double *dens, double *accg2,
+                                  double *pot_out, double *eta_out) {
+    GRID_STRIDE(p, n) {
+        for (int c = 0; c < 3; ++c) accg2[3 * p + c] = G * acc[3 * p + c];
+        eta_out[p] = ksr[p] * ksr[p] / (KSRH * KSRH) * grdh[p] / (3.0 * dens[p]) * etas[p];
+        pot_out[p] = G * pot[p];
+    }
+}
+
+// HydroEPI/EPJ::copyFromFP, hdr_hydro.hpp:45-62 / 95-113 (umin = 0)
+__global__ void hydro_prep(int n, const double *ksr, const double *pres, const double *grdh,
+                           const double *dens, const double *bswt, const double *vsnd, const double *alph,
+                           const double *alphu, const double *uene, const double *eta, dbl4 *h1, dbl4 *h2,
+                           double2 *h3) {
+    GRID_STRIDE(p, n) {
+        h1[p] = make_dbl4(1.0 / ksr[p], pres[p], pres[p] * grdh[p] / (dens[p] * dens[p]), 0.5 * bswt[p]);
+        h2[p] = make_dbl4(dens[p], vsnd[p], alph[p], alphu[p]);
+        h3[p] = make_double2(fmax(uene[p] - 0.0, 0.0), eta[p]);
+    }
+}
+
+struct AlphaParams {
+    double amax, amin, aumax, aumin;
+};
+
+// Hydro write-back (hdr_hydro.hpp:19-26), sumAcceleration (hdr_sph.hpp:95-97),
+// calcAlphaDot (hdr_hgas.hpp:750-762)
+__global__ void hydro_writeback(int n, double G, const double *acch_r, const double *accg_r,
+                                const double *udot_r, const double *vsmx_r, const double *diffu_r,
+                                double *acch, double *accg1, const double *accg2, double *acc, double *udot,
+                                double *vsmx, double *diffu, const double *divv, const double *alph,
+                                const double *alphu, const double *vsnd, const double *ksr,
+                                const double *uene, const double *epsu, AlphaParams ap, double *adot,
+                                double *adotu) {
+    GRID_STRIDE(p, n) {
+        for (int c = 0; c < 3; ++c) {
+            const double h = acch_r[3 * p + c];
+            const double g1 = G * accg_r[3 * p + c];
+            acch[3 * p + c] = h;
+            accg1[3 * p + c] = g1;
+            acc[3 * p + c] = h + g1 + accg2[3 * p + c];
+        }
+        udot[p] = udot_r[p];
+        vsmx[p] = vsmx_r[p];
+        const double df = diffu_r[p];
+        diffu[p] = df;
+        const double src = fmax(-divv[p] * (ap.amax - alph[p]), 0.0);
+        const double tauinv = (0.25 * KSRH * vsnd[p]) / ksr[p];
+        adot[p] = -(alph[p] - ap.amin) * tauinv + src;
+        const double u = fmax(uene[p] - 0.0, 0.0);
+        const double srcu = ksr[p] / KSRH * fabs(df) / sqrt(u + *epsu) * fmax(ap.aumax - alphu[p], 0.0);
+        adotu[p] = -(alphu[p] - ap.aumin) * tauinv + srcu;
+    }
+}
+
+__global__ void finish_ksrmax(double *dsc, int mode) {
+    // dsc[D_XC..D_MC] hold mass-weighted sums; dsc[D_R2], dsc[D_DN] the rho sums
+    if (mode == 1 && dsc[D_DN] > 0.0) dsc[D_KSRMAX] = sqrt(dsc[D_R2] / dsc[D_DN]);
+}
+
+__global__ void com_divide(double *dsc) {
+    const double m = dsc[D_MC];
+    if (m > 0.0) {
+        dsc[D_XC] /= m;
+        dsc[D_YC] /= m;
+        dsc[D_ZC] /= m;
+    }
+}
+
+// calcTimestep's power-of-two adjustment, main.cpp:252-270
+__global__ void update_dt(double *dsc, int *scal, double dt_max, double dt_min) {
+    const double dtc = dsc[D_DTC];
+    double dt = dsc[D_DT];
+    const double t = dsc[D_TIME];
+    if (dt > dtc) {
+        while (dt > dtc) {
+            dt *= 0.5;
+            if (dt <= dt_min) {
+                atomicOr(&scal[S_ERROR], E_DTMIN);
+                break;
+            }
+        }
+    } else if (2.0 * dt <= dtc && 2.0 * dt <= dt_max) {
+        const double dt2 = 2.0 * dt;
+        if (t - (double)(long long)(t / dt2) * dt2 == 0.0) dt *= 2.0;
+    }
+    dsc[D_DT] = dt;
+}
+
+// predict, hdr_hgas.hpp:646-657 (dnuc = 0, gcor3 = 0)
+__global__ void predict(int n, const double *dsc, dbl4 *pos, dbl4 *vel, dbl4 *vel2, const double *acc,
+                        double *uene, double *uene2, const double *udot, double *alph, double *alph2,
+                        const double *adot, double *alphu, double *alphu2, const double *adotu) {
+    const double dt = dsc[D_DT];
+    GRID_STRIDE(p, n) {
+        dbl4 x = pos[p];
+        dbl4 v = vel[p];
+        const double ax = acc[3 * p], ay = acc[3 * p + 1], az = acc[3 * p + 2];
+        x.x = x.x + v.x * dt + 0.5 * ax * dt * dt;
+        x.y = x.y + v.y * dt + 0.5 * ay * dt * dt;
+        x.z = x.z + v.z * dt + 0.5 * az * dt * dt;
+        pos[p] = x;
+        vel2[p] = make_dbl4(v.x + 0.5 * ax * dt, v.y + 0.5 * ay * dt, v.z + 0.5 * az * dt, 0.0);
+        vel[p] = make_dbl4(v.x + ax * dt, v.y + ay * dt, v.z + az * dt, 0.0);
+        uene2[p] = uene[p] + 0.5 * udot[p] * dt;
+        uene[p] = uene[p] + udot[p] * dt;
+        alph2[p] = alph[p] + 0.5 * adot[p] * dt;
+        alph[p] = alph[p] + adot[p] * dt;
+        alphu2[p] = alphu[p] + 0.5 * adotu[p] * dt;
+        alphu[p] = alphu[p] + adotu[p] * dt;
+    }
+}
+
+// correct, hdr_hgas.hpp:659-665
+__global__ void correct(int n, const double *dsc, dbl4 *vel, const dbl4 *vel2, const double *acc,
+                        double *uene, const double *uene2, const double *udot, double *alph,
+                        const double *alph2, const double *adot, double *alphu, const double *alphu2,
+                        const double *adotu) {
+    const double dt = dsc[D_DT];
+    GRID_STRIDE(p, n) {
+        const dbl4 v2 = vel2[p];
+        vel[p] = make_dbl4(v2.x + 0.5 * acc[3 * p] * dt, v2.y + 0.5 * acc[3 * p + 1] * dt,
+                           v2.z + 0.5 * acc[3 * p + 2] * dt, 0.0);
+        uene[p] = uene2[p] + 0.5 * udot[p] * dt;
+        alph[p] = alph2[p] + 0.5 * adot[p] * dt;
+        alphu[p] = alphu2[p] + 0.5 * adotu[p] * dt;
+    }
+}
+
+__global__ void advance_time(double *dsc) { dsc[D_TIME] += dsc[D_DT]; }
+
+__global__ void scatter_field(int n, int width, const int *orig, const double *src, double *dst) {
+    GRID_STRIDE(p, n) {
+        const int q = orig[p];
+        for (int c = 0; c < width; ++c) dst[(size_t)q * width + c] = src[(size_t)p * width + c];
+    }
+}
+
+__global__ void field_from_dbl4(int n, const dbl4 *src, int comp, double *dst) {
+    GRID_STRIDE(p, n) {
+        const dbl4 v = src[p];
+        if (comp < 0) {
+            dst[3 * p] = v.x;
+            dst[3 * p + 1] = v.y;
+            dst[3 * p + 2] = v.z;
+        } else {
+            dst[p] = comp == 3 ? v.w : (comp == 0 ? v.x : (comp == 1 ? v.y : v.z));
+        }
+    }
+}
+
+template <class T>
+__global__ void field_to_double(int n, const T *src, double *dst) {
+    GRID_STRIDE(p, n) { dst[p] = (double)src[p]; }
+}
+
+__global__ void upload_pack(int n, const double *mass, const double *pos, const double *vel, dbl4 *opos,
+                            dbl4 *ovel, dbl4 *ovel2) {
+    GRID_STRIDE(p, n) {
+        opos[p] = make_dbl4(pos[3 * p], pos[3 * p + 1], pos[3 * p + 2], mass[p]);
+        ovel[p] = make_dbl4(vel[3 * p], vel[3 * p + 1], vel[3 * p + 2], 0.0);
+        ovel2[p] = ovel[p];
+    }
+}
+
+__global__ void iota(int n, int *a) {
+    GRID_STRIDE(p, n) { a[p] = p; }
+}
+
+__global__ void fill_double(int n, double *a, double v) {
+    GRID_STRIDE(p, n) { a[p] = v; }
+}
+
+}  // namespace
+
+// ======================================================================= system
+struct sph_system {
+    sph_context *ctx = nullptr;
+    int n = 0;
+    sph_system_params prm;
+    // persistent state (A) and permutation target (B)
+    DevBuf<dbl4> pos[2], vel[2], vel2[2];
+    DevBuf<long long> id[2];
+    DevBuf<int> istar[2], orig[2];
+    DevBuf<double> uene[2], uene2[2], alph[2], alph2[2], alphu[2], alphu2[2], ksr[2];
+    // per-step state
+    DevBuf<double> rs, dens, divv, rotv, grdh, pres, vsnd, bswt, eps2, udot, vsmx, diffu, pot, eta, adot,
+        adotu;
+    DevBuf<long long> np;
+    DevBuf<dbl4> pe, h1, h2;
+    DevBuf<double2> h3;
+    DevBuf<double> acc, acch, accg1, accg2;
+    DevBuf<double> t_dens, t_divv, t_rotv, t_grdh, t_ksr;
+    DevBuf<long long> t_np;
+    DevBuf<unsigned char> t_itr;
+    DevBuf<double> r_acc, r_pot, r_eta, r_acch, r_accg, r_udot, r_vsmx, r_diffu;
+    // tree
+    DevBuf<uint64_t> keys[2];
+    DevBuf<int> perm[2];
+    DevBuf<int2> child;
+    DevBuf<int> parent, first, count, visit;
+    DevBuf<dbl4> lo, hi, mom;
+    DevBuf<double> neps2;
+    // groups and walks
+    DevBuf<int> gflag, groot, gscan, group_node, group_first, group_count;
+    DevBuf<int> aflag, ascan, a_node, a_first, a_count;
+    DevBuf<double> g_r, a_r;
+    // lists per kind (0 density, 1 hydro, 2 gravity)
+    DevBuf<int> lcnt[3], loff[3], jidx[3];
+    long long lcap[3] = {0, 0, 0};
+    int *walk_first[3] = {nullptr, nullptr, nullptr};
+    int *walk_count[3] = {nullptr, nullptr, nullptr};
+    int *walk_num[3] = {nullptr, nullptr, nullptr};   // device count of walks
+    DevBuf<int> icnt, ioff;
+    DevBuf<WorkItem> items;
+    // scalars
+    DevBuf<int> scal;
+    DevBuf<double> dscal, partial, box;
+    DevBuf<long long> lscal;
+    HostBuf<int> h_scal;
+    HostBuf<double> h_dscal;
+    HostBuf<long long> h_lscal;
+    DevBuf<double> staging;
+    DevBuf<char> cub_tmp;
+    size_t cub_bytes = 0;
+    // graph
+    cudaGraphExec_t step_exec = nullptr;
+    bool graph_valid = false;
+    long long steps = 0;
+    int last_status = 0;
+
+    cudaStream_t st() const { return ctx->stream; }
+    Persist persist(int k) {
+        Persist p;
+        p.pos = pos[k].p; p.vel = vel[k].p; p.vel2 = vel2[k].p; p.id = id[k].p; p.istar = istar[k].p;
+        p.orig = orig[k].p; p.uene = uene[k].p; p.uene2 = uene2[k].p; p.alph = alph[k].p;
+        p.alph2 = alph2[k].p; p.alphu = alphu[k].p; p.alphu2 = alphu2[k].p; p.ksr = ksr[k].p;
+        return p;
+    }
+    sphtree::Nodes nodes() {
+        sphtree::Nodes t;
+        t.child = child.p; t.parent = parent.p; t.first = first.p; t.count = count.p; t.lo = lo.p;
+        t.hi = hi.p; t.mom = mom.p; t.eps2 = neps2.p; t.visit = visit.p;
+        return t;
+    }
+};
+
+namespace {
+
+int alloc_all(sph_system *s) {
+    const size_t n = (size_t)s->n;
+    const size_t nn = 2 * n;
+    int e = 0;
+    for (int k = 0; k < 2; ++k) {
+        e |= s->pos[k].ensure(n) | s->vel[k].ensure(n) | s->vel2[k].ensure(n) | s->id[k].ensure(n);
+        e |= s->istar[k].ensure(n) | s->orig[k].ensure(n) | s->uene[k].ensure(n) | s->uene2[k].ensure(n);
+        e |= s->alph[k].ensure(n) | s->alph2[k].ensure(n) | s->alphu[k].ensure(n) | s->alphu2[k].ensure(n);
+        e |= s->ksr[k].ensure(n) | s->keys[k].ensure(n) | s->perm[k].ensure(n);
+    }
+    DevBuf<double> *d1[] = {&s->rs, &s->dens, &s->divv, &s->rotv, &s->grdh, &s->pres, &s->vsnd, &s->bswt,
+                            &s->eps2, &s->udot, &s->vsmx, &s->diffu, &s->pot, &s->eta, &s->adot, &s->adotu,
+                            &s->t_dens, &s->t_divv, &s->t_rotv, &s->t_grdh, &s->t_ksr, &s->r_pot, &s->r_eta,
+                            &s->r_udot, &s->r_vsmx, &s->r_diffu, &s->g_r, &s->a_r};
+    for (auto *b : d1) e |= b->ensure(n);
+    DevBuf<double> *d3[] = {&s->acc, &s->acch, &s->accg1, &s->accg2, &s->r_acc, &s->r_acch, &s->r_accg,
+                            &s->staging};
+    for (auto *b : d3) e |= b->ensure(3 * n);
+    e |= s->np.ensure(n) | s->t_np.ensure(n) | s->t_itr.ensure(n);
+    e |= s->pe.ensure(n) | s->h1.ensure(n) | s->h2.ensure(n) | s->h3.ensure(n);
+    e |= s->child.ensure(n) | s->parent.ensure(nn) | s->first.ensure(nn) | s->count.ensure(nn);
+    e |= s->visit.ensure(n) | s->lo.ensure(nn) | s->hi.ensure(nn) | s->mom.ensure(nn) | s->neps2.ensure(nn);
+    DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
+                         &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff};
+    for (auto *b : i1) e |= b->ensure(n);
+    for (int k = 0; k < 3; ++k) e |= s->lcnt[k].ensure(n) | s->loff[k].ensure(n);
+    e |= s->items.ensure(n);
+    e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
+    e |= s->partial.ensure(RED_BLOCKS * MAX_RED) | s->box.ensure(8);
+    e |= s->h_scal.ensure(S_NI) | s->h_dscal.ensure(D_NI) | s->h_lscal.ensure(L_NI);
+    // CUB scratch: radix sort of (uint64, int) pairs and exclusive sums over n ints
+    size_t b1 = 0, b2 = 0;
+    cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
+    cub::DoubleBuffer<int> vb(s->perm[0].p, s->perm[1].p);
+    cub::DeviceRadixSort::SortPairs(nullptr, b1, kb, vb, s->n, 0, 63);
+    cub::DeviceScan::ExclusiveSum(nullptr, b2, s->gflag.p, s->gscan.p, s->n);
+    s->cub_bytes = std::max(b1, b2);
+    e |= s->cub_tmp.ensure(s->cub_bytes);
+    s->walk_first[0] = s->a_first.p; s->walk_count[0] = s->a_count.p; s->walk_num[0] = s->scal.p + S_NACTIVE;
+    s->walk_first[1] = s->group_first.p; s->walk_count[1] = s->group_count.p; s->walk_num[1] = s->scal.p + S_NGROUPS;
+    s->walk_first[2] = s->group_first.p; s->walk_count[2] = s->group_count.p; s->walk_num[2] = s->scal.p + S_NGROUPS;
+    return e;
+}
+
+#define CUDA_TRY(x)                                                   \
+    do {                                                              \
+        cudaError_t e__ = (x);                                        \
+        if (e__ != cudaSuccess) return sphrt::cuda_error(s->ctx, e__, #x); \
+    } while (0)
+
+int exclusive_scan(sph_system *s, const int *in, int *out) {
+    size_t bytes = s->cub_bytes;
+    CUDA_TRY(cub::DeviceScan::ExclusiveSum(s->cub_tmp.p, bytes, in, out, s->n, s->st()));
+    return SPH_OK;
+}
+
+template <class F>
+void reduce(sph_system *s, F f, double *out) {
+    reduce_stage1<F><<<RED_BLOCKS, RED_THREADS, 0, s->st()>>>(s->n, f, s->partial.p);
+    reduce_stage2<F><<<1, 32, 0, s->st()>>>(s->partial.p, RED_BLOCKS, out);
+}
+
+// Morton sort + permutation + radix tree + refit + groups.
+int build_tree(sph_system *s) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    bbox_stage1<<<RED_BLOCKS, RED_THREADS, 0, st>>>(s->pos[0].p, n, s->partial.p);
+    bbox_stage2<<<1, 32, 0, st>>>(s->partial.p, RED_BLOCKS, s->box.p);
+    sphtree::morton_keys<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, n, s->box.p, s->keys[0].p, s->perm[0].p);
+    cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
+    cub::DoubleBuffer<int> vb(s->perm[0].p, s->perm[1].p);
+    size_t bytes = s->cub_bytes;
+    CUDA_TRY(cub::DeviceRadixSort::SortPairs(s->cub_tmp.p, bytes, kb, vb, n, 0, 63, st));
+    const uint64_t *keys = kb.Current();
+    const int *idx = vb.Current();
+    permute<<<grid_for(n), 256, 0, st>>>(n, idx, s->persist(0), s->persist(1));
+    // copy back so that the persistent arrays stay at fixed addresses (graph replay)
+    const size_t nb = (size_t)n;
+    CUDA_TRY(cudaMemcpyAsync(s->pos[0].p, s->pos[1].p, nb * sizeof(dbl4), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->vel[0].p, s->vel[1].p, nb * sizeof(dbl4), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->vel2[0].p, s->vel2[1].p, nb * sizeof(dbl4), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->id[0].p, s->id[1].p, nb * sizeof(long long), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->istar[0].p, s->istar[1].p, nb * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->orig[0].p, s->orig[1].p, nb * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    DevBuf<double> *dd[][2] = {{&s->uene[0], &s->uene[1]}, {&s->uene2[0], &s->uene2[1]},
+                               {&s->alph[0], &s->alph[1]}, {&s->alph2[0], &s->alph2[1]},
+                               {&s->alphu[0], &s->alphu[1]}, {&s->alphu2[0], &s->alphu2[1]},
+                               {&s->ksr[0], &s->ksr[1]}};
+    for (auto &d : dd)
+        CUDA_TRY(cudaMemcpyAsync(d[0]->p, d[1]->p, nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    sphtree::Nodes t = s->nodes();
+    if (n >= 2) {
+        sphtree::build_radix_tree<<<grid_for(n - 1), 256, 0, st>>>(keys, n, t);
+    } else {
+        set_int<<<1, 1, 0, st>>>(t.parent, -1);
+    }
+    eps2_from_h<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->eps2.p);
+    CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
+    sphtree::refit<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t);
+    // groups
+    CUDA_TRY(cudaMemsetAsync(s->gflag.p, 0, sizeof(int) * nb, st));
+    sphtree::mark_groups<<<grid_for(2LL * n - 1), 256, 0, st>>>(t, n, s->prm.n_group, s->gflag.p, s->groot.p);
+    int r = exclusive_scan(s, s->gflag.p, s->gscan.p);
+    if (r) return r;
+    compact_groups<<<grid_for(n), 256, 0, st>>>(n, s->gflag.p, s->gscan.p, s->groot.p, t, s->group_node.p,
+                                                s->group_first.p, s->group_count.p, s->scal.p);
+    return SPH_OK;
+}
+
+// Builds the lists of `kind` over the walks (group nodes + radii) and the
+// matching work items.  In eager mode (no capture) the list capacity grows to
+// the counted total first.
+int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const double *walk_r, bool eager,
+                          long long *pairs) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    sphtree::ListArgs a;
+    a.t = s->nodes();
+    a.n = n;
+    a.root = 0;
+    a.pos = s->pos[0].p;
+    a.h = s->ksr[0].p;
+    a.n_groups = s->walk_num[kind];
+    a.group_node = walk_node;
+    a.r_group = walk_r;
+    a.n_leaf = s->prm.n_leaf;
+    a.inv_theta2 = 1.0 / (s->prm.theta * s->prm.theta);
+    a.count_out = s->lcnt[kind].p;
+    a.offset = s->loff[kind].p;
+    a.error = s->scal.p + S_ERROR;
+    const int tgrid = s->ctx->sm_count * 8;
+    CUDA_TRY(cudaMemsetAsync(s->lcnt[kind].p, 0, sizeof(int) * (size_t)n, st));
+    const int mode = kind == 0 ? sphtree::GATHER : (kind == 1 ? sphtree::SYMMETRIC : sphtree::GRAVITY);
+    if (mode == sphtree::GATHER) sphtree::build_lists<sphtree::GATHER, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    if (mode == sphtree::SYMMETRIC) sphtree::build_lists<sphtree::SYMMETRIC, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    if (mode == sphtree::GRAVITY) sphtree::build_lists<sphtree::GRAVITY, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    int r = exclusive_scan(s, s->lcnt[kind].p, s->loff[kind].p);
+    if (r) return r;
+    const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : L_LIST_G);
+    if (eager) {
+        list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, (long long)1 << 62, s->scal.p, s->lscal.p, lslot);
+        long long tot = 0;
+        CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (tot + 1 > s->lcap[kind]) {
+            if (s->jidx[kind].ensure((size_t)(tot + tot / 2 + 1024)))
+                return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list allocation of %lld entries failed", tot);
+            s->lcap[kind] = (long long)s->jidx[kind].cap;
+            s->graph_valid = false;
+        }
+    }
+    list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, s->lcap[kind], s->scal.p, s->lscal.p, lslot);
+    a.j_idx = s->jidx[kind].p;
+    a.capacity = s->lcap[kind];
+    if (mode == sphtree::GATHER) sphtree::build_lists<sphtree::GATHER, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    if (mode == sphtree::SYMMETRIC) sphtree::build_lists<sphtree::SYMMETRIC, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    if (mode == sphtree::GRAVITY) sphtree::build_lists<sphtree::GRAVITY, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    // work items
+    item_counts<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], s->walk_count[kind], s->icnt.p);
+    r = exclusive_scan(s, s->icnt.p, s->ioff.p);
+    if (r) return r;
+    fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], s->walk_first[kind], s->walk_count[kind],
+                                            s->ioff.p, s->icnt.p, s->loff[kind].p, s->lcnt[kind].p, s->items.p,
+                                            s->scal.p + S_NITEMS, pairs);
+    return SPH_OK;
+}
+
+int density_phase(sph_system *s, bool eager) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    sph_context *ctx = s->ctx;
+    init_rs<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->rs.p);
+    set_int<<<1, 1, 0, st>>>(s->scal.p + S_ITERS, 1);
+    set_int<<<1, 1, 0, st>>>(s->scal.p + S_UNCONV, 0);
+    DensOut tmp{s->t_dens.p, s->t_divv.p, s->t_rotv.p, s->t_grdh.p, s->t_ksr.p, s->t_np.p, s->t_itr.p};
+    DensOut out{s->dens.p, s->divv.p, s->rotv.p, s->grdh.p, s->ksr[0].p, s->np.p, nullptr};
+    const int max_it = std::max(1, s->prm.max_density_iterations);
+    for (int it = 0; it < max_it; ++it) {
+        CUDA_TRY(cudaMemsetAsync(s->aflag.p, 0, sizeof(int) * (size_t)n, st));
+        group_rs_max<<<ctx->sm_count * 8, 256, 0, st>>>(s->scal.p, s->group_first.p, s->group_count.p, s->rs.p,
+                                                         s->g_r.p, s->aflag.p);
+        int r = exclusive_scan(s, s->aflag.p, s->ascan.p);
+        if (r) return r;
+        compact_active<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->aflag.p, s->ascan.p, s->group_node.p,
+                                                    s->group_first.p, s->group_count.p, s->g_r.p, s->a_node.p,
+                                                    s->a_first.p, s->a_count.p, s->a_r.p, s->scal.p);
+        r = build_lists_and_items(s, 0, s->a_node.p, s->a_r.p, eager && it == 0, s->lscal.p + L_PAIRS_D);
+        if (r) return r;
+        CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+        sphk::DensityArgs a;
+        a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p; a.i_ksr = s->ksr[0].p;
+        a.i_rs = s->rs.p;
+        a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
+        a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+        a.j_off = s->loff[0].p; a.j_idx = s->jidx[0].p; a.queue = s->scal.p + S_QUEUE;
+        a.o_dens = tmp.dens; a.o_divv = tmp.divv; a.o_rotv = tmp.rotv; a.o_grdh = tmp.grdh; a.o_ksr = tmp.ksr;
+        a.o_np = tmp.np; a.o_itr = tmp.itr;
+        a.eta_ksrh = ctx->prm.eta * KSRH;
+        a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
+        a.ksr_max_dev = (s->prm.ksr_max_mode == 1) ? s->dscal.p + D_KSRMAX : nullptr;
+        sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
+        commit_density<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, tmp, out, s->scal.p);
+        iteration_end<<<1, 1, 0, st>>>(s->scal.p, max_it, it);
+        if (eager) {
+            // stop on the host once every particle has converged; a captured
+            // graph keeps all iterations, which then find no active walk
+            int walks = 0;
+            CUDA_TRY(cudaMemcpyAsync(&walks, s->scal.p + S_ITERS, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            if (walks <= it + 1) break;
+        }
+    }
+    return SPH_OK;
+}
+
+int gravity_phase(sph_system *s, bool eager) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    sph_context *ctx = s->ctx;
+    int r = build_lists_and_items(s, 2, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_G);
+    if (r) return r;
+    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+    sphk::GravityArgs a;
+    a.i_pe = s->pe.p;
+    a.j_pm = s->pos[0].p; a.j_eps2 = s->eps2.p;
+    a.s_pm = s->mom.p; a.s_eps2 = s->neps2.p;
+    a.n_split = n;
+    a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+    a.j_off = s->loff[2].p; a.j_idx = s->jidx[2].p; a.queue = s->scal.p + S_QUEUE;
+    a.o_acc = s->r_acc.p; a.o_pot = s->r_pot.p; a.o_eta = s->r_eta.p;
+    sphrt::launch_gravity(a, ctx->prm.precision, ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st);
+    gravity_writeback<<<grid_for(n), 256, 0, st>>>(n, s->prm.G, s->r_acc.p, s->r_pot.p, s->r_eta.p, s->ksr[0].p,
+                                                   s->grdh.p, s->dens.p, s->accg2.p, s->pot.p, s->eta.p);
+    return SPH_OK;
+}
+
+int hydro_phase(sph_system *s, bool eager) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    sph_context *ctx = s->ctx;
+    hydro_prep<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->pres.p, s->grdh.p, s->dens.p, s->bswt.p,
+                                            s->vsnd.p, s->alph[0].p, s->alphu[0].p, s->uene[0].p, s->eta.p,
+                                            s->h1.p, s->h2.p, s->h3.p);
+    int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
+    if (r) return r;
+    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+    sphk::HydroArgs a;
+    a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p;
+    a.i_h1 = s->h1.p; a.i_h2 = s->h2.p; a.i_h3 = s->h3.p;
+    a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
+    a.j_h1 = s->h1.p; a.j_h2 = s->h2.p; a.j_h3 = s->h3.p;
+    a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+    a.j_off = s->loff[1].p; a.j_idx = s->jidx[1].p; a.queue = s->scal.p + S_QUEUE;
+    a.o_acch = s->r_acch.p; a.o_accg = s->r_accg.p; a.o_udot = s->r_udot.p; a.o_vsmx = s->r_vsmx.p;
+    a.o_diffu = s->r_diffu.p;
+    sphrt::launch_hydro(a, ctx->prm.precision, ctx->grid[1][ctx->prm.precision == SPH_PREC_FP64], st);
+    AlphaParams ap{s->prm.alpha_max, s->prm.alpha_min, s->prm.alphu_max, s->prm.alphu_min};
+    hydro_writeback<<<grid_for(n), 256, 0, st>>>(
+        n, s->prm.G, s->r_acch.p, s->r_accg.p, s->r_udot.p, s->r_vsmx.p, s->r_diffu.p, s->acch.p, s->accg1.p,
+        s->accg2.p, s->acc.p, s->udot.p, s->vsmx.p, s->diffu.p, s->divv.p, s->alph[0].p, s->alphu[0].p,
+        s->vsnd.p, s->ksr[0].p, s->uene[0].p, s->dscal.p + D_EPSU, ap, s->adot.p, s->adotu.p);
+    return SPH_OK;
+}
+
+// calcSPHKernel (main.cpp:300-358)
+int force_body(sph_system *s, bool eager) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    CUDA_TRY(cudaMemsetAsync(s->lscal.p, 0, sizeof(long long) * L_NI, st));
+    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_ERROR, 0, sizeof(int), st));
+    int r = build_tree(s);
+    if (r) return r;
+    r = density_phase(s, eager);
+    if (r) return r;
+    post_density<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->dens.p, s->uene[0].p, s->divv.p, s->rotv.p,
+                                              s->ksr[0].p, s->pres.p, s->vsnd.p, s->bswt.p, s->eps2.p, s->pe.p);
+    sphtree::Nodes t = s->nodes();
+    CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
+    sphtree::refit<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t);
+    r = gravity_phase(s, eager);
+    if (r) return r;
+    r = hydro_phase(s, eager);
+    if (r) return r;
+    if (s->prm.ksr_max_mode == 1) {
+        Star0Com f0{};
+        f0.pos = s->pos[0].p;
+        f0.istar = s->istar[0].p;
+        reduce(s, f0, s->dscal.p + D_XC);
+        com_divide<<<1, 1, 0, st>>>(s->dscal.p);
+        KsrMaxSums f1{};
+        f1.pos = s->pos[0].p;
+        f1.dens = s->dens.p;
+        f1.xc = s->dscal.p + D_XC;
+        reduce(s, f1, s->dscal.p + D_R2);
+        finish_ksrmax<<<1, 1, 0, st>>>(s->dscal.p, 1);
+    }
+    Energy fe{};
+    fe.pos = s->pos[0].p; fe.vel = s->vel[0].p; fe.uene = s->uene[0].p; fe.pot = s->pot.p;
+    reduce(s, fe, s->dscal.p + D_EKIN);
+    return SPH_OK;
+}
+
+// loopSimulation body (hdr_hgas.hpp:1499-1540)
+int step_body(sph_system *s, bool eager) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    TimestepMin ft{};
+    ft.ksr = s->ksr[0].p; ft.vsmx = s->vsmx.p; ft.divv = s->divv.p; ft.accg1 = s->accg1.p;
+    ft.accg2 = s->accg2.p; ft.c_dt = s->prm.c_dt; ft.dt_max = s->prm.dt_max;
+    reduce(s, ft, s->dscal.p + D_DTC);
+    update_dt<<<1, 1, 0, st>>>(s->dscal.p, s->scal.p, s->prm.dt_max, s->prm.dt_min);
+    predict<<<grid_for(n), 256, 0, st>>>(n, s->dscal.p, s->pos[0].p, s->vel[0].p, s->vel2[0].p, s->acc.p,
+                                         s->uene[0].p, s->uene2[0].p, s->udot.p, s->alph[0].p, s->alph2[0].p,
+                                         s->adot.p, s->alphu[0].p, s->alphu2[0].p, s->adotu.p);
+    int r = force_body(s, eager);
+    if (r) return r;
+    correct<<<grid_for(n), 256, 0, st>>>(n, s->dscal.p, s->vel[0].p, s->vel2[0].p, s->acc.p, s->uene[0].p,
+                                         s->uene2[0].p, s->udot.p, s->alph[0].p, s->alph2[0].p, s->adot.p,
+                                         s->alphu[0].p, s->alphu2[0].p, s->adotu.p);
+    advance_time<<<1, 1, 0, st>>>(s->dscal.p);
+    Energy fe{};
+    fe.pos = s->pos[0].p; fe.vel = s->vel[0].p; fe.uene = s->uene[0].p; fe.pot = s->pot.p;
+    reduce(s, fe, s->dscal.p + D_EKIN);
+    return SPH_OK;
+}
+
+int check_errors(sph_system *s) {
+    int sc[S_NI];
+    CUDA_TRY(cudaMemcpyAsync(sc, s->scal.p, sizeof(int) * S_NI, cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    const int e = sc[S_ERROR];
+    if (e & E_STACK) return sphrt::set_error(s->ctx, SPH_ERR_CAPACITY, "tree walk stack overflow");
+    if (e & E_LISTCAP) return sphrt::set_error(s->ctx, SPH_ERR_CAPACITY, "interaction list capacity exceeded");
+    if (e & E_NOTCONV)
+        return sphrt::set_error(s->ctx, SPH_ERR_NOT_CONVERGED, "search radius still growing after %d walks",
+                                s->prm.max_density_iterations);
+    if (e & E_DTMIN) return sphrt::set_error(s->ctx, SPH_ERR_NOT_CONVERGED, "time step below dt_min");
+    return SPH_OK;
+}
+
+}  // namespace
+
+// ============================================================== C ABI
+extern "C" void sph_system_params_default(sph_system_params *p) {
+    if (!p) return;
+    p->n_group = 256;
+    p->n_leaf = 8;
+    p->theta = 0.5;
+    p->G = 6.6738480e-8 / ((6.9599e10 * 1e-3) * (6.9599e10 * 1e-3) * (6.9599e10 * 1e-3) / (1.9891e33 * 1e-6));
+    p->c_dt = 0.1;
+    p->dt_max = 10.0;
+    p->dt_min = 1e-16;
+    p->alpha_max = 2.0;
+    p->alpha_min = 0.1;
+    p->alphu_max = 0.0;
+    p->alphu_min = 0.0;
+    p->ksr_max_mode = 1;
+    p->max_density_iterations = 8;
+    p->use_graph = 1;
+}
+
+extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p, sph_system **out) {
+    if (!ctx || !out || n < 2 || n > (1LL << 30)) return SPH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    sph_system *s = new (std::nothrow) sph_system();
+    if (!s) return SPH_ERR_CAPACITY;
+    s->ctx = ctx;
+    s->n = (int)n;
+    if (p) s->prm = *p; else sph_system_params_default(&s->prm);
+    if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || !(s->prm.theta > 0.0)) {
+        delete s;
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(ctx->prm.device);
+    if (alloc_all(s)) {
+        sph_system_destroy(s);
+        return sphrt::set_error(ctx, SPH_ERR_CUDA, "system allocation for %lld particles failed", (long long)n);
+    }
+    cudaMemset(s->scal.p, 0, sizeof(int) * S_NI);
+    cudaMemset(s->dscal.p, 0, sizeof(double) * D_NI);
+    cudaMemset(s->lscal.p, 0, sizeof(long long) * L_NI);
+    *out = s;
+    return SPH_OK;
+}
+
+extern "C" int sph_system_destroy(sph_system *s) {
+    if (!s) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    cudaStreamSynchronize(s->st());
+    if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
+    for (int k = 0; k < 2; ++k) {
+        s->pos[k].release(); s->vel[k].release(); s->vel2[k].release(); s->id[k].release();
+        s->istar[k].release(); s->orig[k].release(); s->uene[k].release(); s->uene2[k].release();
+        s->alph[k].release(); s->alph2[k].release(); s->alphu[k].release(); s->alphu2[k].release();
+        s->ksr[k].release(); s->keys[k].release(); s->perm[k].release();
+    }
+    DevBuf<double> *d1[] = {&s->rs, &s->dens, &s->divv, &s->rotv, &s->grdh, &s->pres, &s->vsnd, &s->bswt,
+                            &s->eps2, &s->udot, &s->vsmx, &s->diffu, &s->pot, &s->eta, &s->adot, &s->adotu,
+                            &s->t_dens, &s->t_divv, &s->t_rotv, &s->t_grdh, &s->t_ksr, &s->r_pot, &s->r_eta,
+                            &s->r_udot, &s->r_vsmx, &s->r_diffu, &s->g_r, &s->a_r, &s->acc, &s->acch,
+                            &s->accg1, &s->accg2, &s->r_acc, &s->r_acch, &s->r_accg, &s->staging,
+                            &s->neps2, &s->dscal, &s->partial, &s->box};
+    for (auto *b : d1) b->release();
+    s->np.release(); s->t_np.release(); s->t_itr.release(); s->pe.release(); s->h1.release();
+    s->h2.release(); s->h3.release(); s->child.release(); s->parent.release(); s->first.release();
+    s->count.release(); s->visit.release(); s->lo.release(); s->hi.release(); s->mom.release();
+    DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
+                         &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff,
+                         &s->scal};
+    for (auto *b : i1) b->release();
+    for (int k = 0; k < 3; ++k) {
+        s->lcnt[k].release(); s->loff[k].release(); s->jidx[k].release();
+    }
+    s->items.release(); s->lscal.release(); s->cub_tmp.release();
+    s->h_scal.release(); s->h_dscal.release(); s->h_lscal.release();
+    delete s;
+    return SPH_OK;
+}
+
+extern "C" int sph_system_upload(sph_system *s, double t0, const int64_t *id, const int32_t *istar,
+                                 const double *mass, const double *pos, const double *vel, const double *uene,
+                                 const double *ksr, const double *alph, const double *alphu) {
+    if (!s || !id || !mass || !pos || !vel || !uene || !ksr) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const int n = s->n;
+    const size_t nb = (size_t)n;
+    cudaStream_t st = s->st();
+    // staging holds 3n doubles; the four 1-D arrays go to per-step buffers first
+    CUDA_TRY(cudaMemcpyAsync(s->r_acc.p, pos, 3 * nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->staging.p, vel, 3 * nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->r_pot.p, mass, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    upload_pack<<<grid_for(n), 256, 0, st>>>(n, s->r_pot.p, s->r_acc.p, s->staging.p, s->pos[0].p,
+                                             s->vel[0].p, s->vel2[0].p);
+    CUDA_TRY(cudaMemcpyAsync(s->id[0].p, id, nb * sizeof(long long), cudaMemcpyHostToDevice, st));
+    if (istar)
+        CUDA_TRY(cudaMemcpyAsync(s->istar[0].p, istar, nb * sizeof(int), cudaMemcpyHostToDevice, st));
+    else
+        CUDA_TRY(cudaMemsetAsync(s->istar[0].p, 0, nb * sizeof(int), st));
+    iota<<<grid_for(n), 256, 0, st>>>(n, s->orig[0].p);
+    CUDA_TRY(cudaMemcpyAsync(s->uene[0].p, uene, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->uene2[0].p, uene, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->ksr[0].p, ksr, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (alph) {
+        CUDA_TRY(cudaMemcpyAsync(s->alph[0].p, alph, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    } else {
+        fill_double<<<grid_for(n), 256, 0, st>>>(n, s->alph[0].p, 1.0);
+    }
+    if (alphu) {
+        CUDA_TRY(cudaMemcpyAsync(s->alphu[0].p, alphu, nb * sizeof(double), cudaMemcpyHostToDevice, st));
+    } else {
+        fill_double<<<grid_for(n), 256, 0, st>>>(n, s->alphu[0].p, 0.0);
+    }
+    CUDA_TRY(cudaMemcpyAsync(s->alph2[0].p, s->alph[0].p, nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->alphu2[0].p, s->alphu[0].p, nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(s->acc.p, 0, 3 * nb * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(s->udot.p, 0, nb * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(s->adot.p, 0, nb * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(s->adotu.p, 0, nb * sizeof(double), st));
+    // run parameters that the reference derives from the initial state:
+    // Timestep = MaximumTimestep (hdr_hgas.hpp:1244), ksrmax = star separation
+    // (hdr_hgas.hpp:1335), epsu = 1e-4 min u (hdr_hgas.hpp:961-970)
+    double dh[D_NI];
+    std::memset(dh, 0, sizeof(dh));
+    dh[D_TIME] = t0;
+    dh[D_DT] = s->prm.dt_max;
+    CUDA_TRY(cudaMemcpyAsync(s->dscal.p, dh, sizeof(dh), cudaMemcpyHostToDevice, st));
+    UeneMin fu{};
+    fu.uene = s->uene[0].p;
+    reduce(s, fu, s->dscal.p + D_EPSU);
+    StarComs fc{};
+    fc.pos = s->pos[0].p;
+    fc.istar = s->istar[0].p;
+    reduce(s, fc, s->box.p);
+    double c[8], eu;
+    CUDA_TRY(cudaMemcpyAsync(c, s->box.p, sizeof(c), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&eu, s->dscal.p + D_EPSU, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    double ksrmax = std::numeric_limits<double>::max();
+    if (c[3] > 0.0 && c[7] > 0.0) {
+        const double dx = c[0] / c[3] - c[4] / c[7], dy = c[1] / c[3] - c[5] / c[7], dz = c[2] / c[3] - c[6] / c[7];
+        ksrmax = std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    eu *= 1e-4;
+    CUDA_TRY(cudaMemcpyAsync(s->dscal.p + D_KSRMAX, &ksrmax, sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(s->dscal.p + D_EPSU, &eu, sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    s->steps = 0;
+    return SPH_OK;
+}
+
+extern "C" int sph_system_compute_forces(sph_system *s) {
+    if (!s) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    int r = force_body(s, true);
+    if (!r) r = check_errors(s);
+    s->last_status = r;
+    return r;
+}
+
+extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
+    if (!s || n_steps < 0) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    cudaStream_t st = s->st();
+    for (int k = 0; k < n_steps; ++k) {
+        int r = SPH_OK;
+        if (!s->prm.use_graph || !s->graph_valid) {
+            // eager step (sizes lists, then the graph is captured for the next steps)
+            r = step_body(s, true);
+            if (!r) r = check_errors(s);
+            if (!r && s->prm.use_graph) {
+                if (s->step_exec) {
+                    cudaGraphExecDestroy(s->step_exec);
+                    s->step_exec = nullptr;
+                }
+                cudaGraph_t g = nullptr;
+                CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                int rc = step_body(s, false);
+                cudaError_t ec = cudaStreamEndCapture(st, &g);
+                if (rc) return rc;
+                if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaStreamEndCapture");
+                ec = cudaGraphInstantiate(&s->step_exec, g, 0);
+                cudaGraphDestroy(g);
+                if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaGraphInstantiate");
+                s->graph_valid = true;
+            }
+        } else {
+            CUDA_TRY(cudaGraphLaunch(s->step_exec, st));
+            if (k == n_steps - 1) r = check_errors(s);
+        }
+        s->steps++;
+        s->last_status = r;
+        if (r) return r;
+    }
+    return SPH_OK;
+}
+
+namespace {
+// Returns the device array of a field (width 1 or 3) or materialises it into
+// s->staging.
+int field_ptr(sph_system *s, int field, const double **ptr, int *width) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    *width = 1;
+    switch (field) {
+        case SPH_F_POS: field_from_dbl4<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, -1, s->staging.p); *ptr = s->staging.p; *width = 3; return 0;
+        case SPH_F_VEL: field_from_dbl4<<<grid_for(n), 256, 0, st>>>(n, s->vel[0].p, -1, s->staging.p); *ptr = s->staging.p; *width = 3; return 0;
+        case SPH_F_MASS: field_from_dbl4<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, 3, s->staging.p); *ptr = s->staging.p; return 0;
+        case SPH_F_ACC: *ptr = s->acc.p; *width = 3; return 0;
+        case SPH_F_ACCH: *ptr = s->acch.p; *width = 3; return 0;
+        case SPH_F_ACCG1: *ptr = s->accg1.p; *width = 3; return 0;
+        case SPH_F_ACCG2: *ptr = s->accg2.p; *width = 3; return 0;
+        case SPH_F_DENS: *ptr = s->dens.p; return 0;
+        case SPH_F_PRES: *ptr = s->pres.p; return 0;
+        case SPH_F_VSND: *ptr = s->vsnd.p; return 0;
+        case SPH_F_KSR: *ptr = s->ksr[0].p; return 0;
+        case SPH_F_DIVV: *ptr = s->divv.p; return 0;
+        case SPH_F_ROTV: *ptr = s->rotv.p; return 0;
+        case SPH_F_BSWT: *ptr = s->bswt.p; return 0;
+        case SPH_F_GRDH: *ptr = s->grdh.p; return 0;
+        case SPH_F_UENE: *ptr = s->uene[0].p; return 0;
+        case SPH_F_UDOT: *ptr = s->udot.p; return 0;
+        case SPH_F_ALPH: *ptr = s->alph[0].p; return 0;
+        case SPH_F_ALPHU: *ptr = s->alphu[0].p; return 0;
+        case SPH_F_POT: *ptr = s->pot.p; return 0;
+        case SPH_F_ETA: *ptr = s->eta.p; return 0;
+        case SPH_F_VSMX: *ptr = s->vsmx.p; return 0;
+        case SPH_F_DIFFU: *ptr = s->diffu.p; return 0;
+        case SPH_F_ADOT: *ptr = s->adot.p; return 0;
+        case SPH_F_ADOTU: *ptr = s->adotu.p; return 0;
+        case SPH_F_NP: field_to_double<long long><<<grid_for(n), 256, 0, st>>>(n, s->np.p, s->staging.p); *ptr = s->staging.p; return 0;
+        case SPH_F_ID: field_to_double<long long><<<grid_for(n), 256, 0, st>>>(n, s->id[0].p, s->staging.p); *ptr = s->staging.p; return 0;
+        case SPH_F_ISTAR: field_to_double<int><<<grid_for(n), 256, 0, st>>>(n, s->istar[0].p, s->staging.p); *ptr = s->staging.p; return 0;
+        default: return 1;
+    }
+}
+}  // namespace
+
+extern "C" int sph_system_download(sph_system *s, int32_t field, double *out) {
+    if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const double *src = nullptr;
+    int w = 1;
+    if (field_ptr(s, field, &src, &w)) return SPH_ERR_INVALID_ARGUMENT;
+    const int n = s->n;
+    double *dst = (src == s->staging.p) ? s->r_acch.p : s->staging.p;
+    scatter_field<<<grid_for(n), 256, 0, s->st()>>>(n, w, s->orig[0].p, src, dst);
+    CUDA_TRY(cudaMemcpyAsync(out, dst, sizeof(double) * w * (size_t)n, cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    return SPH_OK;
+}
+
+extern "C" int sph_system_download_sorted(sph_system *s, int32_t field, double *out) {
+    if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const double *src = nullptr;
+    int w = 1;
+    if (field_ptr(s, field, &src, &w)) return SPH_ERR_INVALID_ARGUMENT;
+    CUDA_TRY(cudaMemcpyAsync(out, src, sizeof(double) * w * (size_t)s->n, cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    return SPH_OK;
+}
+
+extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
+    if (!s || !o) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    int sc[S_NI];
+    double dc[D_NI];
+    long long lc[L_NI];
+    CUDA_TRY(cudaMemcpyAsync(sc, s->scal.p, sizeof(sc), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaMemcpyAsync(dc, s->dscal.p, sizeof(dc), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaMemcpyAsync(lc, s->lscal.p, sizeof(lc), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    o->time = dc[D_TIME];
+    o->dt = dc[D_DT];
+    o->ksr_max = dc[D_KSRMAX];
+    o->e_kin = dc[D_EKIN];
+    o->e_thm = dc[D_ETHM];
+    o->e_pot = dc[D_EPOT];
+    o->e_tot = dc[D_EKIN] + dc[D_ETHM] + dc[D_EPOT];
+    o->n_groups = sc[S_NGROUPS];
+    o->density_iterations = sc[S_ITERS];
+    o->pairs_density = lc[L_PAIRS_D];
+    o->pairs_hydro = lc[L_PAIRS_H];
+    o->pairs_gravity = lc[L_PAIRS_G];
+    o->list_density = lc[L_LIST_D];
+    o->list_hydro = lc[L_LIST_H];
+    o->list_gravity = lc[L_LIST_G];
+    o->steps = s->steps;
+    o->last_status = s->last_status;
+    return SPH_OK;
+}
+
+extern "C" int sph_system_get_lists(sph_system *s, int32_t kind, int32_t *n_walk, int64_t *n_entries,
+                                    int32_t *i_first, int32_t *i_count, int64_t *j_off, int32_t *j_idx) {
+    if (!s || kind < 0 || kind > 2 || !n_walk || !n_entries) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    cudaStream_t st = s->st();
+    int nw = 0;
+    long long tot = 0;
+    CUDA_TRY(cudaMemcpyAsync(&nw, s->walk_num[kind], sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : L_LIST_G);
+    CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    *n_walk = nw;
+    *n_entries = tot;
+    if (!i_first || !i_count || !j_off || !j_idx) return SPH_OK;
+    std::vector<int> off(nw > 0 ? nw : 1), cnt(nw > 0 ? nw : 1);
+    if (nw > 0) {
+        CUDA_TRY(cudaMemcpyAsync(i_first, s->walk_first[kind], sizeof(int) * nw, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(i_count, s->walk_count[kind], sizeof(int) * nw, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(off.data(), s->loff[kind].p, sizeof(int) * nw, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(cnt.data(), s->lcnt[kind].p, sizeof(int) * nw, cudaMemcpyDeviceToHost, st));
+    }
+    if (tot > 0)
+        CUDA_TRY(cudaMemcpyAsync(j_idx, s->jidx[kind].p, sizeof(int) * (size_t)tot, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (int w = 0; w < nw; ++w) j_off[w] = off[w];
+    j_off[nw] = nw > 0 ? (int64_t)off[nw - 1] + cnt[nw - 1] : 0;
+    return SPH_OK;
+}
+
+extern "C" int sph_system_get_nodes(sph_system *s, double *mom, double *eps2) {
+    if (!s || !mom || !eps2) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const size_t nn = 2 * (size_t)s->n - 1;
+    CUDA_TRY(cudaMemcpyAsync(mom, s->mom.p, sizeof(dbl4) * nn, cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaMemcpyAsync(eps2, s->neps2.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    return SPH_OK;
+}

@@ -1,0 +1,231 @@
+"""Device-resident system: the full calcSPHKernel step on the GPU, checked
+against the oracle on the engine's own exported walks (same i-groups, same
+j-lists, same tree monopoles), plus tree-vs-direct gravity accuracy, list
+completeness, graph/eager equality and energy conservation."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import oracle as orc
+from research_codes_gb300 import abi, functors, ic, units
+from research_codes_gb300.system import ParticleSystem, state_from_ic
+
+pytestmark = pytest.mark.gpu
+
+FLOOR = 1e-3
+
+
+def err(a, b):
+    return rel_err(a, b, floor_frac=FLOOR).max()
+
+
+def _star(n=4000, seed=3, eta=1.18, spin=True):
+    s = ic.polytrope(n, 1.0, 1.0, 1.5, seed=seed, eta=eta)
+    s = state_from_ic(s)
+    if spin:
+        rng = np.random.default_rng(seed)
+        s["vel"] = np.cross([0.0, 0.0, 2e-3], s["pos"]) + rng.normal(scale=1.0, size=s["pos"].shape)
+    return s
+
+
+def _two_stars(n=6000, seed=5, eta=1.18):
+    a = ic.polytrope(n // 2, 10.0, 4.0, 3.0, seed=seed, eta=eta)
+    b = ic.polytrope(n - n // 2, 3.0, 1.5, 1.5, seed=seed + 1, eta=eta)
+    sep = 1.2 * (a["R"] + b["R"])
+    s = ic.two_stars(a, b, sep, 0.3 * (a["R"] + b["R"]), 1.2 * ic.escape_speed(a["M"] + b["M"], sep))
+    return state_from_ic(s)
+
+
+@pytest.fixture(scope="module", params=["fp32c", "fp64"])
+def evaluated(request):
+    """A star whose forces were evaluated twice (the second evaluation starts
+    from converged h, so its density pass is a single walk)."""
+    prec = request.param
+    s = _star()
+    ctx = functors.Context(precision=prec, eta=1.18, ksr_max=0.0)
+    sys = ParticleSystem(ctx, len(s["mass"]), n_group=64, use_graph=0, ksr_max_mode=0)
+    sys.upload(s)
+    sys.compute_forces()
+    ksr0 = sys.download("ksr", sorted_order=True)
+    sys.compute_forces()
+    yield dict(ctx=ctx, sys=sys, ksr0=ksr0, prec=prec)
+    sys.close()
+    ctx.close()
+
+
+def _sorted(sys, *names):
+    return {k: sys.download(k, sorted_order=True) for k in names}
+
+
+def _tol(prec, deriv=False):
+    return 1e-11 if prec == "fp64" else (1e-4 if deriv else 1e-5)
+
+
+def test_density_matches_oracle_on_engine_lists(evaluated):
+    sys, ksr0, prec = evaluated["sys"], evaluated["ksr0"], evaluated["prec"]
+    st = sys.stats()
+    assert st["density_iterations"] == 1
+    f = _sorted(sys, "pos", "vel", "mass", "id", "dens", "ksr", "grdh", "divv", "rotv", "np")
+    state = dict(pos=f["pos"], vel=f["vel"], mass=f["mass"], id=f["id"].astype(np.int64),
+                 ksr=ksr0, rs=1.1 * ksr0)
+    i_first, i_count, j_off, j_idx = sys.lists(0)
+    assert i_count.sum() == sys.n
+    from research_codes_gb300 import walks
+    worst = {k: 0.0 for k in ("dens", "ksr", "grdh", "divv", "rotv")}
+    for w in range(len(i_first)):
+        gi = np.arange(i_first[w], i_first[w] + i_count[w])
+        gj = j_idx[j_off[w]:j_off[w + 1]]
+        ref = orc.density(walks.density_epi(gi, state), walks.density_epj(gj, state), eta=1.18,
+                          ksr_max=0.0)
+        for k in worst:
+            worst[k] = max(worst[k], err(f[k][gi], ref[k]))
+        assert np.abs(f["np"][gi] - ref["np"]).max() <= (0 if prec == "fp64" else 1)
+    for k, v in worst.items():
+        assert v < _tol(prec, k in ("divv", "rotv")), (k, v)
+
+
+def test_gravity_matches_oracle_on_engine_lists(evaluated):
+    sys, prec = evaluated["sys"], evaluated["prec"]
+    n = sys.n
+    f = _sorted(sys, "pos", "mass", "ksr", "accg2", "pot", "eta", "grdh", "dens")
+    mom, neps2 = sys.nodes()
+    eps2 = (f["ksr"] / units.KSRH) ** 2
+    i_first, i_count, j_off, j_idx = sys.lists(2)
+    G = sys.params.G
+    errs = []
+    for w in range(0, len(i_first), max(1, len(i_first) // 25)):
+        gi = np.arange(i_first[w], i_first[w] + i_count[w])
+        lst = j_idx[j_off[w]:j_off[w + 1]]
+        pj, sj = lst[lst < n], lst[lst >= n] - n
+        epi = np.zeros(len(gi), abi.GravityEPI)
+        epi["pos"], epi["eps2"] = f["pos"][gi], eps2[gi]
+        epj = np.zeros(len(pj), abi.GravityEPJ)
+        epj["mass"], epj["pos"], epj["eps2"] = f["mass"][pj], f["pos"][pj], eps2[pj]
+        spj = np.zeros(len(sj), abi.GravitySPJ)
+        spj["mass"], spj["pos"], spj["eps2"] = mom[sj, 3], mom[sj, :3], neps2[sj]
+        ref = orc.gravity(epi, epj, spj)
+        errs.append(err(f["accg2"][gi], G * ref["acc"]))
+        errs.append(err(f["pot"][gi], G * ref["pot"]))
+        eta_ref = f["ksr"][gi] ** 2 / units.KSRH ** 2 * f["grdh"][gi] / (3 * f["dens"][gi]) * ref["eta"]
+        errs.append(err(f["eta"][gi], eta_ref))
+    assert max(errs) < _tol(prec), max(errs)
+
+
+def test_hydro_matches_oracle_on_engine_lists(evaluated):
+    sys, prec = evaluated["sys"], evaluated["prec"]
+    f = _sorted(sys, "pos", "vel", "mass", "id", "ksr", "pres", "grdh", "dens", "bswt", "vsnd", "alph",
+                "alphu", "uene", "eta", "acch", "accg1", "udot", "vsmx", "diffu")
+    f["id"] = f["id"].astype(np.int64)
+    from research_codes_gb300 import walks
+    i_first, i_count, j_off, j_idx = sys.lists(1)
+    G = sys.params.G
+    worst = {k: 0.0 for k in ("acch", "accg", "udot", "vsmx", "diffu")}
+    for w in range(0, len(i_first), max(1, len(i_first) // 25)):
+        gi = np.arange(i_first[w], i_first[w] + i_count[w])
+        gj = j_idx[j_off[w]:j_off[w + 1]]
+        ref = orc.hydro(walks.hydro_epi(gi, f), walks.hydro_epj(gj, f))
+        worst["acch"] = max(worst["acch"], err(f["acch"][gi], ref["acch"]))
+        worst["accg"] = max(worst["accg"], err(f["accg1"][gi], G * ref["accg"]))
+        worst["udot"] = max(worst["udot"], err(f["udot"][gi], ref["udot"]))
+        worst["vsmx"] = max(worst["vsmx"], err(f["vsmx"][gi], ref["vsmx"]))
+        worst["diffu"] = max(worst["diffu"], err(f["diffu"][gi], ref["diffu"]))
+    for k, v in worst.items():
+        assert v < _tol(prec, k in ("diffu", "accg")), (k, v)
+
+
+def test_density_lists_are_complete(evaluated):
+    """Every j within rs_i of an i-particle is in i's walk list (the gather
+    rule), checked by brute force on a sample of walks."""
+    sys, ksr0 = evaluated["sys"], evaluated["ksr0"]
+    pos = sys.download("pos", sorted_order=True)
+    rs = 1.1 * ksr0
+    i_first, i_count, j_off, j_idx = sys.lists(0)
+    for w in range(0, len(i_first), max(1, len(i_first) // 20)):
+        gi = np.arange(i_first[w], i_first[w] + i_count[w])
+        have = set(j_idx[j_off[w]:j_off[w + 1]].tolist())
+        for i in gi[:8]:
+            need = np.nonzero(np.linalg.norm(pos - pos[i], axis=1) < rs[i])[0]
+            assert set(need.tolist()) <= have
+
+
+def test_tree_gravity_vs_direct_sum(evaluated):
+    """theta = 0.5 monopole tree force against direct FP64 summation."""
+    sys = evaluated["sys"]
+    f = _sorted(sys, "pos", "mass", "ksr", "accg2", "pot")
+    eps2 = (f["ksr"] / units.KSRH) ** 2
+    rng = np.random.default_rng(0)
+    sel = rng.choice(sys.n, 200, replace=False)
+    epi = np.zeros(len(sel), abi.GravityEPI)
+    epi["pos"], epi["eps2"] = f["pos"][sel], eps2[sel]
+    epj = np.zeros(sys.n, abi.GravityEPJ)
+    epj["mass"], epj["pos"], epj["eps2"] = f["mass"], f["pos"], eps2
+    ref = orc.gravity(epi, epj)
+    G = sys.params.G
+    a_err = np.linalg.norm(f["accg2"][sel] - G * ref["acc"], axis=1) / np.linalg.norm(G * ref["acc"], axis=1)
+    p_err = np.abs(f["pot"][sel] - G * ref["pot"]) / np.abs(G * ref["pot"])
+    assert np.median(a_err) < 3e-3 and a_err.max() < 5e-2, (np.median(a_err), a_err.max())
+    assert p_err.max() < 1e-2
+
+
+def test_download_order_is_upload_order():
+    s = _star(n=1500, seed=9)
+    with functors.Context(eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, 1500, n_group=64, use_graph=0)
+        s["id"] = np.arange(1500, dtype=np.int64)[::-1].copy()
+        sys.upload(s)
+        sys.compute_forces()
+        assert np.array_equal(sys.download("id").astype(np.int64), s["id"])
+        assert np.allclose(sys.download("pos"), s["pos"], rtol=0, atol=0)
+        sys.close()
+
+
+def test_graph_replay_equals_eager_steps():
+    s = _two_stars(n=3000)
+    out = {}
+    for use_graph in (0, 1):
+        with functors.Context(eta=1.18) as ctx:
+            sys = ParticleSystem(ctx, len(s["mass"]), n_group=64, use_graph=use_graph)
+            sys.upload(s)
+            sys.compute_forces()
+            sys.step(4)
+            out[use_graph] = (sys.download("pos"), sys.download("vel"), sys.download("uene"), sys.stats())
+            sys.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
+    assert out[0][3]["time"] == out[1][3]["time"]
+
+
+@pytest.mark.parametrize("prec", ["fp32c", "fp64"])
+def test_energy_conservation_short_run(prec):
+    s = _star(n=3000, seed=4, spin=False)
+    with functors.Context(precision=prec, eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, len(s["mass"]), n_group=64)
+        sys.upload(s)
+        sys.compute_forces()
+        e0 = sys.stats()["e_tot"]
+        sys.step(20)
+        st = sys.stats()
+        drift = abs(st["e_tot"] - e0) / abs(e0)
+        assert st["time"] > 0 and st["steps"] == 20
+        assert drift < 1e-3, drift
+        sys.close()
+
+
+def test_fp32c_step_tracks_fp64_step():
+    """Two-star system, 5 steps in each precision: positions and internal
+    energies agree to well below the step-to-step change."""
+    s = _two_stars(n=4000, seed=8)
+    res = {}
+    for prec in ("fp32c", "fp64"):
+        with functors.Context(precision=prec, eta=1.18) as ctx:
+            sys = ParticleSystem(ctx, len(s["mass"]), n_group=64)
+            sys.upload(s)
+            sys.compute_forces()
+            sys.step(5)
+            res[prec] = dict(pos=sys.download("pos"), uene=sys.download("uene"), acc=sys.download("acc"),
+                             dens=sys.download("dens"))
+            sys.close()
+    assert err(res["fp32c"]["dens"], res["fp64"]["dens"]) < 1e-5
+    assert err(res["fp32c"]["acc"], res["fp64"]["acc"]) < 1e-4
+    assert err(res["fp32c"]["uene"], res["fp64"]["uene"]) < 1e-5
