@@ -1,0 +1,463 @@
+#!/usr/bin/env python
+"""Benchmark of the per-step SPH interaction path on one GB300.
+
+Workload (default): the off-axis unequal-mass collision, N = 1,000,000
+(10 Msun / 4 Rsun n=3 with 600k particles + 3 Msun / 1.5 Rsun n=1.5 with 400k,
+impact parameter 0.5 (R1+R2), relative speed 1.2 v_esc, ~50 neighbours),
+built from seeded synthetic polytropes (no dataset is involved).
+
+A step is one iteration of the reference's loop body — time step, predict,
+density with smoothing-length iteration, EOS, tree gravity, hydro force,
+correct — run by the device-resident engine as one CUDA graph.
+
+Metric: pair-interactions per second over the whole step (density + hydro +
+gravity pairs, each pair = one (i, j) evaluation in a walk's list), plus
+ms/step.  The line also carries the FP64 comparator, FP32C-vs-FP64 parity on
+the same state, the dominant kernel's roofline, the end-to-end rate through
+the C ABI with host buffers, and the CPU oracle's rate on the host cores.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# flop per pair, counted from the reference's GPU kernels (add/mul/cmp/select
+# = 1, fma = 2, rsqrt/sqrt/rcp = 1): density 132 (3 x 23 + 63, four passes),
+# hydro 109, gravity 29.
+FLOP_PER_PAIR = {"density": 132.0, "hydro": 109.0, "gravity": 29.0}
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (sm clock, throttle reasons)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------ CPU oracle
+def oracle_rates(samples, nthreads):
+    """Times the oracle's walk-batched functors on host-built EPI/EPJ samples.
+
+    samples: {"density": (epi, epj, i_off, j_off), "hydro": ..., "gravity": ...}
+    Returns {phase: (pairs, seconds)}."""
+    from oracle import oracle as orc
+    out = {}
+    for phase, (epi, epj, io, jo) in samples.items():
+        pairs = int(sum((io[w + 1] - io[w]) * (jo[w + 1] - jo[w]) for w in range(len(io) - 1)))
+        fn = {"density": lambda: orc.density_walks(io, jo, epi, epj, eta=ETA, nthreads=nthreads),
+              "hydro": lambda: orc.hydro_walks(io, jo, epi, epj, nthreads=nthreads),
+              "gravity": lambda: orc.gravity_walks(io, jo, epi, epj, nthreads=nthreads)}[phase]
+        fn()  # warm-up (page-in, thread pool)
+        t = time.perf_counter()
+        fn()
+        out[phase] = (pairs, time.perf_counter() - t)
+    return out
+
+
+def combined_rate(rates, mix):
+    """Interactions/s of a step with the per-phase pair mix `mix` when each
+    phase runs at the measured rate."""
+    t = sum(mix[p] / (rates[p][0] / rates[p][1]) for p in mix)
+    return sum(mix.values()) / t
+
+
+def samples_from_engine(ps, rng, frac):
+    """EPI/EPJ arrays of a random subset of the engine's own walks."""
+    from research_codes_gb300 import abi, units, walks
+    n = ps.n
+    f = {k: ps.download(k, sorted_order=True) for k in
+         ("pos", "vel", "mass", "id", "ksr", "pres", "grdh", "dens", "bswt", "vsnd", "alph", "alphu", "uene",
+          "eta")}
+    f["id"] = f["id"].astype(np.int64)
+    f["rs"] = 1.1 * f["ksr"]
+    out = {}
+    for kind, phase in ((0, "density"), (1, "hydro"), (2, "gravity")):
+        i_first, i_count, j_off, j_idx = ps.lists(kind)
+        nw = len(i_first)
+        take = np.sort(rng.choice(nw, max(4, int(nw * frac)), replace=False))
+        items = []
+        for w in take:
+            gi = np.arange(i_first[w], i_first[w] + i_count[w])
+            gj = j_idx[j_off[w]:j_off[w + 1]]
+            if phase == "density":
+                items.append((walks.density_epi(gi, f), walks.density_epj(gj, f)))
+            elif phase == "hydro":
+                items.append((walks.hydro_epi(gi, f), walks.hydro_epj(gj, f)))
+            else:
+                mom, neps2 = NODES
+                pj, sj = gj[gj < n], gj[gj >= n] - n
+                epi = walks.gravity_epi(gi, f)
+                epj = np.zeros(len(gj), abi.GravityEPJ)
+                epj["mass"][:len(pj)] = f["mass"][pj]
+                epj["pos"][:len(pj)] = f["pos"][pj]
+                epj["eps2"][:len(pj)] = (f["ksr"][pj] / units.KSRH) ** 2
+                epj["mass"][len(pj):] = mom[sj, 3]
+                epj["pos"][len(pj):] = mom[sj, :3]
+                epj["eps2"][len(pj):] = neps2[sj]
+                items.append((epi, epj))
+        out[phase] = walks.concat_walks(items)
+    return out
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    import torch
+
+    from research_codes_gb300 import functors, ic
+    from research_codes_gb300.system import ParticleSystem, state_from_ic
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+
+    global ETA
+    t_ic = time.time()
+    s, ETA = ic.config_system(args.config, scale=args.scale, seed=args.seed + rank)
+    s = state_from_ic(s)
+    n = len(s["mass"])
+    log(f"[bench] rank {rank}: {args.config} n={n} ic {time.time() - t_ic:.1f}s")
+
+    ctx = functors.Context(device=local, precision="fp32c", eta=ETA)
+    ps = ParticleSystem(ctx, n, n_group=args.n_group)
+    ps.upload(s)
+    ps.compute_forces()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        ps.step(1)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K graph-captured steps, CUDA events on the engine's stream
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ps.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    st = ps.stats()
+    pairs = {"density": st["pairs_density"], "hydro": st["pairs_hydro"], "gravity": st["pairs_gravity"]}
+    inter = sum(pairs.values())
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * inter * args.steps / (ms * 1e-3)
+    log(f"[bench] {ms_step:.2f} ms/step, {inter:.3e} pairs/step, iters {st['density_iterations']}")
+
+    # ---- per-kernel durations (CUDA events recorded inside the captured step)
+    acc_t = {}
+    for _ in range(args.steps):
+        ps.step(1)
+        for k, v in ps.phase_times().items():
+            acc_t[k] = acc_t.get(k, 0.0) + v
+    phases = {k: v / args.steps for k, v in acc_t.items()}
+    st_k = ps.stats()
+    kern = {"density": phases["density_kernel"], "hydro": phases["hydro_kernel"],
+            "gravity": phases["gravity_kernel"]}
+    dom = max(kern, key=kern.get)
+    peak = ctx.probe_fp32_peak()
+    pairs_k = {"density": st_k["pairs_density"], "hydro": st_k["pairs_hydro"], "gravity": st_k["pairs_gravity"]}
+    if st_k["density_iterations"] > 1:
+        pairs_k["density"] = None   # first-walk kernel time vs all-walk pairs: not comparable
+    achieved = (pairs_k[dom] * FLOP_PER_PAIR[dom] / (kern[dom] * 1e-3) / 1e12) if pairs_k[dom] else None
+    traffic = None
+    if os.path.exists(PROFILE_TRAFFIC):
+        tr = json.load(open(PROFILE_TRAFFIC))
+        if dom in tr:
+            traffic = tr[dom].get("bytes_per_launch_scaled")
+
+    line = {"metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
+            "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math (FP32C), f64 state",
+            "data": "synthetic seeded polytropes (ic.config_system)",
+            "config": {"workload": f"{args.config}: off-axis unequal-mass collision, N={n}, n_group={args.n_group}, "
+                                   f"theta=0.5, eta={ETA}", "n_particles": n,
+                       "l2": "inputs larger than L2 (particle state + lists ~2 GB per step)",
+                       "pairs_per_step": pairs, "density_walks": st["density_iterations"],
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+            "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
+                         "traffic": traffic,
+                         "peak_source": "FP32 FMA probe on this GPU (sph_probe_fp32_peak); "
+                                        "MEASURED_PEAKS.json holds no FP32 figure"},
+            "gpu_launches": None, "clocks": clk}
+
+    # kernel launches per step: counted by the engine's structure
+    line["gpu_launches"] = args.steps * LAUNCHES_PER_STEP(args)
+
+    if rank == 0 and not args.no_fp64:
+        # ---- FP64 comparator on the same state and FP32C/FP64 parity
+        f32 = {k: ps.download(k) for k in ("dens", "acc", "udot", "ksr", "pot")}
+        ctx.set_precision("fp64")
+        ps.compute_forces()   # same state, FP64 pair arithmetic
+        f64 = {k: ps.download(k) for k in ("dens", "acc", "udot", "ksr", "pot")}
+        ps.step(1)            # captures the FP64 graph
+        torch.cuda.synchronize()
+        k64 = max(1, min(args.steps, 3))
+        e0.record(stream)
+        ps.step(k64)
+        e1.record(stream)
+        e1.synchronize()
+        ms64 = e0.elapsed_time(e1) / k64
+        ph64 = ps.phase_times()
+        ctx.set_precision("fp32c")
+
+        def rel(a, b, floor=1e-3):
+            a, b = np.asarray(a), np.asarray(b)
+            if a.ndim > 1:
+                d, s_ = np.linalg.norm(a - b, axis=1), np.linalg.norm(b, axis=1)
+            else:
+                d, s_ = np.abs(a - b), np.abs(b)
+            r = d / np.maximum(s_, floor * s_.max())
+            return {"max": float(r.max()), "median": float(np.median(r)), "p99": float(np.quantile(r, 0.99))}
+
+        line["fp64"] = {"ms_per_step": ms64, "speedup_fp32c_over_fp64": ms64 / ms_step,
+                        "phases_ms": {k: round(v, 3) for k, v in ph64.items()}}
+        line["parity_fp32c_vs_fp64"] = {k: rel(f32[k], f64[k]) for k in f32}
+        log(f"[bench] fp64 {ms64:.1f} ms/step (x{ms64 / ms_step:.1f})")
+
+    if rank == 0 and not args.no_e2e:
+        # ---- end to end through the C ABI with host buffers: per step the
+        # host state goes up (pinned), one step runs, acc/udot come back.
+        pin = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy() for k, v in s.items()
+               if isinstance(v, np.ndarray)}
+        out_acc = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+        out_udot = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+        h2d = sum(pin[k].nbytes for k in ("id", "mass", "pos", "vel", "uene", "ksr", "alph", "alphu")) + 4 * n
+        d2h = out_acc.nbytes + out_udot.nbytes
+        ke = max(1, min(args.steps, 5))
+        pairs_e = 0
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(ke):
+            ps.upload(pin)
+            ps.step(1)
+            ps.download("acc", out=out_acc)
+            ps.download("udot", out=out_udot)
+            ste = ps.stats()
+            pairs_e += ste["pairs_density"] + ste["pairs_hydro"] + ste["pairs_gravity"]
+        el = time.perf_counter() - t
+        line["e2e"] = {"value": pairs_e / el, "unit": "interactions/s", "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * el / ke,
+                       "path": "sph_system_upload -> sph_system_step -> sph_system_download (pinned host)"}
+
+    if rank == 0 and not args.no_cpu:
+        # ---- CPU oracle (port) on the host cores, bounded sample of this workload's walks
+        global NODES
+        ps.compute_forces()   # eager evaluation: every list is exported as used
+        NODES = ps.nodes()
+        rng = np.random.default_rng(1)
+        smp = samples_from_engine(ps, rng, args.cpu_frac)
+        nthreads = os.cpu_count() or 1
+        rates = oracle_rates(smp, nthreads)
+        cpu_rate = combined_rate(rates, {k: float(v) for k, v in pairs.items()})
+        line["cpu_baseline"] = {"value": cpu_rate, "unit": "interactions/s", "cores": nthreads, "kind": "port",
+                                "sample": f"{args.cpu_frac:.1%} of the walks of each phase of this step "
+                                          f"({', '.join(f'{k} {v[0]:.2e} pairs in {v[1]:.1f}s' for k, v in rates.items())}); "
+                                          "scalar FP64 C restatement of the reference functors, OpenMP over walks; "
+                                          "tree/list construction not included"}
+    ps.close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def LAUNCHES_PER_STEP(args):
+    """Kernel launches of one captured step (memsets and copies excluded):
+    step glue 6, tree/groups 9, per density walk 12 (x max iterations),
+    post-density + refit 2, gravity 8, hydro 9, ksrmax + energy 7."""
+    return 6 + 9 + 12 * 8 + 2 + 8 + 9 + 7
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args):
+    """The reference's CPU functors for this path, timed on the host cores.
+
+    The reference tree is not available here at run time, so the timed code
+    is the oracle's C restatement of the reference's scalar FP64 functors
+    (kind "port"), pinned bit-for-bit-close to the reference by the golden
+    vectors.  Walks are built on the host (Morton groups of n_group, KD-tree
+    neighbour lists, near-particle + far-cell monopole gravity lists) from the
+    same synthetic initial conditions; FDPS's tree cost is not included."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from scipy.spatial import cKDTree
+
+    from research_codes_gb300 import abi, ic, units, walks
+
+    global ETA
+    s, ETA = ic.config_system(args.config, scale=args.scale, seed=args.seed)
+    n = len(s["mass"])
+    s["id"] = np.arange(n, dtype=np.int64)
+    s["rs"] = 1.1 * s["ksr"]
+    rng = np.random.default_rng(7)
+    groups = walks.make_groups(s["pos"], args.n_group)
+    take = rng.choice(len(groups), max(8, int(len(groups) * args.ref_frac)), replace=False)
+    tree = cKDTree(s["pos"])
+    hmax = s["ksr"].max()
+    # hydro fields from the initial conditions (EOS of the Lane-Emden density)
+    s["dens"] = s["dens"]
+    s["pres"] = s["dens"] * s["uene"] / units.EOS_N
+    s["vsnd"] = np.sqrt(units.GAMMA * s["pres"] / s["dens"])
+    s["grdh"] = np.ones(n)
+    s["bswt"] = np.full(n, 0.1)
+    s["alph"] = np.ones(n)
+    s["alphu"] = np.zeros(n)
+    s["eta"] = np.full(n, 0.05)
+    eps2 = (s["ksr"] / units.KSRH) ** 2
+    d_items, h_items, g_items = [], [], []
+    for g in take:
+        gi = groups[g]
+        lo, hi = s["pos"][gi].min(0), s["pos"][gi].max(0)
+        c, half = 0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo)
+        r = s["rs"][gi].max()
+        cand = np.array(tree.query_ball_point(c, half + r), dtype=np.int64)
+        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
+        d2 = (d * d).sum(1)
+        d_items.append((walks.density_epi(gi, s), walks.density_epj(np.sort(cand[d2 <= r * r]), s)))
+        rh = max(s["ksr"][gi].max(), hmax)
+        cand = np.array(tree.query_ball_point(c, half + rh), dtype=np.int64)
+        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
+        d2 = (d * d).sum(1)
+        rj = np.maximum(s["ksr"][gi].max(), s["ksr"][cand])
+        h_items.append((walks.hydro_epi(gi, s), walks.hydro_epj(np.sort(cand[d2 <= rj * rj]), s)))
+    el, sl = walks.gravity_lists(s["pos"], s["mass"], eps2, [groups[g] for g in take[:max(4, len(take) // 4)]],
+                                 near_factor=2.0, cell_frac=1.0 / 64)
+    for g, e, sp in zip(take, el, sl):
+        epj = np.concatenate([walks.gravity_epj(e, s), sp.view(abi.GravityEPJ)])
+        g_items.append((walks.gravity_epi(groups[g], s), epj))
+    smp = {"density": walks.concat_walks(d_items), "hydro": walks.concat_walks(h_items),
+           "gravity": walks.concat_walks(g_items)}
+    nthreads = os.cpu_count() or 1
+    # pair mix per step of this workload as sampled (scaled to all groups)
+    mix = {}
+    for k, (epi, epj, io, jo) in smp.items():
+        mix[k] = float(sum((io[w + 1] - io[w]) * (jo[w + 1] - jo[w]) for w in range(len(io) - 1)))
+    for _ in range(args.warmup):
+        oracle_rates({"gravity": smp["gravity"]}, nthreads)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rates = oracle_rates(smp, nthreads)
+        vals.append(combined_rate(rates, mix))
+    el_t = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
+            "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * el_t / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded polytropes (ic.config_system)",
+            "config": {"workload": f"{args.config}: off-axis unequal-mass collision, N={n}, n_group={args.n_group}, "
+                                   f"theta=0.5, eta={ETA}", "n_particles": n},
+            "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": nthreads, "kind": "port",
+                             "sample": f"{len(take)} of {len(groups)} walks per step (density, hydro; gravity "
+                                       f"{len(g_items)}), host-built lists; tree construction not included"},
+            "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+ETA = 1.18
+NODES = None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--n-group", type=int, default=256)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-frac", type=float, default=0.03)
+    ap.add_argument("--ref-frac", type=float, default=0.03)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("[bench] warm-up raised to 3 steps")
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

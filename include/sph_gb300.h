@@ -200,6 +200,15 @@ int  sph_context_set_eta(sph_context *ctx, double eta);
 int  sph_context_set_ksr_max(sph_context *ctx, double ksr_max);
 int  sph_context_set_precision(sph_context *ctx, int32_t precision);
 
+/* The context's CUDA stream (a cudaStream_t) for callers that order their
+ * own work or record events around the engine's calls. */
+int  sph_context_stream(const sph_context *ctx, void **stream);
+
+/* Measures the FP32 FMA throughput of the context's device (TFLOP/s) with a
+ * register-resident FMA loop on every SM: the denominator of the pair
+ * kernels' roofline. */
+int  sph_probe_fp32_peak(sph_context *ctx, double *tflops);
+
 /* Human-readable text for a status code (static storage). */
 const char *sph_status_string(int status);
 /* Detail text of the last failure on this context (copied into buf). */
@@ -365,6 +374,14 @@ int sph_system_get_stats(sph_system *sys, sph_system_stats *out);
  * *n_walk and *n_entries first. */
 int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t *n_entries,
                          int32_t *i_first, int32_t *i_count, int64_t *j_off, int32_t *j_idx);
+
+/* Device time (ms) of the phases of the most recent force evaluation,
+ * from CUDA events recorded on the context's stream (also inside a captured
+ * step): [0] tree + groups, [1] density incl. lists and all walks,
+ * [2] density pair kernel of the first walk, [3] gravity lists,
+ * [4] gravity pair kernel, [5] hydro prep + lists, [6] hydro pair kernel,
+ * [7] the whole force evaluation.  Returns the number of values written. */
+int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);
 
 /* Monopoles of the 2n-1 tree nodes: mom[4*k..] = (x, y, z, mass), eps2[k]. */
 int sph_system_get_nodes(sph_system *sys, double *mom, double *eps2);

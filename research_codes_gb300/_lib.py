@@ -56,6 +56,8 @@ def _declare(lib):
         "sph_retrieve_gravity": (ctypes.c_int, [_P, _I32, _I32, _PI32, _PP]),
         "sph_abi_layout": (_I64, [ctypes.POINTER(_I64), _I64]),
         "sph_version": (ctypes.c_char_p, []),
+        "sph_context_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+        "sph_probe_fp32_peak": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):

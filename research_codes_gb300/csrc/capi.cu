@@ -342,6 +342,49 @@ extern "C" int sph_context_set_precision(sph_context *ctx, int32_t precision) {
     return SPH_OK;
 }
 
+extern "C" int sph_context_stream(const sph_context *ctx, void **stream) {
+    if (!ctx || !stream) return SPH_ERR_INVALID_ARGUMENT;
+    *stream = (void *)ctx->stream;
+    return SPH_OK;
+}
+
+namespace {
+// Eight independent FMA chains per thread keep the FP32 pipe full.
+__global__ void fma_probe(float *out, int iters, float b, float c) {
+    float a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    for (int k = 0; k < iters; ++k) {
+        a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+        a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+    }
+    const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 1234.5f) out[0] = s;   // keeps the chains live
+}
+}  // namespace
+
+extern "C" int sph_probe_fp32_peak(sph_context *ctx, double *tflops) {
+    if (!ctx || !tflops) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->prm.device);
+    float *d = nullptr;
+    cudaEvent_t e0, e1;
+    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) return sphrt::set_error(ctx, SPH_ERR_CUDA, "probe alloc");
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int threads = 256, blocks = ctx->sm_count * 8, iters = 1 << 16;
+    fma_probe<<<blocks, threads, 0, ctx->stream>>>(d, 256, 0.999f, 1e-3f);   // warm-up
+    cudaEventRecord(e0, ctx->stream);
+    fma_probe<<<blocks, threads, 0, ctx->stream>>>(d, iters, 0.999f, 1e-3f);
+    cudaEventRecord(e1, ctx->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) return sphrt::cuda_error(ctx, e, "probe");
+    *tflops = 2.0 * 8.0 * (double)iters * threads * blocks / (ms * 1e-3) / 1e12;
+    return SPH_OK;
+}
+
 extern "C" int sph_context_last_error(const sph_context *ctx, char *buf, size_t n) {
     if (!ctx || !buf || n == 0) return SPH_ERR_INVALID_ARGUMENT;
     std::snprintf(buf, n, "%s", ctx->err);

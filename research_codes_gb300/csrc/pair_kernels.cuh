@@ -59,6 +59,7 @@ density_kernel(const DensityArgs a) {
     typedef typename Real<F64>::T4 R4;
     __shared__ R4 s_p[WARPS][32];
     __shared__ R4 s_v[WARPS][32];
+    __shared__ typename Real<F64>::T2 s_vl[WARPS][32];
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -89,7 +90,11 @@ density_kernel(const DensityArgs a) {
         const dbl4 pi = a.i_pm[ii];
         const dbl4 vi = a.i_vel[ii];
         const R xi = (R)(pi.x - cx), yi = (R)(pi.y - cy), zi = (R)(pi.z - cz);
+        // velocities as hi + lo pairs so that dv keeps FP32 relative accuracy
+        // even when the item's centre belongs to another stream
         const R vxi = (R)(vi.x - cvx), vyi = (R)(vi.y - cvy), vzi = (R)(vi.z - cvz);
+        const R lxi = (R)((vi.x - cvx) - (double)vxi), lyi = (R)((vi.y - cvy) - (double)vyi),
+                lzi = (R)((vi.z - cvz) - (double)vzi);
         const long long idi = a.i_id[ii];
         const double rs_i = a.i_rs[ii];
         const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
@@ -151,8 +156,10 @@ density_kernel(const DensityArgs a) {
                     const dbl4 v = a.j_vel[j];
                     s_p[wid][lane] = Real<F64>::make4((R)(p.x - cx), (R)(p.y - cy),
                                                       (R)(p.z - cz), (R)p.w);
-                    s_v[wid][lane] = Real<F64>::make4((R)(v.x - cvx), (R)(v.y - cvy),
-                                                      (R)(v.z - cvz), (R)0);
+                    const R hx = (R)(v.x - cvx), hy = (R)(v.y - cvy), hz = (R)(v.z - cvz);
+                    s_v[wid][lane] = Real<F64>::make4(hx, hy, hz, (R)((v.x - cvx) - (double)hx));
+                    s_vl[wid][lane] = Real<F64>::make2((R)((v.y - cvy) - (double)hy),
+                                                       (R)((v.z - cvz) - (double)hz));
                     s_id[wid][lane] = a.j_id[j];
                 }
                 __syncwarp();
@@ -162,7 +169,13 @@ density_kernel(const DensityArgs a) {
                     const R4 pj = s_p[wid][k];
                     const R4 vj = s_v[wid][k];
                     const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                    const R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
+                    R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
+                    if (!F64) {
+                        const typename Real<F64>::T2 vl = s_vl[wid][k];
+                        ux += lxi - vj.w;
+                        uy += lyi - vl.x;
+                        uz += lzi - vl.y;
+                    }
                     const R r2 = dx * dx + dy * dy + dz * dz;
                     const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
                     const R q = r2 * ri * hinv;
@@ -246,7 +259,8 @@ hydro_kernel(const HydroArgs a) {
     __shared__ R4 s_b[WARPS][32];   // dvx, dvy, dvz, hinv
     __shared__ R4 s_c[WARPS][32];   // pres - pres_c, presc, bswt, dens
     __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, thrm - thrm_c
-    __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, -, -
+    __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, dvx lo, dvy lo
+    __shared__ R s_f[WARPS][32];    // dvz lo
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -285,6 +299,8 @@ hydro_kernel(const HydroArgs a) {
         const long long idi = a.i_id[ii];
         const R xi = (R)(pi.x - cx), yi = (R)(pi.y - cy), zi = (R)(pi.z - cz);
         const R vxi = (R)(vi.x - cvx), vyi = (R)(vi.y - cvy), vzi = (R)(vi.z - cvz);
+        const R lxi = (R)((vi.x - cvx) - (double)vxi), lyi = (R)((vi.y - cvy) - (double)vyi),
+                lzi = (R)((vi.z - cvz) - (double)vzi);
         const R hi_i = (R)h1.x;
         const double hinv4_d = h1.x * h1.x * h1.x * h1.x;
         const R hi4_i = (R)hinv4_d;
@@ -304,11 +320,13 @@ hydro_kernel(const HydroArgs a) {
                 const dbl4 g2 = a.j_h2[j];
                 const double2 g3 = a.j_h3[j];
                 s_a[wid][lane] = Real<F64>::make4((R)(p.x - cx), (R)(p.y - cy), (R)(p.z - cz), (R)p.w);
-                s_b[wid][lane] = Real<F64>::make4((R)(v.x - cvx), (R)(v.y - cvy), (R)(v.z - cvz),
-                                                  (R)g1.x);
+                const R hx = (R)(v.x - cvx), hy = (R)(v.y - cvy), hz = (R)(v.z - cvz);
+                s_b[wid][lane] = Real<F64>::make4(hx, hy, hz, (R)g1.x);
                 s_c[wid][lane] = Real<F64>::make4((R)(g1.y - cp), (R)g1.z, (R)g1.w, (R)g2.x);
                 s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)(g3.x - cu));
-                s_e[wid][lane] = Real<F64>::make4((R)g3.y, (R)(g1.x * g1.x * g1.x * g1.x), (R)0, (R)0);
+                s_e[wid][lane] = Real<F64>::make4((R)g3.y, (R)(g1.x * g1.x * g1.x * g1.x),
+                                                  (R)((v.x - cvx) - (double)hx), (R)((v.y - cvy) - (double)hy));
+                s_f[wid][lane] = (R)((v.z - cvz) - (double)hz);
                 s_id[wid][lane] = a.j_id[j];
             }
             __syncwarp();
@@ -321,7 +339,12 @@ hydro_kernel(const HydroArgs a) {
                 const R4 D = s_d[wid][k];
                 const R4 E = s_e[wid][k];
                 const R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
-                const R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
+                R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
+                if (!F64) {
+                    ux += lxi - E.z;
+                    uy += lyi - E.w;
+                    uz += lzi - s_f[wid][k];
+                }
                 const R r2 = dx * dx + dy * dy + dz * dz;
                 const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
                 const R r = r2 * ri;

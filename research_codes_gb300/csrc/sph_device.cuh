@@ -32,7 +32,9 @@ struct Real;
 template <>
 struct Real<false> {
     typedef float T;
+    typedef float2 T2;
     typedef float4 T4;
+    __device__ static __forceinline__ float2 make2(float a, float b) { return make_float2(a, b); }
     __device__ static __forceinline__ float4 make4(float a, float b, float c, float d) {
         return make_float4(a, b, c, d);
     }
@@ -40,7 +42,9 @@ struct Real<false> {
 template <>
 struct Real<true> {
     typedef double T;
+    typedef double2 T2;
     typedef dbl4 T4;
+    __device__ static __forceinline__ double2 make2(double a, double b) { return make_double2(a, b); }
     __device__ static __forceinline__ dbl4 make4(double a, double b, double c, double d) {
         return make_dbl4(a, b, c, d);
     }

@@ -40,6 +40,9 @@ enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN
 enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_NI };
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
+// phase events
+enum { EV_TREE_B = 0, EV_TREE_E, EV_DENS_B, EV_DENSK_B, EV_DENSK_E, EV_DENS_E, EV_GLIST_B, EV_GK_B, EV_GK_E,
+       EV_HLIST_B, EV_HK_B, EV_HK_E, EV_END, EV_N };
 
 inline int grid_for(long long n, int threads = 256) {
     long long b = (n + threads - 1) / threads;
@@ -604,6 +607,9 @@ struct sph_system {
     // graph
     cudaGraphExec_t step_exec = nullptr;
     bool graph_valid = false;
+    int graph_precision = -1;
+    // phase events
+    cudaEvent_t ev[16] = {nullptr};
     long long steps = 0;
     int last_status = 0;
 
@@ -691,6 +697,7 @@ void reduce(sph_system *s, F f, double *out) {
 int build_tree(sph_system *s) {
     const int n = s->n;
     cudaStream_t st = s->st();
+    cudaEventRecord(s->ev[EV_TREE_B], st);
     bbox_stage1<<<RED_BLOCKS, RED_THREADS, 0, st>>>(s->pos[0].p, n, s->partial.p);
     bbox_stage2<<<1, 32, 0, st>>>(s->partial.p, RED_BLOCKS, s->box.p);
     sphtree::morton_keys<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, n, s->box.p, s->keys[0].p, s->perm[0].p);
@@ -731,6 +738,7 @@ int build_tree(sph_system *s) {
     if (r) return r;
     compact_groups<<<grid_for(n), 256, 0, st>>>(n, s->gflag.p, s->gscan.p, s->groot.p, t, s->group_node.p,
                                                 s->group_first.p, s->group_count.p, s->scal.p);
+    cudaEventRecord(s->ev[EV_TREE_E], st);
     return SPH_OK;
 }
 
@@ -796,6 +804,7 @@ int density_phase(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
+    cudaEventRecord(s->ev[EV_DENS_B], st);
     init_rs<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->rs.p);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_ITERS, 1);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_UNCONV, 0);
@@ -825,7 +834,9 @@ int density_phase(sph_system *s, bool eager) {
         a.eta_ksrh = ctx->prm.eta * KSRH;
         a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
         a.ksr_max_dev = (s->prm.ksr_max_mode == 1) ? s->dscal.p + D_KSRMAX : nullptr;
+        if (it == 0) cudaEventRecord(s->ev[EV_DENSK_B], st);
         sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
+        if (it == 0) cudaEventRecord(s->ev[EV_DENSK_E], st);
         commit_density<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, tmp, out, s->scal.p);
         iteration_end<<<1, 1, 0, st>>>(s->scal.p, max_it, it);
         if (eager) {
@@ -837,6 +848,7 @@ int density_phase(sph_system *s, bool eager) {
             if (walks <= it + 1) break;
         }
     }
+    cudaEventRecord(s->ev[EV_DENS_E], st);
     return SPH_OK;
 }
 
@@ -844,9 +856,11 @@ int gravity_phase(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
+    cudaEventRecord(s->ev[EV_GLIST_B], st);
     int r = build_lists_and_items(s, 2, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_G);
     if (r) return r;
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+    cudaEventRecord(s->ev[EV_GK_B], st);
     sphk::GravityArgs a;
     a.i_pe = s->pe.p;
     a.j_pm = s->pos[0].p; a.j_eps2 = s->eps2.p;
@@ -856,6 +870,7 @@ int gravity_phase(sph_system *s, bool eager) {
     a.j_off = s->loff[2].p; a.j_idx = s->jidx[2].p; a.queue = s->scal.p + S_QUEUE;
     a.o_acc = s->r_acc.p; a.o_pot = s->r_pot.p; a.o_eta = s->r_eta.p;
     sphrt::launch_gravity(a, ctx->prm.precision, ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st);
+    cudaEventRecord(s->ev[EV_GK_E], st);
     gravity_writeback<<<grid_for(n), 256, 0, st>>>(n, s->prm.G, s->r_acc.p, s->r_pot.p, s->r_eta.p, s->ksr[0].p,
                                                    s->grdh.p, s->dens.p, s->accg2.p, s->pot.p, s->eta.p);
     return SPH_OK;
@@ -865,12 +880,14 @@ int hydro_phase(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
+    cudaEventRecord(s->ev[EV_HLIST_B], st);
     hydro_prep<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->pres.p, s->grdh.p, s->dens.p, s->bswt.p,
                                             s->vsnd.p, s->alph[0].p, s->alphu[0].p, s->uene[0].p, s->eta.p,
                                             s->h1.p, s->h2.p, s->h3.p);
     int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
     if (r) return r;
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+    cudaEventRecord(s->ev[EV_HK_B], st);
     sphk::HydroArgs a;
     a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p;
     a.i_h1 = s->h1.p; a.i_h2 = s->h2.p; a.i_h3 = s->h3.p;
@@ -881,6 +898,7 @@ int hydro_phase(sph_system *s, bool eager) {
     a.o_acch = s->r_acch.p; a.o_accg = s->r_accg.p; a.o_udot = s->r_udot.p; a.o_vsmx = s->r_vsmx.p;
     a.o_diffu = s->r_diffu.p;
     sphrt::launch_hydro(a, ctx->prm.precision, ctx->grid[1][ctx->prm.precision == SPH_PREC_FP64], st);
+    cudaEventRecord(s->ev[EV_HK_E], st);
     AlphaParams ap{s->prm.alpha_max, s->prm.alpha_min, s->prm.alphu_max, s->prm.alphu_min};
     hydro_writeback<<<grid_for(n), 256, 0, st>>>(
         n, s->prm.G, s->r_acch.p, s->r_accg.p, s->r_udot.p, s->r_vsmx.p, s->r_diffu.p, s->acch.p, s->accg1.p,
@@ -924,6 +942,7 @@ int force_body(sph_system *s, bool eager) {
     Energy fe{};
     fe.pos = s->pos[0].p; fe.vel = s->vel[0].p; fe.uene = s->uene[0].p; fe.pot = s->pot.p;
     reduce(s, fe, s->dscal.p + D_EKIN);
+    cudaEventRecord(s->ev[EV_END], st);
     return SPH_OK;
 }
 
@@ -1003,6 +1022,7 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
         sph_system_destroy(s);
         return sphrt::set_error(ctx, SPH_ERR_CUDA, "system allocation for %lld particles failed", (long long)n);
     }
+    for (int k = 0; k < EV_N; ++k) cudaEventCreate(&s->ev[k]);
     cudaMemset(s->scal.p, 0, sizeof(int) * S_NI);
     cudaMemset(s->dscal.p, 0, sizeof(double) * D_NI);
     cudaMemset(s->lscal.p, 0, sizeof(long long) * L_NI);
@@ -1015,6 +1035,8 @@ extern "C" int sph_system_destroy(sph_system *s) {
     cudaSetDevice(s->ctx->prm.device);
     cudaStreamSynchronize(s->st());
     if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
+    for (int k = 0; k < EV_N; ++k)
+        if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->vel[k].release(); s->vel2[k].release(); s->id[k].release();
         s->istar[k].release(); s->orig[k].release(); s->uene[k].release(); s->uene2[k].release();
@@ -1130,6 +1152,7 @@ extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
     cudaStream_t st = s->st();
     for (int k = 0; k < n_steps; ++k) {
         int r = SPH_OK;
+        if (s->graph_precision != s->ctx->prm.precision) s->graph_valid = false;
         if (!s->prm.use_graph || !s->graph_valid) {
             // eager step (sizes lists, then the graph is captured for the next steps)
             r = step_body(s, true);
@@ -1149,6 +1172,7 @@ extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
                 cudaGraphDestroy(g);
                 if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaGraphInstantiate");
                 s->graph_valid = true;
+                s->graph_precision = s->ctx->prm.precision;
             }
         } else {
             CUDA_TRY(cudaGraphLaunch(s->step_exec, st));
@@ -1284,6 +1308,25 @@ extern "C" int sph_system_get_lists(sph_system *s, int32_t kind, int32_t *n_walk
     for (int w = 0; w < nw; ++w) j_off[w] = off[w];
     j_off[nw] = nw > 0 ? (int64_t)off[nw - 1] + cnt[nw - 1] : 0;
     return SPH_OK;
+}
+
+extern "C" int sph_system_phase_times(sph_system *s, float *ms, int32_t n) {
+    if (!s || !ms || n < 0) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    CUDA_TRY(cudaEventSynchronize(s->ev[EV_END]));
+    const int pairs[8][2] = {{EV_TREE_B, EV_TREE_E}, {EV_DENS_B, EV_DENS_E}, {EV_DENSK_B, EV_DENSK_E},
+                             {EV_GLIST_B, EV_GK_B},  {EV_GK_B, EV_GK_E},     {EV_HLIST_B, EV_HK_B},
+                             {EV_HK_B, EV_HK_E},     {EV_TREE_B, EV_END}};
+    int k = 0;
+    for (; k < n && k < 8; ++k) {
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, s->ev[pairs[k][0]], s->ev[pairs[k][1]]) != cudaSuccess) {
+            cudaGetLastError();
+            t = -1.0f;
+        }
+        ms[k] = t;
+    }
+    return k;
 }
 
 extern "C" int sph_system_get_nodes(sph_system *s, double *mom, double *eps2) {

@@ -80,6 +80,18 @@ class Context:
     def set_precision(self, precision):
         check(self.lib.sph_context_set_precision(self.handle, _PREC[precision]), self.handle)
 
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        p = ctypes.c_void_p()
+        check(self.lib.sph_context_stream(self.handle, ctypes.byref(p)), self.handle)
+        return p.value or 0
+
+    def probe_fp32_peak(self):
+        """Measured FP32 FMA throughput of the device, TFLOP/s."""
+        v = ctypes.c_double()
+        check(self.lib.sph_probe_fp32_peak(self.handle, ctypes.byref(v)), self.handle, "probe")
+        return v.value
+
 
 class calcDensity:
     """calcDensity::operator() (hdr_density.hpp:248-252); assigns force[:n_i]."""

@@ -61,6 +61,7 @@ def _declare(lib):
         "sph_system_get_lists": (ctypes.c_int, [_P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I64),
                                                 _P, _P, _P, _P]),
         "sph_system_get_nodes": (ctypes.c_int, [_P, _P, _P]),
+        "sph_system_phase_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), _I32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -156,6 +157,17 @@ class ParticleSystem:
                                             _ptr(i_first), _ptr(i_count), _ptr(j_off), _ptr(j_idx)),
               self.ctx.handle, "lists")
         return i_first[:nw.value], i_count[:nw.value], j_off, j_idx[:ne.value]
+
+    PHASES = ("tree", "density", "density_kernel", "gravity_lists", "gravity_kernel", "hydro_lists",
+              "hydro_kernel", "force_total")
+
+    def phase_times(self):
+        """Device ms of the phases of the last force evaluation (CUDA events)."""
+        buf = (ctypes.c_float * 8)()
+        k = self.lib.sph_system_phase_times(self.handle, buf, 8)
+        if k < 0:
+            check(k, self.ctx.handle, "phase_times")
+        return {name: float(buf[i]) for i, name in enumerate(self.PHASES[:k])}
 
     def nodes(self):
         mom = np.empty((2 * self.n - 1, 4), np.float64)
