@@ -380,7 +380,9 @@ int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t
  * step): [0] tree + groups, [1] density incl. lists and all walks,
  * [2] density pair kernel of the first walk, [3] gravity lists,
  * [4] gravity pair kernel, [5] hydro prep + lists, [6] hydro pair kernel,
- * [7] the whole force evaluation.  Returns the number of values written. */
+ * [7] the whole force evaluation.  Returns the number of values written,
+ * or minus a status code.  The events belong to eager evaluations
+ * (sph_system_compute_forces and non-captured steps). */
 int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);
 
 /* Monopoles of the 2n-1 tree nodes: mom[4*k..] = (x, y, z, mass), eps2[k]. */

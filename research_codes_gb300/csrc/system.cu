@@ -1311,9 +1311,10 @@ extern "C" int sph_system_get_lists(sph_system *s, int32_t kind, int32_t *n_walk
 }
 
 extern "C" int sph_system_phase_times(sph_system *s, float *ms, int32_t n) {
-    if (!s || !ms || n < 0) return SPH_ERR_INVALID_ARGUMENT;
+    if (!s || !ms || n < 0) return -SPH_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->ctx->prm.device);
-    CUDA_TRY(cudaEventSynchronize(s->ev[EV_END]));
+    const cudaError_t se = cudaEventSynchronize(s->ev[EV_END]);
+    if (se != cudaSuccess) return -sphrt::cuda_error(s->ctx, se, "cudaEventSynchronize");
     const int pairs[8][2] = {{EV_TREE_B, EV_TREE_E}, {EV_DENS_B, EV_DENS_E}, {EV_DENSK_B, EV_DENSK_E},
                              {EV_GLIST_B, EV_GK_B},  {EV_GK_B, EV_GK_E},     {EV_HLIST_B, EV_HK_B},
                              {EV_HK_B, EV_HK_E},     {EV_TREE_B, EV_END}};

@@ -166,7 +166,7 @@ class ParticleSystem:
         buf = (ctypes.c_float * 8)()
         k = self.lib.sph_system_phase_times(self.handle, buf, 8)
         if k < 0:
-            check(k, self.ctx.handle, "phase_times")
+            check(-k, self.ctx.handle, "phase_times")
         return {name: float(buf[i]) for i, name in enumerate(self.PHASES[:k])}
 
     def nodes(self):

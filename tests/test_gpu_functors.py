@@ -254,7 +254,8 @@ def test_gravity_functor_accumulates(ctx, golden):
 
 def test_capacity_and_state_errors(golden):
     g = golden
-    with functors.Context(max_walks=2, max_j=100) as c:
+    # the truncated j-lists below give rho = 0 (NaN outputs) by design
+    with functors.Context(max_walks=2, max_j=100, check_finite=False) as c:
         epi = g["dens_epi"][:4].copy()
         epj = g["dens_epj"][:200].copy()
         with pytest.raises(abi.SPHError) as e:
