@@ -558,10 +558,20 @@ extern "C" int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_wal
     if (nj > 0)
         unpack_density_j<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(
             (const sph_DensityEPJ *)(d + L.off_epj), nj, ks.a4[2].p, ks.a4[3].p, ks.id[1].p);
+    const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
+    if (f32 && ni > 0)
+        sphk::make_density_records<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(ni, ks.a4[0].p, ks.a4[1].p, ks.f4[0].p,
+                                                                             ks.f4[1].p, ks.f4[2].p, ks.f4[3].p);
+    if (f32 && nj > 0)
+        sphk::make_density_records<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(nj, ks.a4[2].p, ks.a4[3].p, ks.f4[4].p,
+                                                                             ks.f4[5].p, ks.f4[6].p, ks.f4[7].p);
     if (!ks.items.empty()) {
         sphk::DensityArgs a;
         a.i_pm = ks.a4[0].p; a.i_vel = ks.a4[1].p; a.i_id = ks.id[0].p; a.i_ksr = ks.d1[0].p; a.i_rs = ks.d1[1].p;
         a.j_pm = ks.a4[2].p; a.j_vel = ks.a4[3].p; a.j_id = ks.id[1].p;
+        a.fi = sphk::F32Part{ks.f4[0].p, ks.f4[1].p, ks.f4[2].p, ks.f4[3].p};
+        a.fj = sphk::F32Part{ks.f4[4].p, ks.f4[5].p, ks.f4[6].p, ks.f4[7].p};
+        a.i_list = nullptr;
         a.items = (const WorkItem *)(d + L.off_items);
         a.n_items = (int)ks.items.size();
         a.n_items_dev = nullptr;
@@ -625,12 +635,26 @@ extern "C" int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
         unpack_hydro<sph_HydroEPJ><<<eltwise_grid(nj), 256, 0, ctx->stream>>>(
             (const sph_HydroEPJ *)(d + L.off_epj), nj, true, ks.a4[2].p, ks.a4[3].p, ks.id[1].p,
             ks.a4[6].p, ks.a4[7].p, ks.a2[1].p);
+    const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
+    if (f32 && ni > 0)
+        sphk::make_hydro_records<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(
+            ni, ks.a4[0].p, ks.a4[1].p, ks.a4[4].p, ks.a4[5].p, ks.a2[0].p, ks.f4[0].p, ks.f4[1].p, ks.f4[2].p,
+            ks.f4[3].p, ks.f4[8].p, ks.f4[9].p, ks.f4[10].p);
+    if (f32 && nj > 0)
+        sphk::make_hydro_records<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(
+            nj, ks.a4[2].p, ks.a4[3].p, ks.a4[6].p, ks.a4[7].p, ks.a2[1].p, ks.f4[4].p, ks.f4[5].p, ks.f4[6].p,
+            ks.f4[7].p, ks.f4[11].p, ks.f4[12].p, ks.f4[13].p);
     if (!ks.items.empty()) {
         sphk::HydroArgs a;
         a.i_pm = ks.a4[0].p; a.i_vel = ks.a4[1].p; a.i_id = ks.id[0].p;
         a.i_h1 = ks.a4[4].p; a.i_h2 = ks.a4[5].p; a.i_h3 = ks.a2[0].p;
         a.j_pm = ks.a4[2].p; a.j_vel = ks.a4[3].p; a.j_id = ks.id[1].p;
         a.j_h1 = ks.a4[6].p; a.j_h2 = ks.a4[7].p; a.j_h3 = ks.a2[1].p;
+        a.fi = sphk::F32Part{ks.f4[0].p, ks.f4[1].p, ks.f4[2].p, ks.f4[3].p};
+        a.fj = sphk::F32Part{ks.f4[4].p, ks.f4[5].p, ks.f4[6].p, ks.f4[7].p};
+        a.fi_g1 = ks.f4[8].p; a.fi_g2 = ks.f4[9].p; a.fi_g3 = ks.f4[10].p;
+        a.fj_g1 = ks.f4[11].p; a.fj_g2 = ks.f4[12].p; a.fj_g3 = ks.f4[13].p;
+        a.i_list = nullptr;
         a.items = (const WorkItem *)(d + L.off_items);
         a.n_items = (int)ks.items.size();
         a.n_items_dev = nullptr;
@@ -693,11 +717,20 @@ extern "C" int sph_dispatch_gravity(sph_context *ctx, int32_t tag, int32_t n_wal
         unpack_gravity_i<<<eltwise_grid(ni), 256, 0, ctx->stream>>>((const sph_GravityEPI *)(d + L.off_epi), ni, ks.a4[0].p);
     if (nj > 0)
         unpack_gravity_j<<<eltwise_grid(nj), 256, 0, ctx->stream>>>((const sph_GravityEPJ *)(d + L.off_epj), nj, ks.a4[2].p, ks.d1[0].p);
+    const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
+    if (f32 && ni > 0)
+        sphk::make_gravity_records_pe<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(ni, ks.a4[0].p, ks.f4[0].p, ks.f4[1].p);
+    if (f32 && nj > 0)
+        sphk::make_gravity_records<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(nj, ks.a4[2].p, ks.d1[0].p, ks.f4[4].p,
+                                                                             ks.f4[5].p);
     if (!ks.items.empty()) {
         sphk::GravityArgs a;
         a.i_pe = ks.a4[0].p;
         a.j_pm = ks.a4[2].p; a.j_eps2 = ks.d1[0].p;
         a.s_pm = ks.a4[2].p; a.s_eps2 = ks.d1[0].p;
+        a.fi_phi = ks.f4[0].p; a.fi_plo = ks.f4[1].p;
+        a.f_phi = ks.f4[4].p; a.f_plo = ks.f4[5].p; a.f_shi = ks.f4[4].p; a.f_slo = ks.f4[5].p;
+        a.i_list = nullptr;
         a.n_split = 0x7fffffff;
         a.items = (const WorkItem *)(d + L.off_items);
         a.n_items = (int)ks.items.size();

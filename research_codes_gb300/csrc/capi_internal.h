@@ -70,6 +70,7 @@ struct KindState {
     HostBuf<char> h_in, h_out;
     DevBuf<char> d_in, d_out;
     DevBuf<dbl4> a4[8];
+    DevBuf<float4> f4[14];   // FP32C double-float records
     DevBuf<double2> a2[2];
     DevBuf<long long> id[2];
     DevBuf<double> d1[2];
@@ -88,6 +89,7 @@ struct KindState {
         e |= a4[2].ensure(nj) | a4[3].ensure(nj) | id[1].ensure(nj);
         for (int k = 0; k < 5; ++k) e |= o[k].ensure(ni);
         e |= o_np.ensure(ni) | o_itr.ensure(ni);
+        for (int k = 0; k < 4; ++k) e |= f4[k].ensure(ni) | f4[4 + k].ensure(nj);
         return e;
     }
     int ensure_hydro(size_t ni, size_t nj) {
@@ -98,12 +100,15 @@ struct KindState {
         e |= a2[1].ensure(nj) | id[1].ensure(nj);
         e |= o[0].ensure(3 * ni) | o[1].ensure(3 * ni);
         for (int k = 2; k < 5; ++k) e |= o[k].ensure(ni);
+        for (int k = 0; k < 4; ++k) e |= f4[k].ensure(ni) | f4[4 + k].ensure(nj);
+        for (int k = 8; k < 11; ++k) e |= f4[k].ensure(ni) | f4[k + 3].ensure(nj);
         return e;
     }
     int ensure_gravity(size_t ni, size_t nj) {
         int e = 0;
         e |= a4[0].ensure(ni) | a4[2].ensure(nj) | d1[0].ensure(nj);
         e |= o[0].ensure(3 * ni) | o[1].ensure(ni) | o[2].ensure(ni);
+        e |= f4[0].ensure(ni) | f4[1].ensure(ni) | f4[4].ensure(nj) | f4[5].ensure(nj);
         return e;
     }
     void release() {
@@ -112,6 +117,7 @@ struct KindState {
         d_in.release();
         d_out.release();
         for (auto &b : a4) b.release();
+        for (auto &b : f4) b.release();
         for (auto &b : a2) b.release();
         for (auto &b : id) b.release();
         for (auto &b : d1) b.release();

@@ -1,47 +1,90 @@
 // pair_kernels.cuh — the three SPH pair-interaction kernels.
 //
 // Design (shared by density, hydro and gravity):
-//  * Particle data live in HBM as FP64 structure-of-arrays (dbl4 packs).
 //  * Work is a list of WorkItems (<= 32 i-particles of one walk).  A
 //    persistent grid of warps pulls items from a global queue counter
-//    (atomicAdd), largest items first, so walks with very different
-//    neighbour counts balance across the 152 SMs.
+//    (atomicAdd), so walks with very different neighbour counts balance across
+//    the SMs.  Items may address their i-particles through an index list
+//    (search-radius re-walks recompute only the particles still iterating).
 //  * A warp streams its walk's j-list through a private 32-entry shared-memory
-//    tile: lane k loads entry t+k (gathered through j_idx when the list is an
-//    index list), converts it and stores it; every lane then reads the tile by
-//    broadcast.  With n_i < 32 several lanes share one i-particle (tpi lanes,
-//    strided over the tile) and are combined with warp shuffles.
-//  * FP32C mode (F64 == false): positions and velocities are taken relative to
-//    the first i-particle of the item in FP64 and rounded to FP32 at staging,
-//    so pair arithmetic sees small, well-conditioned differences; each lane's
-//    per-tile FP32 partial sums are folded into Kahan accumulators; the
-//    per-particle tail (h update, Omega, normalisation) runs in FP64.
+//    tile: lane k loads entry t+k (gathered through j_idx), converts it and
+//    stores it; every lane then reads the tile by broadcast.  With n_i < 32
+//    several lanes share one i-particle (tpi lanes, strided over the tile) and
+//    are combined with warp shuffles.
+//  * FP32C mode (F64 == false): the engine keeps double-float copies of the
+//    particle state (hi = float(x), lo = float(x - hi)).  Staging forms
+//    (hi_j - hi_c) + (lo_j - lo_c) relative to the item's first i-particle c
+//    in FP32, so pair differences keep FP32 relative accuracy far from the
+//    origin and across colliding streams, and no FP64 instruction runs in the
+//    pair loops (GB300's FP64 rate is ~1/60 of FP32).  Each lane's per-tile
+//    FP32 partial sums are folded into Kahan accumulators.
 //  * FP64 mode (F64 == true): the same kernels in plain FP64 on global
-//    coordinates, no compensation: the "plain FP64 GPU" comparator.
+//    coordinates without compensation: the "plain FP64 GPU" comparator.
 #pragma once
 
 #include "sph_device.cuh"
 
 namespace sphk {
 
+// Double-float particle records of FP32C mode.
+struct F32Part {
+    const float4 *phi;   // x_hi, y_hi, z_hi, mass
+    const float4 *plo;   // x_lo, y_lo, z_lo, aux
+    const float4 *vhi;   // vx_hi, vy_hi, vz_hi, aux
+    const float4 *vlo;   // vx_lo, vy_lo, vz_lo, aux
+};
+
+__device__ __forceinline__ float df_diff(float hi, float lo, float chi, float clo) {
+    return (hi - chi) + (lo - clo);
+}
+
+// Double-float split of an FP64 value: hi = float(x), lo = float(x - hi).
+__device__ __forceinline__ float2 df_split(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+
+struct ItemRef {   // decoded work item
+    int walk, jb, nj, tpi, sub, li, ii, ic;
+    bool act;
+};
+
+__device__ __forceinline__ ItemRef decode(const WorkItem &it, const int *j_off, const int *i_list, int lane) {
+    ItemRef r;
+    r.walk = it.x;
+    r.jb = j_off[it.x];
+    r.nj = j_off[it.x + 1] - r.jb;
+    r.tpi = lanes_per_i(it.z);
+    const int sh = ilog2_pow2(r.tpi);
+    r.li = lane >> sh;
+    r.sub = lane & (r.tpi - 1);
+    r.act = r.li < it.z;
+    const int k = it.y + (r.act ? r.li : 0);
+    r.ii = i_list ? i_list[k] : k;
+    r.ic = i_list ? i_list[it.y] : it.y;   // the item's centre particle
+    return r;
+}
+
 // ---------------------------------------------------------------- density
 struct DensityArgs {
-    // i-particles
-    const dbl4 *i_pm;    // x, y, z, mass
-    const dbl4 *i_vel;   // vx, vy, vz, -
-    const long long *i_id;
-    const double *i_ksr;    // first guess of h (DensityEPI::ksr)
-    const double *i_rs;     // search radius (DensityEPI::rs)
-    // j-particles
+    // FP64 records (i_pm is read in both modes for the i-particle's mass)
+    const dbl4 *i_pm;       // x, y, z, mass
+    const dbl4 *i_vel;      // vx, vy, vz, -
     const dbl4 *j_pm;
     const dbl4 *j_vel;
+    // FP32C mode records (phi.w = mass)
+    F32Part fi, fj;
+    const long long *i_id;
     const long long *j_id;
+    const double *i_ksr;    // first guess of h (DensityEPI::ksr)
+    const double *i_rs;     // search radius (DensityEPI::rs)
     // work
     const WorkItem *items;
     int n_items;
     const int *n_items_dev; // when set, the item count is read from device memory
     const int *j_off;       // per walk: [j_off[w], j_off[w+1]) in j index space
     const int *j_idx;       // null: entries are j indices themselves
+    const int *i_list;      // null: item i-particles are contiguous
     int *queue;             // item counter, 0 at launch
     // outputs, indexed like the i arrays
     double *o_dens, *o_divv, *o_rotv, *o_grdh, *o_ksr;
@@ -59,45 +102,43 @@ density_kernel(const DensityArgs a) {
     typedef typename Real<F64>::T4 R4;
     __shared__ R4 s_p[WARPS][32];
     __shared__ R4 s_v[WARPS][32];
-    __shared__ typename Real<F64>::T2 s_vl[WARPS][32];
+    __shared__ float2 s_vl[WARPS][32];
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
+    const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
 
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.queue, 1);
         item = __shfl_sync(FULL, item, 0);
         if (item >= n_items) return;
-        const WorkItem it = a.items[item];
-        const int jb = a.j_off[it.x];
-        const int nj = a.j_off[it.x + 1] - jb;
-        const int tpi = lanes_per_i(it.z);
-        const int sh = ilog2_pow2(tpi);
-        const int li = lane >> sh;
-        const int sub = lane & (tpi - 1);
-        const bool act = li < it.z;
-        const int ii = it.y + (act ? li : 0);
+        const ItemRef r = decode(a.items[item], a.j_off, a.i_list, lane);
+        const int tpi = r.tpi, sub = r.sub, ii = r.ii, nj = r.nj, jb = r.jb;
 
-        double cx = 0.0, cy = 0.0, cz = 0.0, cvx = 0.0, cvy = 0.0, cvz = 0.0;
-        if (!F64) {
-            const dbl4 c = a.i_pm[it.y];
-            const dbl4 v = a.i_vel[it.y];
-            cx = c.x; cy = c.y; cz = c.z;
-            cvx = v.x; cvy = v.y; cvz = v.z;
+        // i-particle relative to the centre particle c
+        R xi, yi, zi, vxi, vyi, vzi;
+        float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
+        float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
+        if (F64) {
+            const dbl4 p = a.i_pm[ii], v = a.i_vel[ii];
+            xi = (R)p.x; yi = (R)p.y; zi = (R)p.z;
+            vxi = (R)v.x; vyi = (R)v.y; vzi = (R)v.z;
+        } else {
+            cph = a.fi.phi[r.ic]; cpl = a.fi.plo[r.ic];
+            const float4 ph = a.fi.phi[ii], pl = a.fi.plo[ii], vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
+            xi = (R)df_diff(ph.x, pl.x, cph.x, cpl.x);
+            yi = (R)df_diff(ph.y, pl.y, cph.y, cpl.y);
+            zi = (R)df_diff(ph.z, pl.z, cph.z, cpl.z);
+            // velocities stay absolute hi/lo pairs and are differenced per
+            // pair: an item may straddle two colliding streams
+            vxi = vh.x; vyi = vh.y; vzi = vh.z;
+            lxi = vl.x; lyi = vl.y; lzi = vl.z;
         }
-        const dbl4 pi = a.i_pm[ii];
-        const dbl4 vi = a.i_vel[ii];
-        const R xi = (R)(pi.x - cx), yi = (R)(pi.y - cy), zi = (R)(pi.z - cz);
-        // velocities as hi + lo pairs so that dv keeps FP32 relative accuracy
-        // even when the item's centre belongs to another stream
-        const R vxi = (R)(vi.x - cvx), vyi = (R)(vi.y - cvy), vzi = (R)(vi.z - cvz);
-        const R lxi = (R)((vi.x - cvx) - (double)vxi), lyi = (R)((vi.y - cvy) - (double)vyi),
-                lzi = (R)((vi.z - cvz) - (double)vzi);
         const long long idi = a.i_id[ii];
         const double rs_i = a.i_rs[ii];
-        const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
+        const double mi = a.i_pm[ii].w;
         double h = a.i_ksr[ii];
         double rho = 0.0;
         long long np = 0;
@@ -105,17 +146,22 @@ density_kernel(const DensityArgs a) {
 
         // three fixed-point passes, hdr_density.hpp:264-302
         for (int pass = 0; pass < 3; ++pass) {
-            const double hinv_d = 1.0 / h;
-            const R hinv = (R)hinv_d;
+            const R hinv = (R)1 / (R)h;
             Acc<F64> acc;
             int cnt = 0;
             for (int t = 0; t < nj; t += 32) {
                 const int jk = t + lane;
                 if (jk < nj) {
                     const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                    const dbl4 p = a.j_pm[j];
-                    s_p[wid][lane] = Real<F64>::make4((R)(p.x - cx), (R)(p.y - cy),
-                                                      (R)(p.z - cz), (R)p.w);
+                    if (F64) {
+                        const dbl4 p = a.j_pm[j];
+                        s_p[wid][lane] = Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
+                    } else {
+                        const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
+                        s_p[wid][lane] = Real<F64>::make4(
+                            (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
+                            (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
+                    }
                 }
                 __syncwarp();
                 const int n = min(32, nj - t);
@@ -135,8 +181,19 @@ density_kernel(const DensityArgs a) {
             }
             const double sum = seg_sum(acc.value(), tpi);
             const long long c = seg_sum((long long)cnt, tpi);
-            rho = CEFF0 * hinv_d * hinv_d * hinv_d * sum;
-            double hn = a.eta_ksrh * cbrt(pi.w / rho);
+            double hn;
+            if (F64) {
+                const double hinv_d = 1.0 / h;
+                rho = CEFF0 * hinv_d * hinv_d * hinv_d * sum;
+                hn = a.eta_ksrh * cbrt(mi / rho);
+            } else {
+                // FP32 per-particle update (relative error ~1e-7, far inside
+                // the 1e-5 budget) keeps the FP64 pipe out of the loop
+                const float hinv_f = (float)hinv;
+                const float rho_f = (float)CEFF0 * hinv_f * hinv_f * hinv_f * (float)sum;
+                rho = (double)rho_f;
+                hn = (double)((float)a.eta_ksrh * cbrtf((float)mi / rho_f));
+            }
             hn = (hn < ksr_max) ? hn : ksr_max;
             np = c;
             itr = hn > rs_i;
@@ -145,21 +202,26 @@ density_kernel(const DensityArgs a) {
 
         // gradient pass with the final h, hdr_density.hpp:304-349
         {
-            const double hinv_d = 1.0 / h;
-            const R hinv = (R)hinv_d;
+            const R hinv = (R)1 / (R)h;
             Acc<F64> g_acc, d_acc, rx_acc, ry_acc, rz_acc;
             for (int t = 0; t < nj; t += 32) {
                 const int jk = t + lane;
                 if (jk < nj) {
                     const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                    const dbl4 p = a.j_pm[j];
-                    const dbl4 v = a.j_vel[j];
-                    s_p[wid][lane] = Real<F64>::make4((R)(p.x - cx), (R)(p.y - cy),
-                                                      (R)(p.z - cz), (R)p.w);
-                    const R hx = (R)(v.x - cvx), hy = (R)(v.y - cvy), hz = (R)(v.z - cvz);
-                    s_v[wid][lane] = Real<F64>::make4(hx, hy, hz, (R)((v.x - cvx) - (double)hx));
-                    s_vl[wid][lane] = Real<F64>::make2((R)((v.y - cvy) - (double)hy),
-                                                       (R)((v.z - cvz) - (double)hz));
+                    if (F64) {
+                        const dbl4 p = a.j_pm[j];
+                        const dbl4 v = a.j_vel[j];
+                        s_p[wid][lane] = Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
+                        s_v[wid][lane] = Real<F64>::make4((R)v.x, (R)v.y, (R)v.z, (R)0);
+                    } else {
+                        const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
+                        const float4 vh = a.fj.vhi[j], vl = a.fj.vlo[j];
+                        s_p[wid][lane] = Real<F64>::make4(
+                            (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
+                            (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
+                        s_v[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vl.x);
+                        s_vl[wid][lane] = make_float2(vl.y, vl.z);
+                    }
                     s_id[wid][lane] = a.j_id[j];
                 }
                 __syncwarp();
@@ -171,10 +233,10 @@ density_kernel(const DensityArgs a) {
                     const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
                     R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
                     if (!F64) {
-                        const typename Real<F64>::T2 vl = s_vl[wid][k];
-                        ux += lxi - vj.w;
-                        uy += lyi - vl.x;
-                        uz += lzi - vl.y;
+                        const float2 vl = s_vl[wid][k];
+                        ux += (R)(lxi - (float)vj.w);
+                        uy += (R)(lyi - vl.x);
+                        uz += (R)(lzi - vl.y);
                     }
                     const R r2 = dx * dx + dy * dy + dz * dz;
                     const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
@@ -199,20 +261,41 @@ density_kernel(const DensityArgs a) {
                 rz_acc.add(prz);
                 __syncwarp();
             }
-            const double hinv4 = hinv_d * hinv_d * hinv_d * hinv_d;
-            const double grdh = -hinv4 * seg_sum(g_acc.value(), tpi);
-            const double divv = -CEFF1 * hinv4 * seg_sum(d_acc.value(), tpi);
-            const double rx = CEFF1 * hinv4 * seg_sum(rx_acc.value(), tpi);
-            const double ry = CEFF1 * hinv4 * seg_sum(ry_acc.value(), tpi);
-            const double rz = CEFF1 * hinv4 * seg_sum(rz_acc.value(), tpi);
-            if (act && sub == 0) {
-                const double rhoinv = 1.0 / rho;
-                const double omega = 1.0 / (1.0 + h * rhoinv * grdh / 3.0);
-                const double rot2 = rx * rx + ry * ry + rz * rz;
-                const double rot = (rot2 != 0.0) ? sqrt(rot2) : 0.0;
+            const double sg = seg_sum(g_acc.value(), tpi);
+            const double sd = seg_sum(d_acc.value(), tpi);
+            const double sx = seg_sum(rx_acc.value(), tpi);
+            const double sy = seg_sum(ry_acc.value(), tpi);
+            const double sz = seg_sum(rz_acc.value(), tpi);
+            if (r.act && sub == 0) {
+                double divv, rotv, omega;
+                if (F64) {
+                    const double hinv_d = 1.0 / h;
+                    const double hinv4 = hinv_d * hinv_d * hinv_d * hinv_d;
+                    const double grdh = -hinv4 * sg;
+                    const double rx = CEFF1 * hinv4 * sx, ry = CEFF1 * hinv4 * sy, rz = CEFF1 * hinv4 * sz;
+                    const double rhoinv = 1.0 / rho;
+                    omega = 1.0 / (1.0 + h * rhoinv * grdh / 3.0);
+                    const double rot2 = rx * rx + ry * ry + rz * rz;
+                    const double rot = (rot2 != 0.0) ? sqrt(rot2) : 0.0;
+                    divv = -CEFF1 * hinv4 * sd * rhoinv * omega;
+                    rotv = rot * rhoinv * omega;
+                } else {
+                    const float hf = (float)h;
+                    const float hinv_f = 1.0f / hf;
+                    const float hinv4 = hinv_f * hinv_f * hinv_f * hinv_f;
+                    const float rinv = 1.0f / (float)rho;
+                    const float g = -hinv4 * (float)sg;
+                    const float xf = (float)CEFF1 * hinv4 * (float)sx, yf = (float)CEFF1 * hinv4 * (float)sy,
+                                zf = (float)CEFF1 * hinv4 * (float)sz;
+                    const float om = 1.0f / (1.0f + hf * rinv * g / 3.0f);
+                    const float rot2 = xf * xf + yf * yf + zf * zf;
+                    omega = om;
+                    divv = -(float)CEFF1 * hinv4 * (float)sd * rinv * om;
+                    rotv = ((rot2 != 0.0f) ? sqrtf(rot2) : 0.0f) * rinv * om;
+                }
                 a.o_dens[ii] = rho;
-                a.o_divv[ii] = divv * rhoinv * omega;
-                a.o_rotv[ii] = rot * rhoinv * omega;
+                a.o_divv[ii] = divv;
+                a.o_rotv[ii] = rotv;
                 a.o_grdh[ii] = omega;
                 a.o_ksr[ii] = h;
                 a.o_np[ii] = np;
@@ -224,29 +307,34 @@ density_kernel(const DensityArgs a) {
 
 // ---------------------------------------------------------------- hydro
 struct HydroArgs {
-    // i-particles (HydroEPI fields)
+    // FP64 mode records
     const dbl4 *i_pm;    // x, y, z, (mass unused)
     const dbl4 *i_vel;
-    const long long *i_id;
     const dbl4 *i_h1;    // hinv, pres, presc, bswt
     const dbl4 *i_h2;    // dens, vsnd, alph, alphu
-    const double2 *i_h3;    // thrm, eta
-    // j-particles (HydroEPJ fields)
+    const double2 *i_h3; // thrm, eta
     const dbl4 *j_pm;    // x, y, z, mass
     const dbl4 *j_vel;
-    const long long *j_id;
     const dbl4 *j_h1;
     const dbl4 *j_h2;
     const double2 *j_h3;
+    // FP32C mode records: vhi.w = hinv, vlo.w = hinv^4,
+    // g1 = (P_hi, P_lo, presc, bswt), g2 = (dens, vsnd, alph, alphu),
+    // g3 = (thrm_hi, thrm_lo, eta, -)
+    F32Part fi, fj;
+    const float4 *fi_g1, *fi_g2, *fi_g3, *fj_g1, *fj_g2, *fj_g3;
+    const long long *i_id;
+    const long long *j_id;
     const WorkItem *items;
     int n_items;
     const int *n_items_dev;
     const int *j_off;
     const int *j_idx;
+    const int *i_list;
     int *queue;
     // outputs
-    double *o_acch;         // 3 per particle
-    double *o_accg;         // 3 per particle
+    double *o_acch;      // 3 per particle
+    double *o_accg;      // 3 per particle
     double *o_udot, *o_vsmx, *o_diffu;
 };
 
@@ -256,11 +344,11 @@ hydro_kernel(const HydroArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
     __shared__ R4 s_a[WARPS][32];   // dx, dy, dz, mass
-    __shared__ R4 s_b[WARPS][32];   // dvx, dvy, dvz, hinv
-    __shared__ R4 s_c[WARPS][32];   // pres - pres_c, presc, bswt, dens
-    __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, thrm - thrm_c
-    __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, dvx lo, dvy lo
-    __shared__ R s_f[WARPS][32];    // dvz lo
+    __shared__ R4 s_b[WARPS][32];   // vx, vy, vz (hi), hinv
+    __shared__ R4 s_c[WARPS][32];   // dP (vs centre), presc, bswt, dens
+    __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, du (vs centre)
+    __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, vx lo, vy lo
+    __shared__ float s_f[WARPS][32];  // vz lo
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -271,42 +359,34 @@ hydro_kernel(const HydroArgs a) {
         if (lane == 0) item = atomicAdd(a.queue, 1);
         item = __shfl_sync(FULL, item, 0);
         if (item >= n_items) return;
-        const WorkItem it = a.items[item];
-        const int jb = a.j_off[it.x];
-        const int nj = a.j_off[it.x + 1] - jb;
-        const int tpi = lanes_per_i(it.z);
-        const int sh = ilog2_pow2(tpi);
-        const int li = lane >> sh;
-        const int sub = lane & (tpi - 1);
-        const bool act = li < it.z;
-        const int ii = it.y + (act ? li : 0);
+        const ItemRef r = decode(a.items[item], a.j_off, a.i_list, lane);
+        const int tpi = r.tpi, sub = r.sub, ii = r.ii, nj = r.nj, jb = r.jb;
 
-        // centre of the item: position, velocity, pressure, thermal energy
-        double cx = 0, cy = 0, cz = 0, cvx = 0, cvy = 0, cvz = 0, cp = 0, cu = 0;
-        if (!F64) {
-            const dbl4 c = a.i_pm[it.y];
-            const dbl4 v = a.i_vel[it.y];
-            cx = c.x; cy = c.y; cz = c.z;
-            cvx = v.x; cvy = v.y; cvz = v.z;
-            cp = a.i_h1[it.y].y;
-            cu = a.i_h3[it.y].x;
+        R xi, yi, zi, vxi, vyi, vzi, hi_i, hi4_i, pp_i, pc_i, bs_i, dn_i, cs_i, al_i, au_i, eg_i, et_i;
+        float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
+        float4 cph = make_float4(0, 0, 0, 0), cpl = cph, cg1 = cph, cg3 = cph;
+        if (F64) {
+            const dbl4 p = a.i_pm[ii], v = a.i_vel[ii], h1 = a.i_h1[ii], h2 = a.i_h2[ii];
+            const double2 h3 = a.i_h3[ii];
+            xi = p.x; yi = p.y; zi = p.z; vxi = v.x; vyi = v.y; vzi = v.z;
+            hi_i = h1.x; hi4_i = h1.x * h1.x * h1.x * h1.x; pp_i = h1.y; pc_i = h1.z; bs_i = h1.w;
+            dn_i = h2.x; cs_i = h2.y; al_i = h2.z; au_i = h2.w; eg_i = h3.x; et_i = h3.y;
+        } else {
+            cph = a.fi.phi[r.ic]; cpl = a.fi.plo[r.ic];
+            cg1 = a.fi_g1[r.ic]; cg3 = a.fi_g3[r.ic];
+            const float4 ph = a.fi.phi[ii], pl = a.fi.plo[ii], vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
+            const float4 g1 = a.fi_g1[ii], g2 = a.fi_g2[ii], g3 = a.fi_g3[ii];
+            xi = df_diff(ph.x, pl.x, cph.x, cpl.x);
+            yi = df_diff(ph.y, pl.y, cph.y, cpl.y);
+            zi = df_diff(ph.z, pl.z, cph.z, cpl.z);
+            vxi = vh.x; vyi = vh.y; vzi = vh.z;       // absolute hi/lo, differenced per pair
+            lxi = vl.x; lyi = vl.y; lzi = vl.z;
+            hi_i = vh.w; hi4_i = vl.w;
+            pp_i = df_diff(g1.x, g1.y, cg1.x, cg1.y); pc_i = g1.z; bs_i = g1.w;
+            dn_i = g2.x; cs_i = g2.y; al_i = g2.z; au_i = g2.w;
+            eg_i = df_diff(g3.x, g3.y, cg3.x, cg3.y); et_i = g3.z;
         }
-        const dbl4 pi = a.i_pm[ii];
-        const dbl4 vi = a.i_vel[ii];
-        const dbl4 h1 = a.i_h1[ii];
-        const dbl4 h2 = a.i_h2[ii];
-        const double2 h3 = a.i_h3[ii];
         const long long idi = a.i_id[ii];
-        const R xi = (R)(pi.x - cx), yi = (R)(pi.y - cy), zi = (R)(pi.z - cz);
-        const R vxi = (R)(vi.x - cvx), vyi = (R)(vi.y - cvy), vzi = (R)(vi.z - cvz);
-        const R lxi = (R)((vi.x - cvx) - (double)vxi), lyi = (R)((vi.y - cvy) - (double)vyi),
-                lzi = (R)((vi.z - cvz) - (double)vzi);
-        const R hi_i = (R)h1.x;
-        const double hinv4_d = h1.x * h1.x * h1.x * h1.x;
-        const R hi4_i = (R)hinv4_d;
-        const R pp_i = (R)(h1.y - cp), pc_i = (R)h1.z, bs_i = (R)h1.w;
-        const R dn_i = (R)h2.x, cs_i = (R)h2.y, al_i = (R)h2.z, au_i = (R)h2.w;
-        const R eg_i = (R)(h3.x - cu), et_i = (R)h3.y;
 
         Acc<F64> ax, ay, az, ud, df, gx, gy, gz;
         R vsmx = 0;
@@ -314,19 +394,28 @@ hydro_kernel(const HydroArgs a) {
             const int jk = t + lane;
             if (jk < nj) {
                 const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                const dbl4 p = a.j_pm[j];
-                const dbl4 v = a.j_vel[j];
-                const dbl4 g1 = a.j_h1[j];
-                const dbl4 g2 = a.j_h2[j];
-                const double2 g3 = a.j_h3[j];
-                s_a[wid][lane] = Real<F64>::make4((R)(p.x - cx), (R)(p.y - cy), (R)(p.z - cz), (R)p.w);
-                const R hx = (R)(v.x - cvx), hy = (R)(v.y - cvy), hz = (R)(v.z - cvz);
-                s_b[wid][lane] = Real<F64>::make4(hx, hy, hz, (R)g1.x);
-                s_c[wid][lane] = Real<F64>::make4((R)(g1.y - cp), (R)g1.z, (R)g1.w, (R)g2.x);
-                s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)(g3.x - cu));
-                s_e[wid][lane] = Real<F64>::make4((R)g3.y, (R)(g1.x * g1.x * g1.x * g1.x),
-                                                  (R)((v.x - cvx) - (double)hx), (R)((v.y - cvy) - (double)hy));
-                s_f[wid][lane] = (R)((v.z - cvz) - (double)hz);
+                if (F64) {
+                    const dbl4 p = a.j_pm[j], v = a.j_vel[j], g1 = a.j_h1[j], g2 = a.j_h2[j];
+                    const double2 g3 = a.j_h3[j];
+                    s_a[wid][lane] = Real<F64>::make4(p.x, p.y, p.z, p.w);
+                    s_b[wid][lane] = Real<F64>::make4(v.x, v.y, v.z, g1.x);
+                    s_c[wid][lane] = Real<F64>::make4(g1.y, g1.z, g1.w, g2.x);
+                    s_d[wid][lane] = Real<F64>::make4(g2.y, g2.z, g2.w, g3.x);
+                    s_e[wid][lane] = Real<F64>::make4(g3.y, g1.x * g1.x * g1.x * g1.x, 0.0, 0.0);
+                } else {
+                    const float4 ph = a.fj.phi[j], pl = a.fj.plo[j], vh = a.fj.vhi[j], vl = a.fj.vlo[j];
+                    const float4 g1 = a.fj_g1[j], g2 = a.fj_g2[j], g3 = a.fj_g3[j];
+                    s_a[wid][lane] = Real<F64>::make4(
+                        (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
+                        (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
+                    s_b[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vh.w);
+                    s_c[wid][lane] = Real<F64>::make4((R)df_diff(g1.x, g1.y, cg1.x, cg1.y), (R)g1.z, (R)g1.w,
+                                                      (R)g2.x);
+                    s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w,
+                                                      (R)df_diff(g3.x, g3.y, cg3.x, cg3.y));
+                    s_e[wid][lane] = Real<F64>::make4((R)g3.z, (R)vl.w, (R)vl.x, (R)vl.y);
+                    s_f[wid][lane] = vl.z;
+                }
                 s_id[wid][lane] = a.j_id[j];
             }
             __syncwarp();
@@ -341,15 +430,15 @@ hydro_kernel(const HydroArgs a) {
                 const R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
                 R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
                 if (!F64) {
-                    ux += lxi - E.z;
-                    uy += lyi - E.w;
-                    uz += lzi - s_f[wid][k];
+                    ux += (R)(lxi - (float)E.z);
+                    uy += (R)(lyi - (float)E.w);
+                    uz += (R)(lzi - s_f[wid][k]);
                 }
                 const R r2 = dx * dx + dy * dy + dz * dz;
                 const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
-                const R r = r2 * ri;
+                const R rr = r2 * ri;
                 // kernel gradients W1(q) for both smoothing lengths
-                const R qi = r * hi_i, qj = r * B.w;
+                const R qi = rr * hi_i, qj = rr * B.w;
                 const R ui = max0((R)1 - qi), uj = max0((R)1 - qj);
                 const R ui2 = ui * ui, uj2 = uj * uj;
                 const R w1i = ui2 * (ui2 - ui * ((R)1 + (R)4 * qi));
@@ -396,7 +485,7 @@ hydro_kernel(const HydroArgs a) {
         const double sdf = seg_sum(df.value(), tpi), sgx = seg_sum(gx.value(), tpi);
         const double sgy = seg_sum(gy.value(), tpi), sgz = seg_sum(gz.value(), tpi);
         const double svs = seg_max((double)vsmx, tpi);
-        if (act && sub == 0) {
+        if (r.act && sub == 0) {
             a.o_acch[3 * ii + 0] = 0.5 * sax;
             a.o_acch[3 * ii + 1] = 0.5 * say;
             a.o_acch[3 * ii + 2] = 0.5 * saz;
@@ -407,25 +496,29 @@ hydro_kernel(const HydroArgs a) {
             a.o_vsmx[ii] = svs;
             a.o_diffu[ii] = 2.0 * sdf;
         }
-        (void)hinv4_d;
     }
 }
 
 // ---------------------------------------------------------------- gravity
 struct GravityArgs {
-    const dbl4 *i_pe;    // x, y, z, eps2
-    // j sources: index k < n_split reads (j_pm, j_eps2)[k]; k >= n_split reads
+    // FP64 mode: i (x, y, z, eps2); j sources split at n_split: index
+    // k < n_split reads (j_pm, j_eps2)[k], k >= n_split reads
     // (s_pm, s_eps2)[k - n_split] (superparticles / tree-node monopoles)
-    const dbl4 *j_pm;    // x, y, z, mass
+    const dbl4 *i_pe;
+    const dbl4 *j_pm;       // x, y, z, mass
     const double *j_eps2;
     const dbl4 *s_pm;
     const double *s_eps2;
+    // FP32C mode: hi = (x, y, z, mass), lo = (x, y, z, eps2); fi_* for the
+    // i-particles, f_* for the j particles and f_s* for the monopoles
+    const float4 *fi_phi, *fi_plo, *f_phi, *f_plo, *f_shi, *f_slo;
     int n_split;
     const WorkItem *items;
     int n_items;
     const int *n_items_dev;
     const int *j_off;
     const int *j_idx;
+    const int *i_list;
     int *queue;
     double *o_acc;          // 3 per particle (assigned)
     double *o_pot, *o_eta;
@@ -447,40 +540,53 @@ gravity_kernel(const GravityArgs a) {
         if (lane == 0) item = atomicAdd(a.queue, 1);
         item = __shfl_sync(FULL, item, 0);
         if (item >= n_items) return;
-        const WorkItem it = a.items[item];
-        const int jb = a.j_off[it.x];
-        const int nj = a.j_off[it.x + 1] - jb;
-        const int tpi = lanes_per_i(it.z);
-        const int sh = ilog2_pow2(tpi);
-        const int li = lane >> sh;
-        const int sub = lane & (tpi - 1);
-        const bool act = li < it.z;
-        const int ii = it.y + (act ? li : 0);
+        const ItemRef r = decode(a.items[item], a.j_off, a.i_list, lane);
+        const int tpi = r.tpi, sub = r.sub, ii = r.ii, nj = r.nj, jb = r.jb;
 
-        double cx = 0, cy = 0, cz = 0;
-        if (!F64) {
-            const dbl4 c = a.i_pe[it.y];
-            cx = c.x; cy = c.y; cz = c.z;
+        R xi, yi, zi, e2i;
+        float4 ch = make_float4(0, 0, 0, 0), cl = ch;
+        if (F64) {
+            const dbl4 p = a.i_pe[ii];
+            xi = p.x; yi = p.y; zi = p.z; e2i = p.w;
+        } else {
+            ch = a.fi_phi[r.ic]; cl = a.fi_plo[r.ic];
+            const float4 h = a.fi_phi[ii], l = a.fi_plo[ii];
+            xi = df_diff(h.x, l.x, ch.x, cl.x);
+            yi = df_diff(h.y, l.y, ch.y, cl.y);
+            zi = df_diff(h.z, l.z, ch.z, cl.z);
+            e2i = l.w;
         }
-        const dbl4 pi = a.i_pe[ii];
-        const R xi = (R)(pi.x - cx), yi = (R)(pi.y - cy), zi = (R)(pi.z - cz);
-        const R e2i = (R)pi.w;
         Acc<F64> ax, ay, az, pt, et;
         for (int t = 0; t < nj; t += 32) {
             const int jk = t + lane;
             if (jk < nj) {
                 const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                dbl4 p;
-                double e2;
-                if (j < a.n_split) {
-                    p = a.j_pm[j];
-                    e2 = a.j_eps2[j];
+                if (F64) {
+                    dbl4 p;
+                    double e2;
+                    if (j < a.n_split) {
+                        p = a.j_pm[j];
+                        e2 = a.j_eps2[j];
+                    } else {
+                        p = a.s_pm[j - a.n_split];
+                        e2 = a.s_eps2[j - a.n_split];
+                    }
+                    s_p[wid][lane] = Real<F64>::make4(p.x, p.y, p.z, p.w);
+                    s_e[wid][lane] = e2;
                 } else {
-                    p = a.s_pm[j - a.n_split];
-                    e2 = a.s_eps2[j - a.n_split];
+                    float4 h, l;
+                    if (j < a.n_split) {
+                        h = a.f_phi[j];
+                        l = a.f_plo[j];
+                    } else {
+                        h = a.f_shi[j - a.n_split];
+                        l = a.f_slo[j - a.n_split];
+                    }
+                    s_p[wid][lane] = Real<F64>::make4((R)df_diff(h.x, l.x, ch.x, cl.x),
+                                                      (R)df_diff(h.y, l.y, ch.y, cl.y),
+                                                      (R)df_diff(h.z, l.z, ch.z, cl.z), (R)h.w);
+                    s_e[wid][lane] = (R)l.w;
                 }
-                s_p[wid][lane] = Real<F64>::make4((R)(p.x - cx), (R)(p.y - cy), (R)(p.z - cz), (R)p.w);
-                s_e[wid][lane] = (R)e2;
             }
             __syncwarp();
             const int n = min(32, nj - t);
@@ -510,13 +616,69 @@ gravity_kernel(const GravityArgs a) {
         const double sax = seg_sum(ax.value(), tpi), say = seg_sum(ay.value(), tpi);
         const double saz = seg_sum(az.value(), tpi), spt = seg_sum(pt.value(), tpi);
         const double set = seg_sum(et.value(), tpi);
-        if (act && sub == 0) {
+        if (r.act && sub == 0) {
             a.o_acc[3 * ii + 0] = 0.5 * sax;
             a.o_acc[3 * ii + 1] = 0.5 * say;
             a.o_acc[3 * ii + 2] = 0.5 * saz;
             a.o_pot[ii] = 0.5 * spt;
             a.o_eta[ii] = set;
         }
+    }
+}
+
+// ---------------------------------------------------------------- records
+// Builders of the FP32C double-float records from FP64 arrays (one thread
+// per particle).  Each fills hi/lo pairs; aux lanes as documented at the
+// consumers above.
+__global__ inline void make_density_records(int n, const dbl4 *pm, const dbl4 *vel, float4 *phi, float4 *plo,
+                                            float4 *vhi, float4 *vlo) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const dbl4 p = pm[k], v = vel[k];
+        const float2 x = df_split(p.x), y = df_split(p.y), z = df_split(p.z);
+        const float2 u = df_split(v.x), w = df_split(v.y), s = df_split(v.z);
+        phi[k] = make_float4(x.x, y.x, z.x, (float)p.w);
+        plo[k] = make_float4(x.y, y.y, z.y, 0.0f);
+        vhi[k] = make_float4(u.x, w.x, s.x, 0.0f);
+        vlo[k] = make_float4(u.y, w.y, s.y, 0.0f);
+    }
+}
+
+// Gravity records: hi = (x, y, z, mass), lo = (x, y, z, eps2).
+__global__ inline void make_gravity_records(int n, const dbl4 *pm, const double *eps2, float4 *phi, float4 *plo) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const dbl4 p = pm[k];
+        const float2 x = df_split(p.x), y = df_split(p.y), z = df_split(p.z);
+        phi[k] = make_float4(x.x, y.x, z.x, (float)p.w);
+        plo[k] = make_float4(x.y, y.y, z.y, (float)eps2[k]);
+    }
+}
+
+// The same from (x, y, z, eps2) packs without a mass (gravity i-particles).
+__global__ inline void make_gravity_records_pe(int n, const dbl4 *pe, float4 *phi, float4 *plo) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const dbl4 p = pe[k];
+        const float2 x = df_split(p.x), y = df_split(p.y), z = df_split(p.z);
+        phi[k] = make_float4(x.x, y.x, z.x, 0.0f);
+        plo[k] = make_float4(x.y, y.y, z.y, (float)p.w);
+    }
+}
+
+__global__ inline void make_hydro_records(int n, const dbl4 *pm, const dbl4 *vel, const dbl4 *h1, const dbl4 *h2,
+                                          const double2 *h3, float4 *phi, float4 *plo, float4 *vhi, float4 *vlo,
+                                          float4 *g1, float4 *g2, float4 *g3) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const dbl4 p = pm[k], v = vel[k], a = h1[k], b = h2[k];
+        const double2 c = h3[k];
+        const float2 x = df_split(p.x), y = df_split(p.y), z = df_split(p.z);
+        const float2 u = df_split(v.x), w = df_split(v.y), s = df_split(v.z);
+        const float2 P = df_split(a.y), T = df_split(c.x);
+        phi[k] = make_float4(x.x, y.x, z.x, (float)p.w);
+        plo[k] = make_float4(x.y, y.y, z.y, 0.0f);
+        vhi[k] = make_float4(u.x, w.x, s.x, (float)a.x);
+        vlo[k] = make_float4(u.y, w.y, s.y, (float)(a.x * a.x * a.x * a.x));
+        g1[k] = make_float4(P.x, P.y, (float)a.z, (float)a.w);
+        g2[k] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
+        g3[k] = make_float4(T.x, T.y, (float)c.y, 0.0f);
     }
 }
 

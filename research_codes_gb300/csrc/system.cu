@@ -289,13 +289,15 @@ __global__ void list_total(int n, const int *cnt, const int *off, long long cap,
     if (tot > cap) atomicOr(&scal[S_ERROR], E_LISTCAP);
 }
 
-// work items: walk k gets ceil(n_i/32) items
-__global__ void item_counts(int n, const int *n_walks, const int *i_count, int *c) {
+// work items: walk k gets ceil(n_i/chunk) items over its i-segment
+// [i_first[k], i_first[k] + i_count[k]) (particle indices or positions in
+// an index list)
+__global__ void item_counts(int n, const int *n_walks, const int *i_count, int chunk, int *c) {
     const int nw = *n_walks;
-    GRID_STRIDE(k, n) { c[k] = (k < nw) ? (i_count[k] + 31) / 32 : 0; }
+    GRID_STRIDE(k, n) { c[k] = (k < nw) ? (i_count[k] + chunk - 1) / chunk : 0; }
 }
 
-__global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count,
+__global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count, int chunk,
                            const int *item_off, const int *item_cnt, const int *j_off, const int *j_cnt,
                            WorkItem *items, int *n_items, long long *pairs) {
     const int nw = *n_walks;
@@ -306,8 +308,8 @@ __global__ void fill_items(int n, const int *n_walks, const int *i_first, const 
             const int ni = i_count[k];
             const int nj = j_cnt[k];
             for (int c = 0; c < item_cnt[k]; ++c) {
-                const int chunk = min(32, ni - 32 * c);
-                items[base + c] = make_int4(k, i_first[k] + 32 * c, chunk, nj * chunk);
+                const int sz = min(chunk, ni - chunk * c);
+                items[base + c] = make_int4(k, i_first[k] + chunk * c, sz, nj * sz);
             }
             local += (long long)ni * nj;
         }
@@ -315,6 +317,32 @@ __global__ void fill_items(int n, const int *n_walks, const int *i_first, const 
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd((unsigned long long *)pairs, (unsigned long long)local);
+}
+
+// particles still iterating (rs != 0) -> flags for the index list
+__global__ void iterating_flags(int n, const double *rs, int *flag) {
+    GRID_STRIDE(p, n) { flag[p] = rs[p] != 0.0 ? 1 : 0; }
+}
+
+__global__ void scatter_list(int n, const int *flag, const int *scan, int *list) {
+    GRID_STRIDE(p, n) {
+        if (flag[p]) list[scan[p]] = p;
+    }
+}
+
+// the index-list segment of each active walk
+__global__ void walk_segments(int n, const int *scal, const int *a_first, const int *a_count, const int *flag,
+                              const int *scan, int *seg_first, int *seg_count) {
+    const int nw = scal[S_NACTIVE];
+    GRID_STRIDE(k, n) {
+        if (k < nw) {
+            const int f = a_first[k], e = a_first[k] + a_count[k];
+            const int sf = scan[f];
+            const int se = (e < n) ? scan[e] : scan[n - 1] + flag[n - 1];
+            seg_first[k] = sf;
+            seg_count[k] = se - sf;
+        }
+    }
 }
 
 __global__ void init_rs(int n, const double *ksr, double *rs) {
@@ -582,6 +610,11 @@ struct sph_system {
     DevBuf<int> parent, first, count, visit;
     DevBuf<dbl4> lo, hi, mom;
     DevBuf<double> neps2;
+    DevBuf<float4> flo, fhi, fmom, ptest;
+    // FP32C double-float records (particles, hydro fields, tree monopoles)
+    DevBuf<float4> f_phi, f_plo, f_vhi, f_vlo, f_g1, f_g2, f_g3, f_shi, f_slo;
+    // re-walk index list (particles still iterating) and its per-walk segments
+    DevBuf<int> uflag, uscan, ulist, a_sfirst, a_scount;
     // groups and walks
     DevBuf<int> gflag, groot, gscan, group_node, group_first, group_count;
     DevBuf<int> aflag, ascan, a_node, a_first, a_count;
@@ -625,6 +658,7 @@ struct sph_system {
         sphtree::Nodes t;
         t.child = child.p; t.parent = parent.p; t.first = first.p; t.count = count.p; t.lo = lo.p;
         t.hi = hi.p; t.mom = mom.p; t.eps2 = neps2.p; t.visit = visit.p;
+        t.flo = flo.p; t.fhi = fhi.p; t.fmom = fmom.p; t.ptest = ptest.p;
         return t;
     }
 };
@@ -653,6 +687,11 @@ int alloc_all(sph_system *s) {
     e |= s->pe.ensure(n) | s->h1.ensure(n) | s->h2.ensure(n) | s->h3.ensure(n);
     e |= s->child.ensure(n) | s->parent.ensure(nn) | s->first.ensure(nn) | s->count.ensure(nn);
     e |= s->visit.ensure(n) | s->lo.ensure(nn) | s->hi.ensure(nn) | s->mom.ensure(nn) | s->neps2.ensure(nn);
+    e |= s->flo.ensure(nn) | s->fhi.ensure(nn) | s->fmom.ensure(nn) | s->ptest.ensure(n);
+    DevBuf<float4> *f1[] = {&s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo, &s->f_g1, &s->f_g2, &s->f_g3};
+    for (auto *b : f1) e |= b->ensure(n);
+    e |= s->f_shi.ensure(nn) | s->f_slo.ensure(nn);
+    e |= s->uflag.ensure(n) | s->uscan.ensure(n) | s->ulist.ensure(n) | s->a_sfirst.ensure(n) | s->a_scount.ensure(n);
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff};
     for (auto *b : i1) e |= b->ensure(n);
@@ -746,20 +785,20 @@ int build_tree(sph_system *s) {
 // matching work items.  In eager mode (no capture) the list capacity grows to
 // the counted total first.
 int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const double *walk_r, bool eager,
-                          long long *pairs) {
+                          long long *pairs, const int *item_first = nullptr, const int *item_count = nullptr,
+                          int chunk = 32) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sphtree::ListArgs a;
     a.t = s->nodes();
     a.n = n;
     a.root = 0;
-    a.pos = s->pos[0].p;
-    a.h = s->ksr[0].p;
+    a.box = s->box.p;
     a.n_groups = s->walk_num[kind];
     a.group_node = walk_node;
     a.r_group = walk_r;
     a.n_leaf = s->prm.n_leaf;
-    a.inv_theta2 = 1.0 / (s->prm.theta * s->prm.theta);
+    a.inv_theta2 = (float)(1.0 / (s->prm.theta * s->prm.theta));
     a.count_out = s->lcnt[kind].p;
     a.offset = s->loff[kind].p;
     a.error = s->scal.p + S_ERROR;
@@ -791,12 +830,14 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     if (mode == sphtree::SYMMETRIC) sphtree::build_lists<sphtree::SYMMETRIC, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
     if (mode == sphtree::GRAVITY) sphtree::build_lists<sphtree::GRAVITY, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
     // work items
-    item_counts<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], s->walk_count[kind], s->icnt.p);
+    const int *ifirst = item_first ? item_first : s->walk_first[kind];
+    const int *icount = item_count ? item_count : s->walk_count[kind];
+    item_counts<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, chunk, s->icnt.p);
     r = exclusive_scan(s, s->icnt.p, s->ioff.p);
     if (r) return r;
-    fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], s->walk_first[kind], s->walk_count[kind],
-                                            s->ioff.p, s->icnt.p, s->loff[kind].p, s->lcnt[kind].p, s->items.p,
-                                            s->scal.p + S_NITEMS, pairs);
+    fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], ifirst, icount, chunk, s->ioff.p, s->icnt.p,
+                                            s->loff[kind].p, s->lcnt[kind].p, s->items.p, s->scal.p + S_NITEMS,
+                                            pairs);
     return SPH_OK;
 }
 
@@ -805,6 +846,10 @@ int density_phase(sph_system *s, bool eager) {
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
     cudaEventRecord(s->ev[EV_DENS_B], st);
+    const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
+    if (f32)
+        sphk::make_density_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->vel[0].p, s->f_phi.p,
+                                                                s->f_plo.p, s->f_vhi.p, s->f_vlo.p);
     init_rs<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->rs.p);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_ITERS, 1);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_UNCONV, 0);
@@ -820,7 +865,15 @@ int density_phase(sph_system *s, bool eager) {
         compact_active<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->aflag.p, s->ascan.p, s->group_node.p,
                                                     s->group_first.p, s->group_count.p, s->g_r.p, s->a_node.p,
                                                     s->a_first.p, s->a_count.p, s->a_r.p, s->scal.p);
-        r = build_lists_and_items(s, 0, s->a_node.p, s->a_r.p, eager && it == 0, s->lscal.p + L_PAIRS_D);
+        // i-particles: only those still iterating (all of them in the first walk)
+        iterating_flags<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, s->uflag.p);
+        r = exclusive_scan(s, s->uflag.p, s->uscan.p);
+        if (r) return r;
+        scatter_list<<<grid_for(n), 256, 0, st>>>(n, s->uflag.p, s->uscan.p, s->ulist.p);
+        walk_segments<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->a_first.p, s->a_count.p, s->uflag.p,
+                                                   s->uscan.p, s->a_sfirst.p, s->a_scount.p);
+        r = build_lists_and_items(s, 0, s->a_node.p, s->a_r.p, eager && it == 0, s->lscal.p + L_PAIRS_D,
+                                  s->a_sfirst.p, s->a_scount.p, it == 0 ? 32 : 8);
         if (r) return r;
         CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
         sphk::DensityArgs a;
@@ -829,6 +882,9 @@ int density_phase(sph_system *s, bool eager) {
         a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
         a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
         a.j_off = s->loff[0].p; a.j_idx = s->jidx[0].p; a.queue = s->scal.p + S_QUEUE;
+        a.i_list = s->ulist.p;
+        a.fi = sphk::F32Part{s->f_phi.p, s->f_plo.p, s->f_vhi.p, s->f_vlo.p};
+        a.fj = a.fi;
         a.o_dens = tmp.dens; a.o_divv = tmp.divv; a.o_rotv = tmp.rotv; a.o_grdh = tmp.grdh; a.o_ksr = tmp.ksr;
         a.o_np = tmp.np; a.o_itr = tmp.itr;
         a.eta_ksrh = ctx->prm.eta * KSRH;
@@ -859,12 +915,20 @@ int gravity_phase(sph_system *s, bool eager) {
     cudaEventRecord(s->ev[EV_GLIST_B], st);
     int r = build_lists_and_items(s, 2, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_G);
     if (r) return r;
+    if (ctx->prm.precision == SPH_PREC_FP32C) {
+        sphk::make_gravity_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->eps2.p, s->f_phi.p, s->f_plo.p);
+        sphk::make_gravity_records<<<grid_for(2LL * n - 1), 256, 0, st>>>(2 * n - 1, s->mom.p, s->neps2.p,
+                                                                          s->f_shi.p, s->f_slo.p);
+    }
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_GK_B], st);
     sphk::GravityArgs a;
     a.i_pe = s->pe.p;
     a.j_pm = s->pos[0].p; a.j_eps2 = s->eps2.p;
     a.s_pm = s->mom.p; a.s_eps2 = s->neps2.p;
+    a.fi_phi = s->f_phi.p; a.fi_plo = s->f_plo.p; a.f_phi = s->f_phi.p; a.f_plo = s->f_plo.p;
+    a.f_shi = s->f_shi.p; a.f_slo = s->f_slo.p;
+    a.i_list = nullptr;
     a.n_split = n;
     a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
     a.j_off = s->loff[2].p; a.j_idx = s->jidx[2].p; a.queue = s->scal.p + S_QUEUE;
@@ -884,6 +948,10 @@ int hydro_phase(sph_system *s, bool eager) {
     hydro_prep<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->pres.p, s->grdh.p, s->dens.p, s->bswt.p,
                                             s->vsnd.p, s->alph[0].p, s->alphu[0].p, s->uene[0].p, s->eta.p,
                                             s->h1.p, s->h2.p, s->h3.p);
+    if (ctx->prm.precision == SPH_PREC_FP32C)
+        sphk::make_hydro_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->vel[0].p, s->h1.p, s->h2.p,
+                                                              s->h3.p, s->f_phi.p, s->f_plo.p, s->f_vhi.p,
+                                                              s->f_vlo.p, s->f_g1.p, s->f_g2.p, s->f_g3.p);
     int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
     if (r) return r;
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
@@ -893,6 +961,11 @@ int hydro_phase(sph_system *s, bool eager) {
     a.i_h1 = s->h1.p; a.i_h2 = s->h2.p; a.i_h3 = s->h3.p;
     a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
     a.j_h1 = s->h1.p; a.j_h2 = s->h2.p; a.j_h3 = s->h3.p;
+    a.fi = sphk::F32Part{s->f_phi.p, s->f_plo.p, s->f_vhi.p, s->f_vlo.p};
+    a.fj = a.fi;
+    a.fi_g1 = s->f_g1.p; a.fi_g2 = s->f_g2.p; a.fi_g3 = s->f_g3.p;
+    a.fj_g1 = s->f_g1.p; a.fj_g2 = s->f_g2.p; a.fj_g3 = s->f_g3.p;
+    a.i_list = nullptr;
     a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
     a.j_off = s->loff[1].p; a.j_idx = s->jidx[1].p; a.queue = s->scal.p + S_QUEUE;
     a.o_acch = s->r_acch.p; a.o_accg = s->r_accg.p; a.o_udot = s->r_udot.p; a.o_vsmx = s->r_vsmx.p;
@@ -1013,7 +1086,7 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
     s->ctx = ctx;
     s->n = (int)n;
     if (p) s->prm = *p; else sph_system_params_default(&s->prm);
-    if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || !(s->prm.theta > 0.0)) {
+    if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || s->prm.n_leaf > sphtree::MAX_LEAF || !(s->prm.theta > 0.0)) {
         delete s;
         return SPH_ERR_INVALID_ARGUMENT;
     }
@@ -1053,6 +1126,10 @@ extern "C" int sph_system_destroy(sph_system *s) {
     s->np.release(); s->t_np.release(); s->t_itr.release(); s->pe.release(); s->h1.release();
     s->h2.release(); s->h3.release(); s->child.release(); s->parent.release(); s->first.release();
     s->count.release(); s->visit.release(); s->lo.release(); s->hi.release(); s->mom.release();
+    DevBuf<float4> *f1[] = {&s->flo, &s->fhi, &s->fmom, &s->ptest, &s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo,
+                            &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
+    for (auto *b : f1) b->release();
+    s->uflag.release(); s->uscan.release(); s->ulist.release(); s->a_sfirst.release(); s->a_scount.release();
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff,
                          &s->scal};

@@ -44,6 +44,10 @@ struct Nodes {
     dbl4 *mom;        // centre of mass x, y, z; w = mass
     double *eps2;     // mass-weighted eps^2
     int *visit;       // refit arrival counters
+    float4 *flo;      // FP32 traversal copies: lo (rounded down), w = max h (up)
+    float4 *fhi;      // hi (rounded up), w = largest box side (up)
+    float4 *fmom;     // centre of mass, mass
+    float4 *ptest;    // per particle: position (nearest), h (rounded up)
 };
 
 // ---- 1. keys ------------------------------------------------------------
@@ -116,6 +120,18 @@ __device__ __forceinline__ dbl4 ldcg4(const dbl4 *p) {
     return make_dbl4(a.x, a.y, b.x, b.y);
 }
 
+// FP32 copies of the node geometry for the traversal: boxes rounded outwards,
+// h_max and size rounded up, so that FP32 tests are conservative.
+__device__ __forceinline__ void write_fgeom(const Nodes &t, int node, const dbl4 &lo, const dbl4 &hi,
+                                            const dbl4 &m) {
+    const double size = fmax(fmax(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
+    t.flo[node] = make_float4(__double2float_rd(lo.x), __double2float_rd(lo.y), __double2float_rd(lo.z),
+                              __double2float_ru(lo.w));
+    t.fhi[node] = make_float4(__double2float_ru(hi.x), __double2float_ru(hi.y), __double2float_ru(hi.z),
+                              __double2float_ru(size));
+    t.fmom[node] = make_float4((float)m.x, (float)m.y, (float)m.z, (float)m.w);
+}
+
 __global__ void refit(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes t) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
@@ -123,10 +139,15 @@ __global__ void refit(const dbl4 *pos, const double *h, const double *eps2, int 
     const dbl4 x = pos[p];
     t.first[node] = p;
     t.count[node] = 1;
-    t.lo[node] = make_dbl4(x.x, x.y, x.z, h[p]);
-    t.hi[node] = make_dbl4(x.x, x.y, x.z, 0.0);
-    t.mom[node] = make_dbl4(x.x, x.y, x.z, x.w);
+    const dbl4 l0 = make_dbl4(x.x, x.y, x.z, h[p]);
+    const dbl4 h0 = make_dbl4(x.x, x.y, x.z, 0.0);
+    const dbl4 m0 = make_dbl4(x.x, x.y, x.z, x.w);
+    t.lo[node] = l0;
+    t.hi[node] = h0;
+    t.mom[node] = m0;
     t.eps2[node] = eps2[p];
+    write_fgeom(t, node, l0, h0, m0);
+    t.ptest[p] = make_float4((float)x.x, (float)x.y, (float)x.z, __double2float_ru(h[p]));
     if (n == 1) return;
     node = t.parent[node];
     while (node >= 0) {
@@ -147,15 +168,18 @@ __global__ void refit(const dbl4 *pos, const double *h, const double *eps2, int 
         t.lo[node] = lo;
         t.hi[node] = hi;
         const double m = ma.w + mb.w;
+        dbl4 mom;
         if (m > 0.0) {
             const double mi = 1.0 / m;
-            t.mom[node] = make_dbl4((ma.w * ma.x + mb.w * mb.x) * mi, (ma.w * ma.y + mb.w * mb.y) * mi,
-                                    (ma.w * ma.z + mb.w * mb.z) * mi, m);
+            mom = make_dbl4((ma.w * ma.x + mb.w * mb.x) * mi, (ma.w * ma.y + mb.w * mb.y) * mi,
+                            (ma.w * ma.z + mb.w * mb.z) * mi, m);
             t.eps2[node] = (ma.w * ea + mb.w * eb) * mi;
         } else {
-            t.mom[node] = make_dbl4(0.5 * (lo.x + hi.x), 0.5 * (lo.y + hi.y), 0.5 * (lo.z + hi.z), 0.0);
+            mom = make_dbl4(0.5 * (lo.x + hi.x), 0.5 * (lo.y + hi.y), 0.5 * (lo.z + hi.z), 0.0);
             t.eps2[node] = 0.5 * (ea + eb);
         }
+        t.mom[node] = mom;
+        write_fgeom(t, node, lo, hi, mom);
         node = t.parent[node];
     }
 }
@@ -178,17 +202,19 @@ __global__ void mark_groups(Nodes t, int n, int n_group, int *flag, int *root_at
 // ---- 5. lists ---------------------------------------------------------------
 enum ListMode { GATHER = 0, SYMMETRIC = 1, GRAVITY = 2 };
 
+constexpr int CAND = 64;           // candidate buckets buffered per warp
+constexpr int MAX_LEAF = 8;        // n_leaf limit (bucket expansion buffer)
+
 struct ListArgs {
     Nodes t;
     int n;                  // particles
     int root;
-    const dbl4 *pos;        // sorted positions (w = mass)
-    const double *h;        // per-particle h (symmetric mode)
+    const double *box;      // global bounding box (min xyz, max xyz) of the step
     const int *n_groups;    // device count of groups to traverse
     const int *group_node;  // tree node of each group (indexed by position in this list)
     const double *r_group;  // gather: search radius of the group
-    int n_leaf;
-    double inv_theta2;
+    int n_leaf;             // <= MAX_LEAF
+    float inv_theta2;
     // pass 1 writes counts, pass 2 fills at offsets
     int *count_out;
     const int *offset;      // exclusive scan of counts (fill pass)
@@ -197,144 +223,155 @@ struct ListArgs {
     int *error;             // bit 1: stack overflow, bit 2: capacity exceeded
 };
 
-__device__ __forceinline__ double box_box_d2(const dbl4 &alo, const dbl4 &ahi, const dbl4 &blo,
-                                             const dbl4 &bhi) {
-    const double dx = fmax(0.0, fmax(alo.x - bhi.x, blo.x - ahi.x));
-    const double dy = fmax(0.0, fmax(alo.y - bhi.y, blo.y - ahi.y));
-    const double dz = fmax(0.0, fmax(alo.z - bhi.z, blo.z - ahi.z));
+__device__ __forceinline__ float box_box_d2f(const float4 &alo, const float4 &ahi, const float4 &blo,
+                                             const float4 &bhi) {
+    const float dx = fmaxf(0.0f, fmaxf(alo.x - bhi.x, blo.x - ahi.x));
+    const float dy = fmaxf(0.0f, fmaxf(alo.y - bhi.y, blo.y - ahi.y));
+    const float dz = fmaxf(0.0f, fmaxf(alo.z - bhi.z, blo.z - ahi.z));
     return dx * dx + dy * dy + dz * dz;
 }
 
-__device__ __forceinline__ double point_box_d2(double x, double y, double z, const dbl4 &lo,
-                                               const dbl4 &hi) {
-    const double dx = fmax(0.0, fmax(lo.x - x, x - hi.x));
-    const double dy = fmax(0.0, fmax(lo.y - y, y - hi.y));
-    const double dz = fmax(0.0, fmax(lo.z - z, z - hi.z));
+__device__ __forceinline__ float point_box_d2f(float x, float y, float z, const float4 &lo, const float4 &hi) {
+    const float dx = fmaxf(0.0f, fmaxf(lo.x - x, x - hi.x));
+    const float dy = fmaxf(0.0f, fmaxf(lo.y - y, y - hi.y));
+    const float dz = fmaxf(0.0f, fmaxf(lo.z - z, z - hi.z));
     return dx * dx + dy * dy + dz * dz;
 }
+
+// Search radius with FP32 safety margins: relative 2e-6 for the arithmetic,
+// plus an absolute term covering the rounding of coordinates to FP32.
+__device__ __forceinline__ float widen(float r, float slack) { return r * 1.000002f + slack; }
 
 template <int MODE, bool FILL>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
     __shared__ int stack[TRAV_WARPS][STACK];
+    __shared__ int cand[TRAV_WARPS][CAND];
+    __shared__ int cpre[TRAV_WARPS][CAND + 1];
+    __shared__ int pidx[TRAV_WARPS][CAND * MAX_LEAF];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int n_groups = *a.n_groups;
     const int warps = gridDim.x * TRAV_WARPS;
+    // coordinates were rounded to FP32: |error| <= 2^-24 max|x| per axis
+    const double cmax = fmax(fmax(fmax(fabs(a.box[0]), fabs(a.box[3])), fmax(fabs(a.box[1]), fabs(a.box[4]))),
+                             fmax(fabs(a.box[2]), fabs(a.box[5])));
+    const float slack = (float)(4.0e-7 * cmax);
     for (int g = blockIdx.x * TRAV_WARPS + wid; g < n_groups; g += warps) {
         const int gn = a.group_node[g];
-        const dbl4 glo = a.t.lo[gn];
-        const dbl4 ghi = a.t.hi[gn];
-        double rg = 0.0;
-        if (MODE == GATHER) rg = a.r_group[g];
-        if (MODE == SYMMETRIC) rg = glo.w;          // max h of the group
-        const double rg2 = rg * rg;
+        const float4 glo = a.t.flo[gn];
+        const float4 ghi = a.t.fhi[gn];
+        float rg = 0.0f;
+        if (MODE == GATHER) rg = __double2float_ru(a.r_group[g]);
+        if (MODE == SYMMETRIC) rg = glo.w;          // max h of the group (rounded up)
         long long out = FILL ? (long long)a.offset[g] : 0;
         int total = 0;
-        int sp = 0;
+        int sp = 1, nc = 0;
         if (lane == 0) stack[wid][0] = a.root;
-        sp = 1;
         __syncwarp();
         bool overflow = false;
-        while (sp > 0) {
-            const int take = min(sp, 32);
-            const int node = (lane < take) ? stack[wid][sp - take + lane] : -1;
-            sp -= take;
-            __syncwarp();
-            bool push = false;
-            int e_first = 0, e_cnt = 0;   // particle bucket [e_first, e_first + e_cnt)
-            bool e_test = false;          // bucket entries need the per-particle test
-            int e_node = -1;              // gravity: accepted node
-            int2 ch = make_int2(0, 0);
-            if (node >= 0) {
-                const dbl4 lo = a.t.lo[node];
-                const dbl4 hi = a.t.hi[node];
-                const int cnt = a.t.count[node];
-                const bool leafish = (node >= a.n - 1) || cnt <= a.n_leaf;
-                if (MODE == GRAVITY) {
-                    const dbl4 m = a.t.mom[node];
-                    const double d2 = point_box_d2(m.x, m.y, m.z, glo, ghi);
-                    const double sx = hi.x - lo.x, sy = hi.y - lo.y, sz = hi.z - lo.z;
-                    const double sz2 = fmax(fmax(sx * sx, sy * sy), sz * sz);
-                    if (d2 > sz2 * a.inv_theta2) {
-                        e_node = node;
-                    } else if (leafish) {
-                        e_first = a.t.first[node];
-                        e_cnt = cnt;
+        while (sp > 0 || nc > 0) {
+            if (sp > 0) {
+                const int take = min(sp, 32);
+                const int node = (lane < take) ? stack[wid][sp - take + lane] : -1;
+                sp -= take;
+                __syncwarp();
+                bool push = false, bucket = false, accept = false;
+                int2 ch = make_int2(0, 0);
+                if (node >= 0) {
+                    const float4 lo = a.t.flo[node];
+                    const float4 hi = a.t.fhi[node];
+                    const bool leafish = (node >= a.n - 1) || a.t.count[node] <= a.n_leaf;
+                    if (MODE == GRAVITY) {
+                        const float4 m = a.t.fmom[node];
+                        const float d2 = point_box_d2f(m.x, m.y, m.z, glo, ghi);
+                        if (d2 > hi.w * hi.w * a.inv_theta2) accept = true;
+                        else if (leafish) bucket = true;
+                        else push = true;
                     } else {
-                        push = true;
-                    }
-                } else {
-                    double r2 = rg2;
-                    if (MODE == SYMMETRIC) r2 = fmax(rg, lo.w) * fmax(rg, lo.w);
-                    if (box_box_d2(glo, ghi, lo, hi) <= r2) {
-                        if (leafish) {
-                            e_first = a.t.first[node];
-                            e_cnt = cnt;
-                            e_test = true;
-                        } else {
-                            push = true;
+                        const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, lo.w) : rg, slack);
+                        if (box_box_d2f(glo, ghi, lo, hi) <= r * r) {
+                            if (leafish) bucket = true;
+                            else push = true;
                         }
                     }
+                    if (push) ch = a.t.child[node];
                 }
-                if (push) ch = a.t.child[node];
-            }
-            // push children of opened nodes
-            const unsigned pm = __ballot_sync(FULL, push);
-            const int pre = __popc(pm & lt_mask);
-            if (sp + 2 * __popc(pm) > STACK) {
-                overflow = true;
-            } else if (push) {
-                stack[wid][sp + 2 * pre] = ch.y;
-                stack[wid][sp + 2 * pre + 1] = ch.x;
-            }
-            if (!overflow) sp += 2 * __popc(pm);
-            // entries of this lane
-            int mine = (e_node >= 0) ? 1 : 0;
-            if (e_cnt > 0) {
-                if (!e_test) {
-                    mine += e_cnt;
+                // children of opened nodes
+                const unsigned pm = __ballot_sync(FULL, push);
+                if (sp + 2 * __popc(pm) > STACK) {
+                    overflow = true;
                 } else {
-                    for (int k = 0; k < e_cnt; ++k) {
-                        const int p = e_first + k;
-                        const dbl4 x = a.pos[p];
-                        double r2 = rg2;
-                        if (MODE == SYMMETRIC) r2 = fmax(rg, a.h[p]) * fmax(rg, a.h[p]);
-                        mine += (point_box_d2(x.x, x.y, x.z, glo, ghi) <= r2) ? 1 : 0;
+                    if (push) {
+                        const int pre = __popc(pm & lt_mask);
+                        stack[wid][sp + 2 * pre] = ch.y;
+                        stack[wid][sp + 2 * pre + 1] = ch.x;
+                    }
+                    sp += 2 * __popc(pm);
+                }
+                // accepted monopoles (gravity)
+                if (MODE == GRAVITY) {
+                    const unsigned am = __ballot_sync(FULL, accept);
+                    if (FILL && accept) {
+                        const long long w = out + __popc(am & lt_mask);
+                        if (w < a.capacity) a.j_idx[w] = a.n + node;
+                        else atomicOr(a.error, 2);
+                    }
+                    out += __popc(am);
+                    total += __popc(am);
+                }
+                // particle buckets to test
+                const unsigned bm = __ballot_sync(FULL, bucket);
+                if (bucket) cand[wid][nc + __popc(bm & lt_mask)] = node;
+                nc += __popc(bm);
+                __syncwarp();
+            }
+            if (nc >= 32 || (sp == 0 && nc > 0) || (overflow && nc > 0)) {
+                // expand the buffered buckets into particle indices, then test
+                // 32 particles at a time
+                const int c0 = (lane < nc) ? a.t.count[cand[wid][lane]] : 0;
+                const int c1 = (lane + 32 < nc) ? a.t.count[cand[wid][lane + 32]] : 0;
+                int inc0 = c0, inc1 = c1;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v0 = __shfl_up_sync(FULL, inc0, o);
+                    const int v1 = __shfl_up_sync(FULL, inc1, o);
+                    if (lane >= o) {
+                        inc0 += v0;
+                        inc1 += v1;
                     }
                 }
-            }
-            // exclusive prefix over lanes
-            int incl = mine;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += v;
-            }
-            const int step_total = __shfl_sync(FULL, incl, 31);
-            if (FILL) {
-                long long w = out + (incl - mine);
-                if (w + mine <= a.capacity) {
-                    if (e_node >= 0) a.j_idx[w++] = a.n + e_node;
-                    if (e_cnt > 0) {
-                        for (int k = 0; k < e_cnt; ++k) {
-                            const int p = e_first + k;
-                            bool take_p = true;
-                            if (e_test) {
-                                const dbl4 x = a.pos[p];
-                                double r2 = rg2;
-                                if (MODE == SYMMETRIC) r2 = fmax(rg, a.h[p]) * fmax(rg, a.h[p]);
-                                take_p = point_box_d2(x.x, x.y, x.z, glo, ghi) <= r2;
-                            }
-                            if (take_p) a.j_idx[w++] = p;
-                        }
-                    }
-                } else if (mine > 0) {
-                    atomicOr(a.error, 2);
+                const int tot0 = __shfl_sync(FULL, inc0, 31);
+                const int base0 = inc0 - c0, base1 = tot0 + inc1 - c1;
+                const int tot = tot0 + __shfl_sync(FULL, inc1, 31);
+                if (lane < nc) {
+                    const int f = a.t.first[cand[wid][lane]];
+                    for (int k = 0; k < c0; ++k) pidx[wid][base0 + k] = f + k;
                 }
-                out += step_total;
+                if (lane + 32 < nc) {
+                    const int f = a.t.first[cand[wid][lane + 32]];
+                    for (int k = 0; k < c1; ++k) pidx[wid][base1 + k] = f + k;
+                }
+                __syncwarp();
+                for (int b = 0; b < tot; b += 32) {
+                    const int p = (b + lane < tot) ? pidx[wid][b + lane] : -1;
+                    bool ok = p >= 0;
+                    if (ok && MODE != GRAVITY) {
+                        const float4 x = a.t.ptest[p];
+                        const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, x.w) : rg, slack);
+                        ok = point_box_d2f(x.x, x.y, x.z, glo, ghi) <= r * r;
+                    }
+                    const unsigned om = __ballot_sync(FULL, ok);
+                    if (FILL && ok) {
+                        const long long w = out + __popc(om & lt_mask);
+                        if (w < a.capacity) a.j_idx[w] = p;
+                        else atomicOr(a.error, 2);
+                    }
+                    out += __popc(om);
+                    total += __popc(om);
+                }
+                nc = 0;
+                __syncwarp();
             }
-            total += step_total;
-            __syncwarp();
             if (overflow) break;
         }
         if (overflow && lane == 0) atomicOr(a.error, 1);
