@@ -328,7 +328,9 @@ typedef struct sph_system_stats {
     double  e_kin, e_thm, e_pot, e_tot;   /* FP64 sums, sum m(v^2/2), m u, m pot/2 */
     int64_t n_groups;
     int64_t density_iterations;           /* walks of the last density evaluation */
-    int64_t pairs_density;                /* sum over walks of n_i * n_j          */
+    int64_t pairs_density;                /* sum over walks of n_i * n_j, all
+                                             search-radius walks                  */
+    int64_t pairs_density_first;          /* the first density walk alone         */
     int64_t pairs_hydro;
     int64_t pairs_gravity;                /* particles + monopoles                */
     int64_t list_density, list_hydro, list_gravity;  /* list entries            */
@@ -366,8 +368,8 @@ int sph_system_download_sorted(sph_system *sys, int32_t field, double *out);
 
 int sph_system_get_stats(sph_system *sys, sph_system_stats *out);
 
-/* Interaction lists of the last force evaluation (kind 0 density — the last
- * search-radius expansion —, 1 hydro, 2 gravity), in Morton order:
+/* Interaction lists of the last force evaluation (kind 0 density — the first
+ * walk, which covers every group —, 1 hydro, 2 gravity), in Morton order:
  * walk w has i-particles [i_first[w], i_first[w] + i_count[w]) and list
  * entries j_idx[j_off[w] .. j_off[w+1]); for gravity an entry >= n is tree
  * node entry - n (see sph_system_get_nodes).  Call with null arrays to get

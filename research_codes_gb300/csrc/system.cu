@@ -37,7 +37,7 @@ enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, 
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
 // 64-bit counters
-enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_NI };
+enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_NI };
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
@@ -619,12 +619,13 @@ struct sph_system {
     DevBuf<int> gflag, groot, gscan, group_node, group_first, group_count;
     DevBuf<int> aflag, ascan, a_node, a_first, a_count;
     DevBuf<double> g_r, a_r;
-    // lists per kind (0 density, 1 hydro, 2 gravity)
-    DevBuf<int> lcnt[3], loff[3], jidx[3];
-    long long lcap[3] = {0, 0, 0};
-    int *walk_first[3] = {nullptr, nullptr, nullptr};
-    int *walk_count[3] = {nullptr, nullptr, nullptr};
-    int *walk_num[3] = {nullptr, nullptr, nullptr};   // device count of walks
+    // lists per kind: 0 density (first walk), 1 hydro, 2 gravity,
+    // 3 density re-walks (search radius expanded)
+    DevBuf<int> lcnt[4], loff[4], jidx[4];
+    long long lcap[4] = {0, 0, 0, 0};
+    int *walk_first[4] = {nullptr, nullptr, nullptr, nullptr};
+    int *walk_count[4] = {nullptr, nullptr, nullptr, nullptr};
+    int *walk_num[4] = {nullptr, nullptr, nullptr, nullptr};   // device count of walks
     DevBuf<int> icnt, ioff;
     DevBuf<WorkItem> items;
     // scalars
@@ -695,7 +696,7 @@ int alloc_all(sph_system *s) {
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff};
     for (auto *b : i1) e |= b->ensure(n);
-    for (int k = 0; k < 3; ++k) e |= s->lcnt[k].ensure(n) | s->loff[k].ensure(n);
+    for (int k = 0; k < 4; ++k) e |= s->lcnt[k].ensure(n) | s->loff[k].ensure(n);
     e |= s->items.ensure(n);
     e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
     e |= s->partial.ensure(RED_BLOCKS * MAX_RED) | s->box.ensure(8);
@@ -708,7 +709,9 @@ int alloc_all(sph_system *s) {
     cub::DeviceScan::ExclusiveSum(nullptr, b2, s->gflag.p, s->gscan.p, s->n);
     s->cub_bytes = std::max(b1, b2);
     e |= s->cub_tmp.ensure(s->cub_bytes);
-    s->walk_first[0] = s->a_first.p; s->walk_count[0] = s->a_count.p; s->walk_num[0] = s->scal.p + S_NACTIVE;
+    // the first density walk covers every group, in group order
+    s->walk_first[0] = s->group_first.p; s->walk_count[0] = s->group_count.p; s->walk_num[0] = s->scal.p + S_NGROUPS;
+    s->walk_first[3] = s->a_first.p; s->walk_count[3] = s->a_count.p; s->walk_num[3] = s->scal.p + S_NACTIVE;
     s->walk_first[1] = s->group_first.p; s->walk_count[1] = s->group_count.p; s->walk_num[1] = s->scal.p + S_NGROUPS;
     s->walk_first[2] = s->group_first.p; s->walk_count[2] = s->group_count.p; s->walk_num[2] = s->scal.p + S_NGROUPS;
     return e;
@@ -804,20 +807,22 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.error = s->scal.p + S_ERROR;
     const int tgrid = s->ctx->sm_count * 8;
     CUDA_TRY(cudaMemsetAsync(s->lcnt[kind].p, 0, sizeof(int) * (size_t)n, st));
-    const int mode = kind == 0 ? sphtree::GATHER : (kind == 1 ? sphtree::SYMMETRIC : sphtree::GRAVITY);
+    const int mode = (kind == 0 || kind == 3) ? sphtree::GATHER : (kind == 1 ? sphtree::SYMMETRIC : sphtree::GRAVITY);
     if (mode == sphtree::GATHER) sphtree::build_lists<sphtree::GATHER, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
     if (mode == sphtree::SYMMETRIC) sphtree::build_lists<sphtree::SYMMETRIC, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
     if (mode == sphtree::GRAVITY) sphtree::build_lists<sphtree::GRAVITY, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
     int r = exclusive_scan(s, s->lcnt[kind].p, s->loff[kind].p);
     if (r) return r;
-    const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : L_LIST_G);
+    const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : (kind == 2 ? L_LIST_G : L_LIST_R));
     if (eager) {
         list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, (long long)1 << 62, s->scal.p, s->lscal.p, lslot);
         long long tot = 0;
         CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         if (tot + 1 > s->lcap[kind]) {
-            if (s->jidx[kind].ensure((size_t)(tot + tot / 2 + 1024)))
+            long long want = tot + tot / 2 + 1024;
+            if (kind == 3) want = std::max(want, s->lcap[0]);   // re-walks may cover many walks
+            if (s->jidx[kind].ensure((size_t)want))
                 return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list allocation of %lld entries failed", tot);
             s->lcap[kind] = (long long)s->jidx[kind].cap;
             s->graph_valid = false;
@@ -872,7 +877,8 @@ int density_phase(sph_system *s, bool eager) {
         scatter_list<<<grid_for(n), 256, 0, st>>>(n, s->uflag.p, s->uscan.p, s->ulist.p);
         walk_segments<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->a_first.p, s->a_count.p, s->uflag.p,
                                                    s->uscan.p, s->a_sfirst.p, s->a_scount.p);
-        r = build_lists_and_items(s, 0, s->a_node.p, s->a_r.p, eager && it == 0, s->lscal.p + L_PAIRS_D,
+        const int kind = it == 0 ? 0 : 3;
+        r = build_lists_and_items(s, kind, s->a_node.p, s->a_r.p, eager, s->lscal.p + (it == 0 ? L_PAIRS_D1 : L_PAIRS_D),
                                   s->a_sfirst.p, s->a_scount.p, it == 0 ? 32 : 8);
         if (r) return r;
         CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
@@ -881,7 +887,7 @@ int density_phase(sph_system *s, bool eager) {
         a.i_rs = s->rs.p;
         a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
         a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
-        a.j_off = s->loff[0].p; a.j_idx = s->jidx[0].p; a.queue = s->scal.p + S_QUEUE;
+        a.j_off = s->loff[kind].p; a.j_idx = s->jidx[kind].p; a.queue = s->scal.p + S_QUEUE;
         a.i_list = s->ulist.p;
         a.fi = sphk::F32Part{s->f_phi.p, s->f_plo.p, s->f_vhi.p, s->f_vlo.p};
         a.fj = a.fi;
@@ -1134,7 +1140,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff,
                          &s->scal};
     for (auto *b : i1) b->release();
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         s->lcnt[k].release(); s->loff[k].release(); s->jidx[k].release();
     }
     s->items.release(); s->lscal.release(); s->cub_tmp.release();
@@ -1347,7 +1353,8 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->e_tot = dc[D_EKIN] + dc[D_ETHM] + dc[D_EPOT];
     o->n_groups = sc[S_NGROUPS];
     o->density_iterations = sc[S_ITERS];
-    o->pairs_density = lc[L_PAIRS_D];
+    o->pairs_density = lc[L_PAIRS_D] + lc[L_PAIRS_D1];
+    o->pairs_density_first = lc[L_PAIRS_D1];
     o->pairs_hydro = lc[L_PAIRS_H];
     o->pairs_gravity = lc[L_PAIRS_G];
     o->list_density = lc[L_LIST_D];

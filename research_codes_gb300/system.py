@@ -40,7 +40,7 @@ class SystemParams(ctypes.Structure):
 class SystemStats(ctypes.Structure):
     _fields_ = [("time", _D), ("dt", _D), ("ksr_max", _D), ("e_kin", _D), ("e_thm", _D), ("e_pot", _D),
                 ("e_tot", _D), ("n_groups", _I64), ("density_iterations", _I64), ("pairs_density", _I64),
-                ("pairs_hydro", _I64), ("pairs_gravity", _I64), ("list_density", _I64),
+                ("pairs_density_first", _I64), ("pairs_hydro", _I64), ("pairs_gravity", _I64), ("list_density", _I64),
                 ("list_hydro", _I64), ("list_gravity", _I64), ("steps", _I64), ("last_status", _I32)]
 
     def as_dict(self):

@@ -177,19 +177,23 @@ def _collision_system(seed, n=3000):
 
 @pytest.mark.parametrize("seed", [11, 12])
 def test_density_vs_oracle_collision(ctx, seed):
+    """Errors judged over all walks together (the field's own scale)."""
     s, _ = _collision_system(seed)
     groups = walks.make_groups(s["pos"], 100)
     jl = walks.gather_lists(s["pos"], s["rs"], groups)
     ctx.set_eta(1.2)
+    outs, refs = [], []
     try:
         f = functors.calcDensity(ctx)
         for g, j in list(zip(groups, jl))[::2]:
             epi, epj = walks.density_epi(g, s), walks.density_epj(j, s)
             out = np.zeros(len(epi), abi.Density)
             f(epi, len(epi), epj, len(epj), out)
-            check_density(ctx, out, orc.density(epi, epj, eta=1.2))
+            outs.append(out)
+            refs.append(orc.density(epi, epj, eta=1.2))
     finally:
         ctx.set_eta(1.6)
+    check_density(ctx, np.concatenate(outs), np.concatenate(refs))
 
 
 def test_hydro_gravity_vs_oracle_collision(ctx):
@@ -202,20 +206,26 @@ def test_hydro_gravity_vs_oracle_collision(ctx):
     groups = walks.make_groups(s["pos"], 64)
     hl = walks.symmetric_lists(s["pos"], s["ksr"], groups)
     fh = functors.calcHydro(ctx)
+    outs, refs = [], []
     for g, j in list(zip(groups, hl))[::5]:
         epi, epj = walks.hydro_epi(g, s), walks.hydro_epj(j, s)
         out = np.zeros(len(epi), abi.Hydro)
         fh(epi, len(epi), epj, len(epj), out)
-        check_hydro(ctx, out, orc.hydro(epi, epj))
+        outs.append(out)
+        refs.append(orc.hydro(epi, epj))
+    check_hydro(ctx, np.concatenate(outs), np.concatenate(refs))
     fg = functors.calcGravity(ctx)
     eps2 = (s["ksr"] / 1.936492) ** 2
     el, sl = walks.gravity_lists(s["pos"], s["mass"], eps2, groups, near_factor=1.0, cell_frac=0.1)
+    outs, refs = [], []
     for g, e, sp in list(zip(groups, el, sl))[::7]:
         epi, epj = walks.gravity_epi(g, s), walks.gravity_epj(e, s)
         out = np.zeros(len(epi), abi.Gravity)
         fg(epi, len(epi), epj, len(epj), out)
         fg(epi, len(epi), sp, len(sp), out)
-        check_gravity(ctx, out, orc.gravity(epi, epj, sp))
+        outs.append(out)
+        refs.append(orc.gravity(epi, epj, sp))
+    check_gravity(ctx, np.concatenate(outs), np.concatenate(refs))
 
 
 # ---- edge cases ---------------------------------------------------------------
