@@ -335,6 +335,8 @@ typedef struct sph_system_stats {
     int64_t pairs_gravity;                /* particles + monopoles                */
     int64_t list_density, list_hydro, list_gravity;  /* list entries            */
     int64_t steps;
+    int64_t density_rechecked;            /* FP32C results re-evaluated in FP64
+                                             because h fell within 4e-6 of rs    */
     int32_t last_status;
 } sph_system_stats;
 
@@ -360,6 +362,10 @@ int sph_system_compute_forces(sph_system *sys);
 /* n_steps iterations of the reference's loop body: time step, predict,
  * calcSPHKernel, correct. */
 int sph_system_step(sph_system *sys, int32_t n_steps);
+
+/* Switches CUDA-graph replay of compute_forces / step on or off (off: every
+ * call runs eagerly, e.g. for per-phase event timings). */
+int sph_system_set_graph(sph_system *sys, int32_t use_graph);
 
 /* Device -> host copy of one field in upload order (3 or 1 doubles each). */
 int sph_system_download(sph_system *sys, int32_t field, double *out);

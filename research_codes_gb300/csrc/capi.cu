@@ -47,6 +47,10 @@ using sphk::WorkItem;
 
 namespace sphrt {
 
+// Relative band |h - rs| <= AMB_TOL * rs in which an FP32C density result is
+// recomputed in FP64 (FP32 h carries ~1e-7 relative error).
+const float AMB_TOL = 4.0e-6f;
+
 int set_error(sph_context *ctx, int status, const char *fmt, ...) {
     if (ctx) {
         va_list ap;
@@ -583,7 +587,32 @@ extern "C" int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_wal
         a.eta_ksrh = ctx->prm.eta * sphk::KSRH;
         a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
         a.ksr_max_dev = nullptr;
+        const int cap = std::max(256, ni / 16);
+        if (ks.amb_i.ensure(cap) || ks.amb_w.ensure(cap) || ks.fitems.ensure(cap))
+            return set_error(ctx, SPH_ERR_CUDA, "allocation failed");
+        a.amb_count = f32 ? ctx->d_queue + 3 : nullptr;
+        a.amb_i = ks.amb_i.p;
+        a.amb_w = ks.amb_w.p;
+        a.amb_cap = cap;
+        a.amb_tol = AMB_TOL;
+        if (f32) {
+            cudaError_t e = cudaMemsetAsync(ctx->d_queue + 3, 0, sizeof(int), ctx->stream);
+            if (e != cudaSuccess) return cuda_error(ctx, e, "memset");
+        }
         launch_density(a, ctx->prm.precision, pair_grid(ctx, K_DENS, ctx->prm.precision, a.n_items), ctx->stream);
+        if (f32) {
+            // FP64 recomputation of the particles queued as decision-ambiguous
+            sphk::make_fixup_items<<<1, 256, 0, ctx->stream>>>(ctx->d_queue + 3, ks.amb_w.p, cap, ks.fitems.p,
+                                                                ctx->d_queue + 7);
+            cudaError_t e = cudaMemsetAsync(ctx->d_queue + K_DENS, 0, sizeof(int), ctx->stream);
+            if (e != cudaSuccess) return cuda_error(ctx, e, "memset");
+            sphk::DensityArgs f = a;
+            f.items = ks.fitems.p;
+            f.n_items_dev = ctx->d_queue + 7;
+            f.i_list = ks.amb_i.p;
+            f.amb_count = nullptr;
+            launch_density(f, SPH_PREC_FP64, pair_grid(ctx, K_DENS, SPH_PREC_FP64, cap), ctx->stream);
+        }
     }
     if (ni > 0)
         pack_density<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(

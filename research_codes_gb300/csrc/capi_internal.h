@@ -77,6 +77,8 @@ struct KindState {
     DevBuf<double> o[5];
     DevBuf<long long> o_np;
     DevBuf<unsigned char> o_itr;
+    DevBuf<int> amb_i, amb_w;          // FP64 re-check queue of the density
+    DevBuf<int4> fitems;
     std::vector<int4> items;
     std::vector<int> i_off;
     bool pending = false;
@@ -124,6 +126,9 @@ struct KindState {
         for (auto &b : o) b.release();
         o_np.release();
         o_itr.release();
+        amb_i.release();
+        amb_w.release();
+        fitems.release();
     }
 };
 
@@ -133,7 +138,8 @@ struct sph_context {
     sph_params prm;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
-    int *d_queue = nullptr;   // [0..2] work-queue counters, [4..6] finite flags
+    int *d_queue = nullptr;   // [0..2] work-queue counters, [3] density re-check count,
+                              // [4..6] finite flags, [7] re-check item count
     int *h_flags = nullptr;   // pinned copies of the flags
     int grid[3][2] = {{0}};   // persistent grid per kind and precision
     sphrt::KindState kind[3];
@@ -141,6 +147,7 @@ struct sph_context {
 };
 
 namespace sphrt {
+extern const float AMB_TOL;
 int set_error(sph_context *ctx, int status, const char *fmt, ...);
 int cuda_error(sph_context *ctx, cudaError_t e, const char *what);
 int pair_grid(const sph_context *ctx, int kind, int precision, int n_items);

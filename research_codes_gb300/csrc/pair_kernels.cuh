@@ -93,6 +93,14 @@ struct DensityArgs {
     double eta_ksrh;        // eta * ksrh
     double ksr_max;         // clamp of h (+inf disables)
     const double *ksr_max_dev;  // when set, the clamp is read from device memory
+    // FP32C only: particles whose final h lies within amb_tol of rs (where
+    // the search-radius decision h > rs of hdr_density.hpp:299 could come out
+    // differently in FP64) are queued here for an FP64 recomputation
+    int *amb_count;         // null disables the queue
+    int *amb_i;             // queued particle index
+    int *amb_w;             // its walk
+    int amb_cap;
+    float amb_tol;
 };
 
 template <bool F64, int WARPS>
@@ -198,6 +206,13 @@ density_kernel(const DensityArgs a) {
             np = c;
             itr = hn > rs_i;
             h = hn;
+        }
+        if (!F64 && a.amb_count && r.act && sub == 0 && fabs(h - rs_i) <= (double)a.amb_tol * rs_i) {
+            const int k = atomicAdd(a.amb_count, 1);
+            if (k < a.amb_cap) {
+                a.amb_i[k] = ii;
+                a.amb_w[k] = r.walk;
+            }
         }
 
         // gradient pass with the final h, hdr_density.hpp:304-349
@@ -624,6 +639,15 @@ gravity_kernel(const GravityArgs a) {
             a.o_eta[ii] = set;
         }
     }
+}
+
+// One FP64 work item per queued particle (single-i items use all 32 lanes).
+__global__ inline void make_fixup_items(const int *amb_count, const int *amb_w, int cap, WorkItem *items,
+                                        int *n_items) {
+    const int n = min(*amb_count, cap);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        items[k] = make_int4(amb_w[k], k, 1, 0);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_items = n;
 }
 
 // ---------------------------------------------------------------- records

@@ -32,7 +32,8 @@ constexpr int RED_THREADS = 256;
 constexpr int MAX_RED = 8;
 
 // int scalars
-enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_NI };
+enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
+       S_NI };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -278,6 +279,7 @@ __global__ void compact_active(int n, const int *scal, const int *flag, const in
 }
 
 __global__ void set_int(int *p, int v) { *p = v; }
+__global__ void accumulate_int(const int *src, int *dst) { *dst += *src; }
 __global__ void copy_int(const int *src, int *dst) { *dst = *src; }
 
 // list totals: offset[n-1] + count[n-1] (counts beyond the walk count are 0)
@@ -615,6 +617,10 @@ struct sph_system {
     DevBuf<float4> f_phi, f_plo, f_vhi, f_vlo, f_g1, f_g2, f_g3, f_shi, f_slo;
     // re-walk index list (particles still iterating) and its per-walk segments
     DevBuf<int> uflag, uscan, ulist, a_sfirst, a_scount;
+    // FP64 re-check queue of decision-ambiguous density results
+    DevBuf<int> amb_i, amb_w;
+    DevBuf<WorkItem> fitems;
+    int amb_cap = 0;
     // groups and walks
     DevBuf<int> gflag, groot, gscan, group_node, group_first, group_count;
     DevBuf<int> aflag, ascan, a_node, a_first, a_count;
@@ -642,6 +648,9 @@ struct sph_system {
     cudaGraphExec_t step_exec = nullptr;
     bool graph_valid = false;
     int graph_precision = -1;
+    cudaGraphExec_t force_exec = nullptr;
+    bool force_graph_valid = false;
+    int force_graph_precision = -1;
     // phase events
     cudaEvent_t ev[16] = {nullptr};
     long long steps = 0;
@@ -693,6 +702,8 @@ int alloc_all(sph_system *s) {
     for (auto *b : f1) e |= b->ensure(n);
     e |= s->f_shi.ensure(nn) | s->f_slo.ensure(nn);
     e |= s->uflag.ensure(n) | s->uscan.ensure(n) | s->ulist.ensure(n) | s->a_sfirst.ensure(n) | s->a_scount.ensure(n);
+    s->amb_cap = std::max<int>(1024, s->n / 16);
+    e |= s->amb_i.ensure(s->amb_cap) | s->amb_w.ensure(s->amb_cap) | s->fitems.ensure(s->amb_cap);
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff};
     for (auto *b : i1) e |= b->ensure(n);
@@ -857,6 +868,7 @@ int density_phase(sph_system *s, bool eager) {
                                                                 s->f_plo.p, s->f_vhi.p, s->f_vlo.p);
     init_rs<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->rs.p);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_ITERS, 1);
+    set_int<<<1, 1, 0, st>>>(s->scal.p + S_AMBTOT, 0);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_UNCONV, 0);
     DensOut tmp{s->t_dens.p, s->t_divv.p, s->t_rotv.p, s->t_grdh.p, s->t_ksr.p, s->t_np.p, s->t_itr.p};
     DensOut out{s->dens.p, s->divv.p, s->rotv.p, s->grdh.p, s->ksr[0].p, s->np.p, nullptr};
@@ -896,9 +908,28 @@ int density_phase(sph_system *s, bool eager) {
         a.eta_ksrh = ctx->prm.eta * KSRH;
         a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
         a.ksr_max_dev = (s->prm.ksr_max_mode == 1) ? s->dscal.p + D_KSRMAX : nullptr;
+        a.amb_count = f32 ? s->scal.p + S_AMB : nullptr;
+        a.amb_i = s->amb_i.p;
+        a.amb_w = s->amb_w.p;
+        a.amb_cap = s->amb_cap;
+        a.amb_tol = sphrt::AMB_TOL;
+        if (f32) CUDA_TRY(cudaMemsetAsync(s->scal.p + S_AMB, 0, sizeof(int), st));
         if (it == 0) cudaEventRecord(s->ev[EV_DENSK_B], st);
         sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
         if (it == 0) cudaEventRecord(s->ev[EV_DENSK_E], st);
+        if (f32) {
+            // FP64 recomputation of decision-ambiguous particles (same lists)
+            sphk::make_fixup_items<<<8, 256, 0, st>>>(s->scal.p + S_AMB, s->amb_w.p, s->amb_cap, s->fitems.p,
+                                                      s->scal.p + S_NFIX);
+            accumulate_int<<<1, 1, 0, st>>>(s->scal.p + S_AMB, s->scal.p + S_AMBTOT);
+            CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+            sphk::DensityArgs f = a;
+            f.items = s->fitems.p;
+            f.n_items_dev = s->scal.p + S_NFIX;
+            f.i_list = s->amb_i.p;
+            f.amb_count = nullptr;
+            sphrt::launch_density(f, SPH_PREC_FP64, ctx->grid[0][1], st);
+        }
         commit_density<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, tmp, out, s->scal.p);
         iteration_end<<<1, 1, 0, st>>>(s->scal.p, max_it, it);
         if (eager) {
@@ -1114,6 +1145,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
     cudaSetDevice(s->ctx->prm.device);
     cudaStreamSynchronize(s->st());
     if (s->step_exec) cudaGraphExecDestroy(s->step_exec);
+    if (s->force_exec) cudaGraphExecDestroy(s->force_exec);
     for (int k = 0; k < EV_N; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     for (int k = 0; k < 2; ++k) {
@@ -1136,6 +1168,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
                             &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
     for (auto *b : f1) b->release();
     s->uflag.release(); s->uscan.release(); s->ulist.release(); s->a_sfirst.release(); s->a_scount.release();
+    s->amb_i.release(); s->amb_w.release(); s->fitems.release();
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff,
                          &s->scal};
@@ -1220,13 +1253,58 @@ extern "C" int sph_system_upload(sph_system *s, double t0, const int64_t *id, co
     return SPH_OK;
 }
 
+namespace {
+int capture(sph_system *s, bool step, cudaGraphExec_t *exec) {
+    cudaStream_t st = s->st();
+    if (*exec) {
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = step ? step_body(s, false) : force_body(s, false);
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaStreamEndCapture");
+    const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return sphrt::cuda_error(s->ctx, ei, "cudaGraphInstantiate");
+    return SPH_OK;
+}
+}  // namespace
+
 extern "C" int sph_system_compute_forces(sph_system *s) {
     if (!s) return SPH_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->ctx->prm.device);
-    int r = force_body(s, true);
-    if (!r) r = check_errors(s);
+    int r = SPH_OK;
+    if (s->force_graph_precision != s->ctx->prm.precision) s->force_graph_valid = false;
+    if (!s->prm.use_graph || !s->force_graph_valid) {
+        // eager evaluation (sizes the lists); the graph is captured afterwards
+        r = force_body(s, true);
+        if (!r) r = check_errors(s);
+        if (!r && s->prm.use_graph) {
+            r = capture(s, false, &s->force_exec);
+            if (!r) {
+                s->force_graph_valid = true;
+                s->force_graph_precision = s->ctx->prm.precision;
+            }
+        }
+    } else {
+        const cudaError_t e = cudaGraphLaunch(s->force_exec, s->st());
+        if (e != cudaSuccess) return sphrt::cuda_error(s->ctx, e, "cudaGraphLaunch");
+        r = check_errors(s);
+    }
     s->last_status = r;
     return r;
+}
+
+extern "C" int sph_system_set_graph(sph_system *s, int32_t use_graph) {
+    if (!s) return SPH_ERR_INVALID_ARGUMENT;
+    s->prm.use_graph = use_graph ? 1 : 0;
+    return SPH_OK;
 }
 
 extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
@@ -1241,19 +1319,8 @@ extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
             r = step_body(s, true);
             if (!r) r = check_errors(s);
             if (!r && s->prm.use_graph) {
-                if (s->step_exec) {
-                    cudaGraphExecDestroy(s->step_exec);
-                    s->step_exec = nullptr;
-                }
-                cudaGraph_t g = nullptr;
-                CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                int rc = step_body(s, false);
-                cudaError_t ec = cudaStreamEndCapture(st, &g);
-                if (rc) return rc;
-                if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaStreamEndCapture");
-                ec = cudaGraphInstantiate(&s->step_exec, g, 0);
-                cudaGraphDestroy(g);
-                if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaGraphInstantiate");
+                r = capture(s, true, &s->step_exec);
+                if (r) return r;
                 s->graph_valid = true;
                 s->graph_precision = s->ctx->prm.precision;
             }
@@ -1361,6 +1428,7 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->list_hydro = lc[L_LIST_H];
     o->list_gravity = lc[L_LIST_G];
     o->steps = s->steps;
+    o->density_rechecked = sc[S_AMBTOT];
     o->last_status = s->last_status;
     return SPH_OK;
 }

@@ -41,7 +41,8 @@ class SystemStats(ctypes.Structure):
     _fields_ = [("time", _D), ("dt", _D), ("ksr_max", _D), ("e_kin", _D), ("e_thm", _D), ("e_pot", _D),
                 ("e_tot", _D), ("n_groups", _I64), ("density_iterations", _I64), ("pairs_density", _I64),
                 ("pairs_density_first", _I64), ("pairs_hydro", _I64), ("pairs_gravity", _I64), ("list_density", _I64),
-                ("list_hydro", _I64), ("list_gravity", _I64), ("steps", _I64), ("last_status", _I32)]
+                ("list_hydro", _I64), ("list_gravity", _I64), ("steps", _I64), ("density_rechecked", _I64),
+                ("last_status", _I32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -62,6 +63,7 @@ def _declare(lib):
                                                 _P, _P, _P, _P]),
         "sph_system_get_nodes": (ctypes.c_int, [_P, _P, _P]),
         "sph_system_phase_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), _I32]),
+        "sph_system_set_graph": (ctypes.c_int, [_P, _I32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -125,6 +127,9 @@ class ParticleSystem:
 
     def compute_forces(self):
         check(self.lib.sph_system_compute_forces(self.handle), self.ctx.handle, "compute_forces")
+
+    def set_graph(self, on):
+        check(self.lib.sph_system_set_graph(self.handle, 1 if on else 0), self.ctx.handle, "set_graph")
 
     def step(self, n_steps=1):
         check(self.lib.sph_system_step(self.handle, n_steps), self.ctx.handle, "step")

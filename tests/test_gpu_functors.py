@@ -6,11 +6,12 @@ Tolerances (relative, per particle; vector fields by norm):
   FP64 mode   : 1e-11 on every real field (same arithmetic, different order).
   FP32C mode  : 1e-5 on rho, h, Omega (grdh), a (hydro, softening correction,
                 gravity), du/dt, pot, eta, v_sig; 1e-4 on div v, |rot v| and the
-                conduction signal diffu, which are differences of nearly equal
-                neighbour sums.  Per-particle errors are floored at 1e-3 of the
-                field's largest magnitude, so a particle whose vector nearly
-                cancels (symmetric neighbourhood) is judged against the field's
-                scale.  np and itr must match except where a neighbour sits at
+                conduction signal diffu and the softening correction accg,
+                which are sums of strongly cancelling neighbour terms.
+                Per-particle errors are floored at 1e-3 of the field's largest
+                magnitude (1e-2 for the cancelling sums), so a particle whose
+                vector nearly cancels (symmetric neighbourhood) is judged
+                against the field's scale.  np and itr must match except where a neighbour sits at
                 q = 1 within FP32 rounding (at most 1% of particles).
 """
 import numpy as np
@@ -26,10 +27,11 @@ TOL64 = 1e-11
 TOL32 = 1e-5
 TOL32_DERIV = 1e-4
 FLOOR = 1e-3
+FLOOR_DERIV = 1e-2
 
 
-def err(a, b):
-    return rel_err(a, b, floor_frac=FLOOR).max()
+def err(a, b, floor=FLOOR):
+    return rel_err(a, b, floor_frac=floor).max()
 
 
 @pytest.fixture(scope="module", params=["fp32c", "fp64"])
@@ -50,7 +52,7 @@ def check_density(ctx, out, ref):
     for f in ("dens", "ksr", "grdh"):
         assert err(out[f], ref[f]) < _tol(ctx), (f, err(out[f], ref[f]))
     for f in ("divv", "rotv"):
-        assert err(out[f], ref[f]) < _tol(ctx, True), (f, err(out[f], ref[f]))
+        assert err(out[f], ref[f], FLOOR_DERIV) < _tol(ctx, True), (f, err(out[f], ref[f], FLOOR_DERIV))
     if ctx.mode == "fp64":
         assert np.array_equal(out["np"], ref["np"])
         assert np.array_equal(out["itr"], ref["itr"])
@@ -64,7 +66,7 @@ def check_hydro(ctx, out, ref):
     for f in ("acch", "udot", "vsmx"):
         assert err(out[f], ref[f]) < _tol(ctx), (f, err(out[f], ref[f]))
     for f in ("accg", "diffu"):
-        assert err(out[f], ref[f]) < _tol(ctx, True), (f, err(out[f], ref[f]))
+        assert err(out[f], ref[f], FLOOR_DERIV) < _tol(ctx, True), (f, err(out[f], ref[f], FLOOR_DERIV))
 
 
 def check_gravity(ctx, out, ref):

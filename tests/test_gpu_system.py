@@ -13,10 +13,12 @@ from research_codes_gb300.system import ParticleSystem, state_from_ic
 pytestmark = pytest.mark.gpu
 
 FLOOR = 1e-3
+FLOOR_DERIV = 1e-2   # div v, |rot v|, diffu, accg: sums of cancelling terms
+DERIV = ("divv", "rotv", "diffu", "accg")
 
 
-def err(a, b):
-    return rel_err(a, b, floor_frac=FLOOR).max()
+def err(a, b, floor=FLOOR):
+    return rel_err(a, b, floor_frac=floor).max()
 
 
 def _star(n=4000, seed=3, eta=1.18, spin=True):
@@ -79,8 +81,8 @@ def test_density_matches_oracle_on_engine_lists(evaluated):
                               ksr_max=0.0)
     assert np.abs(f["np"] - ref["np"]).max() <= (0 if prec == "fp64" else 1)
     for k in ("dens", "ksr", "grdh", "divv", "rotv"):
-        e = err(f[k], ref[k])
-        assert e < _tol(prec, k in ("divv", "rotv")), (k, e)
+        e = err(f[k], ref[k], FLOOR_DERIV if k in DERIV else FLOOR)
+        assert e < _tol(prec, k in DERIV), (k, e)
 
 
 def test_gravity_matches_oracle_on_engine_lists(evaluated):
@@ -126,9 +128,10 @@ def test_hydro_matches_oracle_on_engine_lists(evaluated):
         refs.append(orc.hydro(walks.hydro_epi(gi, f), walks.hydro_epj(gj, f)))
     gi = np.concatenate(sel)
     ref = np.concatenate(refs)
-    worst = {"acch": err(f["acch"][gi], ref["acch"]), "accg": err(f["accg1"][gi], G * ref["accg"]),
+    worst = {"acch": err(f["acch"][gi], ref["acch"]),
+             "accg": err(f["accg1"][gi], G * ref["accg"], FLOOR_DERIV),
              "udot": err(f["udot"][gi], ref["udot"]), "vsmx": err(f["vsmx"][gi], ref["vsmx"]),
-             "diffu": err(f["diffu"][gi], ref["diffu"])}
+             "diffu": err(f["diffu"][gi], ref["diffu"], FLOOR_DERIV)}
     for k, v in worst.items():
         assert v < _tol(prec, k in ("diffu", "accg")), (k, v)
 
@@ -229,3 +232,34 @@ def test_fp32c_step_tracks_fp64_step():
     assert err(res["fp32c"]["dens"], res["fp64"]["dens"]) < 1e-5
     assert err(res["fp32c"]["acc"], res["fp64"]["acc"]) < 1e-4
     assert err(res["fp32c"]["uene"], res["fp64"]["uene"]) < 1e-5
+
+
+def test_fp32c_forces_match_fp64_on_same_state():
+    """North-star parity: rho, h, a, du/dt and pot of the FP32C engine against
+    the plain FP64 engine on identical particle state, every particle at
+    1e-5 relative (floor 1e-3 of the field maximum).  FP32C density results
+    whose search-radius decision lies within FP32 rounding of the threshold
+    are recomputed in FP64, so both precisions take the same walks."""
+    s = _two_stars(n=12000, seed=21)
+    res = {}
+    with functors.Context(precision="fp64", eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, len(s["mass"]), n_group=128, use_graph=0)
+        sys.upload(s)
+        sys.compute_forces()
+        sys.compute_forces()
+        state = {k: sys.download(k) for k in ("ksr",)}
+        sys.close()
+    s2 = dict(s)
+    s2["ksr"] = state["ksr"]
+    for prec in ("fp64", "fp32c"):
+        with functors.Context(precision=prec, eta=1.18) as ctx:
+            sys = ParticleSystem(ctx, len(s["mass"]), n_group=128, use_graph=0)
+            sys.upload(s2)
+            sys.compute_forces()
+            res[prec] = {k: sys.download(k) for k in ("dens", "ksr", "acc", "udot", "pot", "grdh")}
+            res[prec]["stats"] = sys.stats()
+            sys.close()
+    for k in ("dens", "ksr", "acc", "udot", "pot", "grdh"):
+        e = err(res["fp32c"][k], res["fp64"][k])
+        assert e < 1e-5, (k, e)
+    assert res["fp32c"]["stats"]["density_iterations"] == res["fp64"]["stats"]["density_iterations"]
