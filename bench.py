@@ -261,14 +261,23 @@ def run_ours(args):
     line["gpu_launches"] = args.steps * LAUNCHES_PER_STEP(args)
 
     if rank == 0 and not args.no_fp64:
-        # ---- FP64 comparator on the same state and FP32C/FP64 parity
-        f32 = {k: ps.download(k) for k in ("dens", "acc", "udot", "ksr", "pot")}
-        ctx.set_precision("fp64")
+        # ---- FP64 comparator: parity of one force evaluation of identical
+        # state in both precisions, then the FP64 step time
+        fields = ("dens", "ksr", "acch", "accg1", "accg2", "udot", "pot")
+        host = {k: ps.download(k) for k in ("pos", "vel", "mass", "uene", "ksr", "alph", "alphu", "id", "istar")}
+        host["id"] = host["id"].astype(np.int64)
+        host["istar"] = host["istar"].astype(np.int32)
         ps.set_graph(False)
-        ps.compute_forces()   # same state, FP64 pair arithmetic
-        ps.set_graph(True)
-        f64 = {k: ps.download(k) for k in ("dens", "acc", "udot", "ksr", "pot")}
+        res = {}
+        for prec in ("fp32c", "fp64"):
+            ctx.set_precision(prec)
+            ps.upload(host)
+            ps.compute_forces()
+            res[prec] = {k: ps.download(k) for k in fields}
+            res[prec]["stats"] = ps.stats()
         ph64 = ps.phase_times()
+        ps.set_graph(True)
+        f32, f64 = res["fp32c"], res["fp64"]
         ps.step(1)            # captures the FP64 graph
         torch.cuda.synchronize()
         k64 = max(1, min(args.steps, 3))
@@ -290,7 +299,18 @@ def run_ours(args):
 
         line["fp64"] = {"ms_per_step": ms64, "speedup_fp32c_over_fp64": ms64 / ms_step,
                         "phases_ms": {k: round(v, 3) for k, v in ph64.items()}}
-        line["parity_fp32c_vs_fp64"] = {k: rel(f32[k], f64[k]) for k in f32}
+        par = {k: rel(f32[k], f64[k], 1e-2 if k == "accg1" else 1e-3) for k in fields}
+        for k in fields:
+            a_, b_ = np.asarray(f32[k]), np.asarray(f64[k])
+            d_ = np.linalg.norm(a_ - b_, axis=1) if a_.ndim > 1 else np.abs(a_ - b_)
+            s_ = np.linalg.norm(b_, axis=1) if b_.ndim > 1 else np.abs(b_)
+            floor = (1e-2 if k == "accg1" else 1e-3) * s_.max()
+            par[k]["n_above_1e-5"] = int((d_ / np.maximum(s_, floor) > 1e-5).sum())
+        par["density_rechecked_fp64"] = int(f32["stats"]["density_rechecked"])
+        par["same_density_walks"] = f32["stats"]["density_iterations"] == f64["stats"]["density_iterations"]
+        par["note"] = ("per-particle |d|/max(|ref|, floor), floor 1e-3 of the field max (1e-2 for the "
+                       "softening correction accg1); the total acceleration is compared by parts")
+        line["parity_fp32c_vs_fp64"] = par
         log(f"[bench] fp64 {ms64:.1f} ms/step (x{ms64 / ms_step:.1f})")
 
     if rank == 0 and not args.no_e2e:

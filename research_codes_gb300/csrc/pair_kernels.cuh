@@ -155,6 +155,7 @@ density_kernel(const DensityArgs a) {
         // three fixed-point passes, hdr_density.hpp:264-302
         for (int pass = 0; pass < 3; ++pass) {
             const R hinv = (R)1 / (R)h;
+            const R hinv2 = hinv * hinv;
             Acc<F64> acc;
             int cnt = 0;
             for (int t = 0; t < nj; t += 32) {
@@ -174,15 +175,28 @@ density_kernel(const DensityArgs a) {
                 __syncwarp();
                 const int n = min(32, nj - t);
                 R part = 0;
-                for (int k = sub; k < n; k += tpi) {
+                // rho pair term m_j W0(q)/c0; neighbour count only in the
+                // last pass (the only np the reference stores, :297)
+                auto pair = [&](int k, bool count) {
                     const R4 pj = s_p[wid][k];
                     const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
                     const R r2 = dx * dx + dy * dy + dz * dz;
-                    const R q = r2 * rsqrt_r(r2 > (R)0 ? r2 : (R)1e-30) * hinv;
+                    const R q = sqrt_q(r2, hinv2);
                     const R u = max0((R)1 - q);
                     const R u2 = u * u;
                     part += pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
-                    cnt += (q < (R)1) ? 1 : 0;
+                    if (count) cnt += (q < (R)1) ? 1 : 0;
+                };
+                if (tpi == 1 && n == 32) {
+                    if (pass == 2) {
+#pragma unroll 8
+                        for (int k = 0; k < 32; ++k) pair(k, true);
+                    } else {
+#pragma unroll 8
+                        for (int k = 0; k < 32; ++k) pair(k, false);
+                    }
+                } else {
+                    for (int k = sub; k < n; k += tpi) pair(k, pass == 2);
                 }
                 acc.add(part);
                 __syncwarp();
@@ -242,7 +256,7 @@ density_kernel(const DensityArgs a) {
                 __syncwarp();
                 const int n = min(32, nj - t);
                 R pg = 0, pd = 0, prx = 0, pry = 0, prz = 0;
-                for (int k = sub; k < n; k += tpi) {
+                auto pair = [&](int k) {
                     const R4 pj = s_p[wid][k];
                     const R4 vj = s_v[wid][k];
                     const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
@@ -268,6 +282,12 @@ density_kernel(const DensityArgs a) {
                     prx += (uy * dz - uz * dy) * dw;
                     pry += (uz * dx - ux * dz) * dw;
                     prz += (ux * dy - uy * dx) * dw;
+                };
+                if (tpi == 1 && n == 32) {
+#pragma unroll 4
+                    for (int k = 0; k < 32; ++k) pair(k);
+                } else {
+                    for (int k = sub; k < n; k += tpi) pair(k);
                 }
                 g_acc.add(pg);
                 d_acc.add(pd);
@@ -360,10 +380,10 @@ hydro_kernel(const HydroArgs a) {
     typedef typename Real<F64>::T4 R4;
     __shared__ R4 s_a[WARPS][32];   // dx, dy, dz, mass
     __shared__ R4 s_b[WARPS][32];   // vx, vy, vz (hi), hinv
-    __shared__ R4 s_c[WARPS][32];   // dP (vs centre), presc, bswt, dens
-    __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, du (vs centre)
+    __shared__ R4 s_c[WARPS][32];   // P (hi), presc, bswt, dens
+    __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, u (hi)
     __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, vx lo, vy lo
-    __shared__ float s_f[WARPS][32];  // vz lo
+    __shared__ float4 s_f[WARPS][32]; // vz lo, P lo, u lo, -
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -378,8 +398,8 @@ hydro_kernel(const HydroArgs a) {
         const int tpi = r.tpi, sub = r.sub, ii = r.ii, nj = r.nj, jb = r.jb;
 
         R xi, yi, zi, vxi, vyi, vzi, hi_i, hi4_i, pp_i, pc_i, bs_i, dn_i, cs_i, al_i, au_i, eg_i, et_i;
-        float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
-        float4 cph = make_float4(0, 0, 0, 0), cpl = cph, cg1 = cph, cg3 = cph;
+        float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f, plo_i = 0.0f, elo_i = 0.0f;
+        float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
         if (F64) {
             const dbl4 p = a.i_pm[ii], v = a.i_vel[ii], h1 = a.i_h1[ii], h2 = a.i_h2[ii];
             const double2 h3 = a.i_h3[ii];
@@ -388,7 +408,6 @@ hydro_kernel(const HydroArgs a) {
             dn_i = h2.x; cs_i = h2.y; al_i = h2.z; au_i = h2.w; eg_i = h3.x; et_i = h3.y;
         } else {
             cph = a.fi.phi[r.ic]; cpl = a.fi.plo[r.ic];
-            cg1 = a.fi_g1[r.ic]; cg3 = a.fi_g3[r.ic];
             const float4 ph = a.fi.phi[ii], pl = a.fi.plo[ii], vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
             const float4 g1 = a.fi_g1[ii], g2 = a.fi_g2[ii], g3 = a.fi_g3[ii];
             xi = df_diff(ph.x, pl.x, cph.x, cpl.x);
@@ -397,9 +416,9 @@ hydro_kernel(const HydroArgs a) {
             vxi = vh.x; vyi = vh.y; vzi = vh.z;       // absolute hi/lo, differenced per pair
             lxi = vl.x; lyi = vl.y; lzi = vl.z;
             hi_i = vh.w; hi4_i = vl.w;
-            pp_i = df_diff(g1.x, g1.y, cg1.x, cg1.y); pc_i = g1.z; bs_i = g1.w;
-            dn_i = g2.x; cs_i = g2.y; al_i = g2.z; au_i = g2.w;
-            eg_i = df_diff(g3.x, g3.y, cg3.x, cg3.y); et_i = g3.z;
+            pp_i = g1.x; plo_i = g1.y; pc_i = g1.z; bs_i = g1.w;   // P and u as hi/lo,
+            dn_i = g2.x; cs_i = g2.y; al_i = g2.z; au_i = g2.w;    // differenced per pair
+            eg_i = g3.x; elo_i = g3.y; et_i = g3.z;
         }
         const long long idi = a.i_id[ii];
 
@@ -424,19 +443,17 @@ hydro_kernel(const HydroArgs a) {
                         (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
                         (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
                     s_b[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vh.w);
-                    s_c[wid][lane] = Real<F64>::make4((R)df_diff(g1.x, g1.y, cg1.x, cg1.y), (R)g1.z, (R)g1.w,
-                                                      (R)g2.x);
-                    s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w,
-                                                      (R)df_diff(g3.x, g3.y, cg3.x, cg3.y));
+                    s_c[wid][lane] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
+                    s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)g3.x);
                     s_e[wid][lane] = Real<F64>::make4((R)g3.z, (R)vl.w, (R)vl.x, (R)vl.y);
-                    s_f[wid][lane] = vl.z;
+                    s_f[wid][lane] = make_float4(vl.z, g1.y, g3.y, 0.0f);
                 }
                 s_id[wid][lane] = a.j_id[j];
             }
             __syncwarp();
             const int n = min(32, nj - t);
             R pax = 0, pay = 0, paz = 0, pud = 0, pdf = 0, pgx = 0, pgy = 0, pgz = 0;
-            for (int k = sub; k < n; k += tpi) {
+            auto pair = [&](int k) {
                 const R4 A = s_a[wid][k];
                 const R4 B = s_b[wid][k];
                 const R4 C = s_c[wid][k];
@@ -444,10 +461,14 @@ hydro_kernel(const HydroArgs a) {
                 const R4 E = s_e[wid][k];
                 const R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
                 R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
+                R dp = pp_i - C.x, du = eg_i - D.w;
                 if (!F64) {
+                    const float4 F = s_f[wid][k];
                     ux += (R)(lxi - (float)E.z);
                     uy += (R)(lyi - (float)E.w);
-                    uz += (R)(lzi - s_f[wid][k]);
+                    uz += (R)(lzi - F.x);
+                    dp += (R)(plo_i - F.y);
+                    du += (R)(elo_i - F.z);
                 }
                 const R r2 = dx * dx + dy * dy + dz * dz;
                 const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
@@ -474,9 +495,8 @@ hydro_kernel(const HydroArgs a) {
                 pay -= ta * dy;
                 paz -= ta * dz;
                 // energy equation with conduction, :384-393
-                const R vsu2 = fabs(pp_i - C.x) * rhi * (R)2;
+                const R vsu2 = fabs(dp) * rhi * (R)2;
                 const R vsu = vsu2 > (R)0 ? vsu2 * rsqrt_r(vsu2) : (R)0;
-                const R du = eg_i - D.w;
                 pud += ka * (pc_i * w - rhi * ((R)0.25 * av * wneg - (au_i + D.z) * vsu * du));
                 pdf += rhi * du * ka * ri;
                 // softening correction, :395-398
@@ -484,6 +504,12 @@ hydro_kernel(const HydroArgs a) {
                 pgx += dg * dx;
                 pgy += dg * dy;
                 pgz += dg * dz;
+            };
+            if (tpi == 1 && n == 32) {
+#pragma unroll 2
+                for (int k = 0; k < 32; ++k) pair(k);
+            } else {
+                for (int k = sub; k < n; k += tpi) pair(k);
             }
             ax.add(pax);
             ay.add(pay);
@@ -606,7 +632,7 @@ gravity_kernel(const GravityArgs a) {
             __syncwarp();
             const int n = min(32, nj - t);
             R pax = 0, pay = 0, paz = 0, ppt = 0, pet = 0;
-            for (int k = sub; k < n; k += tpi) {
+            auto pair = [&](int k) {
                 const R4 pj = s_p[wid][k];
                 const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
                 const R r2 = dx * dx + dy * dy + dz * dz;
@@ -620,6 +646,12 @@ gravity_kernel(const GravityArgs a) {
                 pay -= dy * g;
                 paz -= dz * g;
                 pet += pj.w * rei3;
+            };
+            if (tpi == 1 && n == 32) {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) pair(k);
+            } else {
+                for (int k = sub; k < n; k += tpi) pair(k);
             }
             ax.add(pax);
             ay.add(pay);

@@ -63,6 +63,15 @@ __device__ __forceinline__ float rcp_r(float x) {
 }
 __device__ __forceinline__ double rcp_r(double x) { return 1.0 / x; }
 
+// q = sqrt(r2 * hinv2): FP32 by sqrt.approx (relative error ~2^-23,
+// exact 0 at r2 = 0), FP64 by the library sqrt.
+__device__ __forceinline__ float sqrt_q(float r2, float hinv2) {
+    float q;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(q) : "f"(r2 * hinv2));
+    return q;
+}
+__device__ __forceinline__ double sqrt_q(double r2, double hinv2) { return sqrt(r2 * hinv2); }
+
 __device__ __forceinline__ float max0(float x) { return fmaxf(x, 0.0f); }
 __device__ __forceinline__ double max0(double x) { return fmax(x, 0.0); }
 

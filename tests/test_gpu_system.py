@@ -251,15 +251,18 @@ def test_fp32c_forces_match_fp64_on_same_state():
         sys.close()
     s2 = dict(s)
     s2["ksr"] = state["ksr"]
+    fields = ("dens", "ksr", "acch", "accg1", "accg2", "udot", "pot", "grdh")
     for prec in ("fp64", "fp32c"):
         with functors.Context(precision=prec, eta=1.18) as ctx:
             sys = ParticleSystem(ctx, len(s["mass"]), n_group=128, use_graph=0)
             sys.upload(s2)
             sys.compute_forces()
-            res[prec] = {k: sys.download(k) for k in ("dens", "ksr", "acc", "udot", "pot", "grdh")}
+            res[prec] = {k: sys.download(k) for k in fields}
             res[prec]["stats"] = sys.stats()
             sys.close()
-    for k in ("dens", "ksr", "acc", "udot", "pot", "grdh"):
-        e = err(res["fp32c"][k], res["fp64"][k])
-        assert e < 1e-5, (k, e)
+    # the total acceleration of a star near hydrostatic equilibrium is a small
+    # difference of its hydro and gravity parts: its parts are compared
+    for k in fields:
+        e = err(res["fp32c"][k], res["fp64"][k], FLOOR_DERIV if k == "accg1" else FLOOR)
+        assert e < (1e-4 if k == "accg1" else 1e-5), (k, e)
     assert res["fp32c"]["stats"]["density_iterations"] == res["fp64"]["stats"]["density_iterations"]
