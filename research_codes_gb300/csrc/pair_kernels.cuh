@@ -275,7 +275,7 @@ density_kernel(const DensityArgs a) {
                     const R u3 = u2 * u;
                     const R p14 = (R)1 + (R)4 * q;
                     const R w0 = u2 * u2 * p14;            // W0 / c0
-                    const R w1 = u2 * u2 - u3 * p14;       // W1 / c1
+                    const R w1 = w1_term(q, u, u2, u3, p14);   // W1 / c1
                     pg += pj.w * ((R)(3.0 * CEFF0) * w0 + (R)CEFF1 * q * w1);
                     const R dw = pj.w * w1 * ri;
                     pd += (ux * dx + uy * dy + uz * dz) * dw;
@@ -477,8 +477,8 @@ hydro_kernel(const HydroArgs a) {
                 const R qi = rr * hi_i, qj = rr * B.w;
                 const R ui = max0((R)1 - qi), uj = max0((R)1 - qj);
                 const R ui2 = ui * ui, uj2 = uj * uj;
-                const R w1i = ui2 * (ui2 - ui * ((R)1 + (R)4 * qi));
-                const R w1j = uj2 * (uj2 - uj * ((R)1 + (R)4 * qj));
+                const R w1i = w1_term(qi, ui, ui2, ui2 * ui, (R)1 + (R)4 * qi);
+                const R w1j = w1_term(qj, uj, uj2, uj2 * uj, (R)1 + (R)4 * qj);
                 const R dw_i = (R)CEFF1 * hi4_i * w1i;
                 const R dw_j = (R)CEFF1 * E.y * w1j;
                 const R ka = (dw_i + dw_j) * A.w;

@@ -72,6 +72,19 @@ __device__ __forceinline__ float sqrt_q(float r2, float hinv2) {
 }
 __device__ __forceinline__ double sqrt_q(double r2, double hinv2) { return sqrt(r2 * hinv2); }
 
+// Radial kernel-gradient factor W1(q)/c1 with u = (1-q)_+ (hdr_kernel.hpp:251-257).
+// The reference's form u^4 - u^3 (1+4q) subtracts two nearly equal terms for
+// small q; FP32 evaluates the algebraically identical -5 q u^3 instead (no
+// cancellation), FP64 keeps the reference's form.
+__device__ __forceinline__ float w1_term(float q, float u, float u2, float u3, float p14) {
+    (void)u; (void)u2; (void)p14;
+    return -5.0f * q * u3;
+}
+__device__ __forceinline__ double w1_term(double q, double u, double u2, double u3, double p14) {
+    (void)q; (void)u;
+    return u2 * u2 - u3 * p14;
+}
+
 __device__ __forceinline__ float max0(float x) { return fmaxf(x, 0.0f); }
 __device__ __forceinline__ double max0(double x) { return fmax(x, 0.0); }
 

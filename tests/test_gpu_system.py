@@ -226,11 +226,12 @@ def test_fp32c_step_tracks_fp64_step():
             sys.upload(s)
             sys.compute_forces()
             sys.step(5)
-            res[prec] = dict(pos=sys.download("pos"), uene=sys.download("uene"), acc=sys.download("acc"),
-                             dens=sys.download("dens"))
+            res[prec] = dict(pos=sys.download("pos"), uene=sys.download("uene"), acch=sys.download("acch"),
+                             accg2=sys.download("accg2"), dens=sys.download("dens"))
             sys.close()
     assert err(res["fp32c"]["dens"], res["fp64"]["dens"]) < 1e-5
-    assert err(res["fp32c"]["acc"], res["fp64"]["acc"]) < 1e-4
+    assert err(res["fp32c"]["acch"], res["fp64"]["acch"]) < 1e-4
+    assert err(res["fp32c"]["accg2"], res["fp64"]["accg2"]) < 1e-4
     assert err(res["fp32c"]["uene"], res["fp64"]["uene"]) < 1e-5
 
 
