@@ -111,6 +111,7 @@ density_kernel(const DensityArgs a) {
     __shared__ R4 s_p[WARPS][32];
     __shared__ R4 s_v[WARPS][32];
     __shared__ float2 s_vl[WARPS][32];
+    __shared__ float4 s_pl[WARPS][32];
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -128,6 +129,7 @@ density_kernel(const DensityArgs a) {
         // i-particle relative to the centre particle c
         R xi, yi, zi, vxi, vyi, vzi;
         float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
+        float xhi = 0.0f, yhi = 0.0f, zhi = 0.0f, xlo = 0.0f, ylo = 0.0f, zlo = 0.0f;
         float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
         if (F64) {
             const dbl4 p = a.i_pm[ii], v = a.i_vel[ii];
@@ -139,6 +141,8 @@ density_kernel(const DensityArgs a) {
             xi = (R)df_diff(ph.x, pl.x, cph.x, cpl.x);
             yi = (R)df_diff(ph.y, pl.y, cph.y, cpl.y);
             zi = (R)df_diff(ph.z, pl.z, cph.z, cpl.z);
+            xhi = ph.x - cph.x; yhi = ph.y - cph.y; zhi = ph.z - cph.z;
+            xlo = pl.x - cpl.x; ylo = pl.y - cpl.y; zlo = pl.z - cpl.z;
             // velocities stay absolute hi/lo pairs and are differenced per
             // pair: an item may straddle two colliding streams
             vxi = vh.x; vyi = vh.y; vzi = vh.z;
@@ -245,9 +249,11 @@ density_kernel(const DensityArgs a) {
                     } else {
                         const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
                         const float4 vh = a.fj.vhi[j], vl = a.fj.vlo[j];
-                        s_p[wid][lane] = Real<F64>::make4(
-                            (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
-                            (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
+                        // centred hi parts are exact (nearby floats); the lo
+                        // parts carry the rest and are differenced separately
+                        s_p[wid][lane] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y),
+                                                          (R)(ph.z - cph.z), (R)ph.w);
+                        s_pl[wid][lane] = make_float4(pl.x - cpl.x, pl.y - cpl.y, pl.z - cpl.z, 0.0f);
                         s_v[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vl.x);
                         s_vl[wid][lane] = make_float2(vl.y, vl.z);
                     }
@@ -259,7 +265,15 @@ density_kernel(const DensityArgs a) {
                 auto pair = [&](int k) {
                     const R4 pj = s_p[wid][k];
                     const R4 vj = s_v[wid][k];
-                    const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                    R dx, dy, dz;
+                    if (F64) {
+                        dx = xi - pj.x; dy = yi - pj.y; dz = zi - pj.z;
+                    } else {
+                        const float4 pl = s_pl[wid][k];
+                        dx = (R)((xhi - (float)pj.x) + (xlo - pl.x));
+                        dy = (R)((yhi - (float)pj.y) + (ylo - pl.y));
+                        dz = (R)((zhi - (float)pj.z) + (zlo - pl.z));
+                    }
                     R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
                     if (!F64) {
                         const float2 vl = s_vl[wid][k];
@@ -384,6 +398,7 @@ hydro_kernel(const HydroArgs a) {
     __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, u (hi)
     __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, vx lo, vy lo
     __shared__ float4 s_f[WARPS][32]; // vz lo, P lo, u lo, -
+    __shared__ float4 s_g[WARPS][32]; // position lo parts (centred)
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -399,6 +414,7 @@ hydro_kernel(const HydroArgs a) {
 
         R xi, yi, zi, vxi, vyi, vzi, hi_i, hi4_i, pp_i, pc_i, bs_i, dn_i, cs_i, al_i, au_i, eg_i, et_i;
         float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f, plo_i = 0.0f, elo_i = 0.0f;
+        float xlo = 0.0f, ylo = 0.0f, zlo = 0.0f;
         float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
         if (F64) {
             const dbl4 p = a.i_pm[ii], v = a.i_vel[ii], h1 = a.i_h1[ii], h2 = a.i_h2[ii];
@@ -410,9 +426,8 @@ hydro_kernel(const HydroArgs a) {
             cph = a.fi.phi[r.ic]; cpl = a.fi.plo[r.ic];
             const float4 ph = a.fi.phi[ii], pl = a.fi.plo[ii], vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
             const float4 g1 = a.fi_g1[ii], g2 = a.fi_g2[ii], g3 = a.fi_g3[ii];
-            xi = df_diff(ph.x, pl.x, cph.x, cpl.x);
-            yi = df_diff(ph.y, pl.y, cph.y, cpl.y);
-            zi = df_diff(ph.z, pl.z, cph.z, cpl.z);
+            xi = ph.x - cph.x; yi = ph.y - cph.y; zi = ph.z - cph.z;   // exact hi parts
+            xlo = pl.x - cpl.x; ylo = pl.y - cpl.y; zlo = pl.z - cpl.z;
             vxi = vh.x; vyi = vh.y; vzi = vh.z;       // absolute hi/lo, differenced per pair
             lxi = vl.x; lyi = vl.y; lzi = vl.z;
             hi_i = vh.w; hi4_i = vl.w;
@@ -439,9 +454,9 @@ hydro_kernel(const HydroArgs a) {
                 } else {
                     const float4 ph = a.fj.phi[j], pl = a.fj.plo[j], vh = a.fj.vhi[j], vl = a.fj.vlo[j];
                     const float4 g1 = a.fj_g1[j], g2 = a.fj_g2[j], g3 = a.fj_g3[j];
-                    s_a[wid][lane] = Real<F64>::make4(
-                        (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
-                        (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
+                    s_a[wid][lane] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y),
+                                                      (R)(ph.z - cph.z), (R)ph.w);
+                    s_g[wid][lane] = make_float4(pl.x - cpl.x, pl.y - cpl.y, pl.z - cpl.z, 0.0f);
                     s_b[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vh.w);
                     s_c[wid][lane] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
                     s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)g3.x);
@@ -459,11 +474,15 @@ hydro_kernel(const HydroArgs a) {
                 const R4 C = s_c[wid][k];
                 const R4 D = s_d[wid][k];
                 const R4 E = s_e[wid][k];
-                const R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
+                R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
                 R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
                 R dp = pp_i - C.x, du = eg_i - D.w;
                 if (!F64) {
                     const float4 F = s_f[wid][k];
+                    const float4 Gl = s_g[wid][k];
+                    dx += (R)(xlo - Gl.x);
+                    dy += (R)(ylo - Gl.y);
+                    dz += (R)(zlo - Gl.z);
                     ux += (R)(lxi - (float)E.z);
                     uy += (R)(lyi - (float)E.w);
                     uz += (R)(lzi - F.x);
