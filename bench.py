@@ -306,6 +306,7 @@ def run_ours(args):
             s_ = np.linalg.norm(b_, axis=1) if b_.ndim > 1 else np.abs(b_)
             floor = (1e-2 if k == "accg1" else 1e-3) * s_.max()
             par[k]["n_above_1e-5"] = int((d_ / np.maximum(s_, floor) > 1e-5).sum())
+            par[k]["normwise"] = float(np.linalg.norm(a_ - b_) / max(np.linalg.norm(b_), 1e-300))
         par["density_rechecked_fp64"] = int(f32["stats"]["density_rechecked"])
         par["same_density_walks"] = f32["stats"]["density_iterations"] == f64["stats"]["density_iterations"]
         par["note"] = ("per-particle |d|/max(|ref|, floor), floor 1e-3 of the field max (1e-2 for the "

@@ -111,7 +111,6 @@ density_kernel(const DensityArgs a) {
     __shared__ R4 s_p[WARPS][32];
     __shared__ R4 s_v[WARPS][32];
     __shared__ float2 s_vl[WARPS][32];
-    __shared__ float4 s_pl[WARPS][32];
     __shared__ long long s_id[WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
@@ -129,7 +128,6 @@ density_kernel(const DensityArgs a) {
         // i-particle relative to the centre particle c
         R xi, yi, zi, vxi, vyi, vzi;
         float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
-        float xhi = 0.0f, yhi = 0.0f, zhi = 0.0f, xlo = 0.0f, ylo = 0.0f, zlo = 0.0f;
         float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
         if (F64) {
             const dbl4 p = a.i_pm[ii], v = a.i_vel[ii];
@@ -141,8 +139,6 @@ density_kernel(const DensityArgs a) {
             xi = (R)df_diff(ph.x, pl.x, cph.x, cpl.x);
             yi = (R)df_diff(ph.y, pl.y, cph.y, cpl.y);
             zi = (R)df_diff(ph.z, pl.z, cph.z, cpl.z);
-            xhi = ph.x - cph.x; yhi = ph.y - cph.y; zhi = ph.z - cph.z;
-            xlo = pl.x - cpl.x; ylo = pl.y - cpl.y; zlo = pl.z - cpl.z;
             // velocities stay absolute hi/lo pairs and are differenced per
             // pair: an item may straddle two colliding streams
             vxi = vh.x; vyi = vh.y; vzi = vh.z;
@@ -249,11 +245,9 @@ density_kernel(const DensityArgs a) {
                     } else {
                         const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
                         const float4 vh = a.fj.vhi[j], vl = a.fj.vlo[j];
-                        // centred hi parts are exact (nearby floats); the lo
-                        // parts carry the rest and are differenced separately
-                        s_p[wid][lane] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y),
-                                                          (R)(ph.z - cph.z), (R)ph.w);
-                        s_pl[wid][lane] = make_float4(pl.x - cpl.x, pl.y - cpl.y, pl.z - cpl.z, 0.0f);
+                        s_p[wid][lane] = Real<F64>::make4(
+                            (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
+                            (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
                         s_v[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vl.x);
                         s_vl[wid][lane] = make_float2(vl.y, vl.z);
                     }
@@ -265,15 +259,7 @@ density_kernel(const DensityArgs a) {
                 auto pair = [&](int k) {
                     const R4 pj = s_p[wid][k];
                     const R4 vj = s_v[wid][k];
-                    R dx, dy, dz;
-                    if (F64) {
-                        dx = xi - pj.x; dy = yi - pj.y; dz = zi - pj.z;
-                    } else {
-                        const float4 pl = s_pl[wid][k];
-                        dx = (R)((xhi - (float)pj.x) + (xlo - pl.x));
-                        dy = (R)((yhi - (float)pj.y) + (ylo - pl.y));
-                        dz = (R)((zhi - (float)pj.z) + (zlo - pl.z));
-                    }
+                    const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
                     R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
                     if (!F64) {
                         const float2 vl = s_vl[wid][k];
