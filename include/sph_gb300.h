@@ -245,6 +245,29 @@ int sph_calc_gravity_sp(sph_context *ctx,
                         const sph_GravitySPJ *spj, int32_t n_j,
                         sph_Gravity *force);
 
+/* Allocation-free variant of sph_calc_gravity_ep for callers that cannot
+ * allocate device memory: code recording a CUDA graph (cudaMalloc cannot be
+ * captured), host callbacks and library hooks that may not synchronise the
+ * device, runtimes that own all device memory through a fixed arena.  No
+ * counterpart in the reference.
+ *
+ * epi, epj and force are DEVICE pointers owned by the caller; the work is
+ * queued on `stream` (a cudaStream_t, NULL = default stream) and the call
+ * returns without waiting.  FP32C arithmetic; forces ACCUMULATE like the
+ * reference functor.  Scratch lives in one file-scope __device__ array of the
+ * library (~2.4 MB, held by every GPU that loads the library until the process
+ * exits), which bounds a call to n_i <= SPH_NOALLOC_MAX_I and
+ * n_j <= SPH_NOALLOC_MAX_J (larger calls return SPH_ERR_CAPACITY).  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress
+ * with that device current): make that first call before any stream capture.
+ * All calls share the array; calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+#define SPH_NOALLOC_MAX_I 4096
+#define SPH_NOALLOC_MAX_J 65536
+int sph_calc_gravity_ep_noalloc(const sph_GravityEPI *epi, int32_t n_i,
+                                const sph_GravityEPJ *epj, int32_t n_j,
+                                sph_Gravity *force, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Batched multiwalk pairs (use_gpu.hpp:28-64).  Dispatch copies the walks to
  * the device and launches; it returns before the kernel finishes.  Retrieve
