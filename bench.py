@@ -257,8 +257,9 @@ def run_ours(args):
                                         "MEASURED_PEAKS.json holds no FP32 figure"},
             "gpu_launches": None, "clocks": clk}
 
-    # kernel launches per step: counted by the engine's structure
-    line["gpu_launches"] = args.steps * LAUNCHES_PER_STEP(args)
+    # kernel launches in the timed region: the kernel nodes of the captured
+    # step graph (CUB sort/scan kernels compiled into the library included)
+    line["gpu_launches"] = args.steps * ps.graph_kernels(step=True)
 
     if rank == 0 and not args.no_fp64:
         # ---- FP64 comparator: parity of one force evaluation of identical
@@ -366,13 +367,6 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-
-
-def LAUNCHES_PER_STEP(args):
-    """Kernel launches of one captured step (memsets and copies excluded):
-    step glue 6, tree/groups 9, per density walk 12 (x max iterations),
-    post-density + refit 2, gravity 8, hydro 9, ksrmax + energy 7."""
-    return 6 + 9 + 12 * 8 + 2 + 8 + 9 + 7
 
 
 # ------------------------------------------------------------------ reference arm

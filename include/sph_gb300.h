@@ -416,6 +416,13 @@ int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t
  * (sph_system_compute_forces and non-captured steps). */
 int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);
 
+/* Kernel launches per replay of the captured graph: step = 1 for the
+ * sph_system_step graph, 0 for the sph_system_compute_forces graph (every
+ * kernel node of the graph, including the predicated density iterations
+ * that return at once when no particle iterates).  SPH_ERR_STATE when that
+ * graph has not been captured. */
+int sph_system_graph_kernels(sph_system *sys, int32_t step, int64_t *kernels);
+
 /* Monopoles of the 2n-1 tree nodes: mom[4*k..] = (x, y, z, mass), eps2[k]. */
 int sph_system_get_nodes(sph_system *sys, double *mom, double *eps2);
 

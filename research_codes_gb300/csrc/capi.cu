@@ -80,7 +80,8 @@ int init_grids(sph_context *ctx) {
     e |= occupancy_grid(sphk::density_kernel<false, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[0][0]);
     e |= occupancy_grid(sphk::density_kernel<true, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[0][1]);
     e |= occupancy_grid(sphk::hydro_kernel<false, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[1][0]);
-    e |= occupancy_grid(sphk::hydro_kernel<true, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[1][1]);
+    e |= occupancy_grid(sphk::hydro_kernel<true, HYDRO64_WARPS>, HYDRO64_WARPS * 32, ctx->sm_count,
+                        &ctx->grid[1][1]);
     e |= occupancy_grid(sphk::gravity_kernel<false, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[2][0]);
     e |= occupancy_grid(sphk::gravity_kernel<true, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[2][1]);
     return e;
@@ -88,7 +89,8 @@ int init_grids(sph_context *ctx) {
 
 int pair_grid(const sph_context *ctx, int kind, int precision, int n_items) {
     const int full = ctx->grid[kind][precision == SPH_PREC_FP64 ? 1 : 0];
-    const int need = (n_items + PAIR_WARPS - 1) / PAIR_WARPS;
+    const int warps = (kind == 1 && precision == SPH_PREC_FP64) ? HYDRO64_WARPS : PAIR_WARPS;
+    const int need = (n_items + warps - 1) / warps;
     return std::max(1, std::min(full, need));
 }
 
@@ -101,7 +103,7 @@ void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStr
 
 void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s) {
     if (precision == SPH_PREC_FP64)
-        sphk::hydro_kernel<true, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
+        sphk::hydro_kernel<true, HYDRO64_WARPS><<<grid, HYDRO64_WARPS * 32, 0, s>>>(a);
     else
         sphk::hydro_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
 }

@@ -10,6 +10,9 @@
 #include "pair_kernels.cuh"
 
 #define PAIR_WARPS 4
+// the FP64 hydro kernel's shared rings need half the warps per block to stay
+// within the 48 KB static shared-memory limit
+#define HYDRO64_WARPS 2
 
 namespace sphrt {
 

@@ -108,12 +108,15 @@ __global__ void __launch_bounds__(WARPS * 32)
 density_kernel(const DensityArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
-    __shared__ R4 s_p[WARPS][32];
-    __shared__ R4 s_v[WARPS][32];
-    __shared__ float2 s_vl[WARPS][32];
-    __shared__ long long s_id[WARPS][32];
+    // per warp a 64-entry ring of compacted j records: entries accumulate
+    // until 32 are ready, the pair loop consumes one 32-entry half at a time
+    __shared__ R4 s_p[WARPS][64];
+    __shared__ R4 s_v[WARPS][64];
+    __shared__ float2 s_vl[WARPS][64];
+    __shared__ long long s_id[WARPS][64];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
     const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
     const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
 
@@ -144,6 +147,11 @@ density_kernel(const DensityArgs a) {
             vxi = vh.x; vyi = vh.y; vzi = vh.z;
             lxi = vl.x; lyi = vl.y; lzi = vl.z;
         }
+        // The kernel is zero for r >= h, so a j-particle farther than the
+        // largest h of the item from the item's box adds nothing to any sum
+        // or count of this item: staging drops it before the pair loop.
+        IBox<R> box;
+        box.from_lanes(xi, yi, zi);
         const long long idi = a.i_id[ii];
         const double rs_i = a.i_rs[ii];
         const double mi = a.i_pm[ii].w;
@@ -152,55 +160,96 @@ density_kernel(const DensityArgs a) {
         long long np = 0;
         bool itr = false;
 
+        // Stages the j-entries [t, t+32) of the list that can lie within
+        // sqrt(rf2) of the box into the ring at (head + fill); with_v also
+        // stages velocities and ids (gradient pass).
+        auto stage = [&](int t, R rf2, int head, int &fill, bool with_v) {
+            const int jk = t + lane;
+            bool keep = false;
+            R4 p4;
+            float4 vh = make_float4(0, 0, 0, 0), vl = vh;
+            dbl4 v64;
+            int j = 0;
+            if (jk < nj) {
+                j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
+                if (F64) {
+                    const dbl4 p = a.j_pm[j];
+                    p4 = Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
+                } else {
+                    const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
+                    p4 = Real<F64>::make4((R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
+                                          (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
+                }
+                keep = !(box.d2(p4.x, p4.y, p4.z) > rf2);
+            }
+            const unsigned m = __ballot_sync(FULL, keep);
+            if (keep) {
+                const int slot = (head + fill + __popc(m & lt)) & 63;
+                s_p[wid][slot] = p4;
+                if (with_v) {
+                    if (F64) {
+                        v64 = a.j_vel[j];
+                        s_v[wid][slot] = Real<F64>::make4((R)v64.x, (R)v64.y, (R)v64.z, (R)0);
+                    } else {
+                        vh = a.fj.vhi[j];
+                        vl = a.fj.vlo[j];
+                        s_v[wid][slot] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vl.x);
+                        s_vl[wid][slot] = make_float2(vl.y, vl.z);
+                    }
+                    s_id[wid][slot] = a.j_id[j];
+                }
+            }
+            fill += __popc(m);
+            __syncwarp();
+        };
+
         // three fixed-point passes, hdr_density.hpp:264-302
         for (int pass = 0; pass < 3; ++pass) {
             const R hinv = (R)1 / (R)h;
             const R hinv2 = hinv * hinv;
+            const R rf2 = support2<R>(h);
             Acc<F64> acc;
             int cnt = 0;
-            for (int t = 0; t < nj; t += 32) {
-                const int jk = t + lane;
-                if (jk < nj) {
-                    const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                    if (F64) {
-                        const dbl4 p = a.j_pm[j];
-                        s_p[wid][lane] = Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
-                    } else {
-                        const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
-                        s_p[wid][lane] = Real<F64>::make4(
-                            (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
-                            (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
-                    }
-                }
-                __syncwarp();
-                const int n = min(32, nj - t);
-                R part = 0;
-                // rho pair term m_j W0(q)/c0; neighbour count only in the
-                // last pass (the only np the reference stores, :297)
-                auto pair = [&](int k, bool count) {
-                    const R4 pj = s_p[wid][k];
-                    const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                    const R r2 = dx * dx + dy * dy + dz * dz;
-                    const R q = sqrt_q(r2, hinv2);
-                    const R u = max0((R)1 - q);
-                    const R u2 = u * u;
-                    part += pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
-                    if (count) cnt += (q < (R)1) ? 1 : 0;
-                };
+            int head = 0, fill = 0;
+            R part = 0;
+            // rho pair term m_j W0(q)/c0; neighbour count only in the last
+            // pass (the only np the reference stores, :297)
+            auto pair = [&](const R4 *tile, int k, bool count) {
+                const R4 pj = tile[k];
+                const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                const R q = sqrt_q(r2, hinv2);
+                const R u = max0((R)1 - q);
+                const R u2 = u * u;
+                part += pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
+                if (count) cnt += (q < (R)1) ? 1 : 0;
+            };
+            auto run = [&](int n) {
+                const R4 *tile = &s_p[wid][head];
+                part = 0;
                 if (tpi == 1 && n == 32) {
                     if (pass == 2) {
 #pragma unroll 8
-                        for (int k = 0; k < 32; ++k) pair(k, true);
+                        for (int k = 0; k < 32; ++k) pair(tile, k, true);
                     } else {
 #pragma unroll 8
-                        for (int k = 0; k < 32; ++k) pair(k, false);
+                        for (int k = 0; k < 32; ++k) pair(tile, k, false);
                     }
                 } else {
-                    for (int k = sub; k < n; k += tpi) pair(k, pass == 2);
+                    for (int k = sub; k < n; k += tpi) pair(tile, k, pass == 2);
                 }
                 acc.add(part);
                 __syncwarp();
+            };
+            for (int t = 0; t < nj; t += 32) {
+                stage(t, rf2, head, fill, false);
+                if (fill >= 32) {
+                    run(32);
+                    head ^= 32;
+                    fill -= 32;
+                }
             }
+            if (fill > 0) run(fill);
             const double sum = seg_sum(acc.value(), tpi);
             const long long c = seg_sum((long long)cnt, tpi);
             double hn;
@@ -232,62 +281,44 @@ density_kernel(const DensityArgs a) {
         // gradient pass with the final h, hdr_density.hpp:304-349
         {
             const R hinv = (R)1 / (R)h;
+            const R rf2 = support2<R>(h);
             Acc<F64> g_acc, d_acc, rx_acc, ry_acc, rz_acc;
-            for (int t = 0; t < nj; t += 32) {
-                const int jk = t + lane;
-                if (jk < nj) {
-                    const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                    if (F64) {
-                        const dbl4 p = a.j_pm[j];
-                        const dbl4 v = a.j_vel[j];
-                        s_p[wid][lane] = Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
-                        s_v[wid][lane] = Real<F64>::make4((R)v.x, (R)v.y, (R)v.z, (R)0);
-                    } else {
-                        const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
-                        const float4 vh = a.fj.vhi[j], vl = a.fj.vlo[j];
-                        s_p[wid][lane] = Real<F64>::make4(
-                            (R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
-                            (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
-                        s_v[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vl.x);
-                        s_vl[wid][lane] = make_float2(vl.y, vl.z);
-                    }
-                    s_id[wid][lane] = a.j_id[j];
+            int head = 0, fill = 0;
+            R pg = 0, pd = 0, prx = 0, pry = 0, prz = 0;
+            auto pair = [&](int k) {
+                const R4 pj = s_p[wid][k];
+                const R4 vj = s_v[wid][k];
+                const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
+                if (!F64) {
+                    const float2 vl = s_vl[wid][k];
+                    ux += (R)(lxi - (float)vj.w);
+                    uy += (R)(lyi - vl.x);
+                    uz += (R)(lzi - vl.y);
                 }
-                __syncwarp();
-                const int n = min(32, nj - t);
-                R pg = 0, pd = 0, prx = 0, pry = 0, prz = 0;
-                auto pair = [&](int k) {
-                    const R4 pj = s_p[wid][k];
-                    const R4 vj = s_v[wid][k];
-                    const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                    R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
-                    if (!F64) {
-                        const float2 vl = s_vl[wid][k];
-                        ux += (R)(lxi - (float)vj.w);
-                        uy += (R)(lyi - vl.x);
-                        uz += (R)(lzi - vl.y);
-                    }
-                    const R r2 = dx * dx + dy * dy + dz * dz;
-                    const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
-                    const R q = r2 * ri * hinv;
-                    const R u = max0((R)1 - q);
-                    const R u2 = u * u;
-                    const R u3 = u2 * u;
-                    const R p14 = (R)1 + (R)4 * q;
-                    const R w0 = u2 * u2 * p14;            // W0 / c0
-                    const R w1 = w1_term(q, u, u2, u3, p14);   // W1 / c1
-                    pg += pj.w * ((R)(3.0 * CEFF0) * w0 + (R)CEFF1 * q * w1);
-                    const R dw = pj.w * w1 * ri;
-                    pd += (ux * dx + uy * dy + uz * dz) * dw;
-                    prx += (uy * dz - uz * dy) * dw;
-                    pry += (uz * dx - ux * dz) * dw;
-                    prz += (ux * dy - uy * dx) * dw;
-                };
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
+                const R q = r2 * ri * hinv;
+                const R u = max0((R)1 - q);
+                const R u2 = u * u;
+                const R u3 = u2 * u;
+                const R p14 = (R)1 + (R)4 * q;
+                const R w0 = u2 * u2 * p14;            // W0 / c0
+                const R w1 = w1_term(q, u, u2, u3, p14);   // W1 / c1
+                pg += pj.w * ((R)(3.0 * CEFF0) * w0 + (R)CEFF1 * q * w1);
+                const R dw = pj.w * w1 * ri;
+                pd += (ux * dx + uy * dy + uz * dz) * dw;
+                prx += (uy * dz - uz * dy) * dw;
+                pry += (uz * dx - ux * dz) * dw;
+                prz += (ux * dy - uy * dx) * dw;
+            };
+            auto run = [&](int n) {
+                pg = 0; pd = 0; prx = 0; pry = 0; prz = 0;
                 if (tpi == 1 && n == 32) {
 #pragma unroll 4
-                    for (int k = 0; k < 32; ++k) pair(k);
+                    for (int k = 0; k < 32; ++k) pair(head + k);
                 } else {
-                    for (int k = sub; k < n; k += tpi) pair(k);
+                    for (int k = sub; k < n; k += tpi) pair(head + k);
                 }
                 g_acc.add(pg);
                 d_acc.add(pd);
@@ -295,7 +326,16 @@ density_kernel(const DensityArgs a) {
                 ry_acc.add(pry);
                 rz_acc.add(prz);
                 __syncwarp();
+            };
+            for (int t = 0; t < nj; t += 32) {
+                stage(t, rf2, head, fill, true);
+                if (fill >= 32) {
+                    run(32);
+                    head ^= 32;
+                    fill -= 32;
+                }
             }
+            if (fill > 0) run(fill);
             const double sg = seg_sum(g_acc.value(), tpi);
             const double sd = seg_sum(d_acc.value(), tpi);
             const double sx = seg_sum(rx_acc.value(), tpi);
@@ -378,16 +418,25 @@ __global__ void __launch_bounds__(WARPS * 32)
 hydro_kernel(const HydroArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
-    __shared__ R4 s_a[WARPS][32];   // dx, dy, dz, mass
-    __shared__ R4 s_b[WARPS][32];   // vx, vy, vz (hi), hinv
-    __shared__ R4 s_c[WARPS][32];   // P (hi), presc, bswt, dens
-    __shared__ R4 s_d[WARPS][32];   // vsnd, alph, alphu, u (hi)
-    __shared__ R4 s_e[WARPS][32];   // eta, hinv^4, vx lo, vy lo
-    __shared__ float4 s_f[WARPS][32]; // vz lo, P lo, u lo, -
-    __shared__ float4 s_g[WARPS][32]; // position lo parts (centred)
-    __shared__ long long s_id[WARPS][32];
+    // Two 64-entry rings of compacted j records per warp.  Near ring: the
+    // j-particles that can lie within the kernel support of some i-particle
+    // of the item (r < max(h_i, h_j)), with every field of the pair formula.
+    // Far ring: the others, whose pair terms all vanish except the
+    // signal-velocity maximum (hdr_hydro.hpp:372 takes it over every j of
+    // the list), kept as position + sound speed and velocity only.
+    __shared__ R4 s_a[WARPS][64];   // dx, dy, dz (exact hi parts), mass
+    __shared__ R4 s_b[WARPS][64];   // vx, vy, vz (hi), hinv
+    __shared__ R4 s_c[WARPS][64];   // P (hi), presc, bswt, dens
+    __shared__ R4 s_d[WARPS][64];   // vsnd, alph, alphu, u (hi)
+    __shared__ R4 s_e[WARPS][64];   // eta, hinv^4, vx lo, vy lo
+    __shared__ float4 s_f[WARPS][64]; // vz lo, P lo, u lo, -
+    __shared__ float4 s_g[WARPS][64]; // position lo parts (centred)
+    __shared__ long long s_id[WARPS][64];
+    __shared__ R4 s_fp[WARPS][64];  // far: centred position, vsnd
+    __shared__ R4 s_fv[WARPS][64];  // far: velocity (hi)
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
     const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
 
     for (;;) {
@@ -422,99 +471,91 @@ hydro_kernel(const HydroArgs a) {
             eg_i = g3.x; elo_i = g3.y; et_i = g3.z;
         }
         const long long idi = a.i_id[ii];
+        // i position in the item frame as one number (box and far pairs)
+        const R xc = xi + (R)xlo, yc = yi + (R)ylo, zc = zi + (R)zlo;
+        IBox<R> box;
+        box.from_lanes(xc, yc, zc);
+        const R hm2 = support2<R>(1.0 / (double)hi_i);
 
         Acc<F64> ax, ay, az, ud, df, gx, gy, gz;
         R vsmx = 0;
-        for (int t = 0; t < nj; t += 32) {
-            const int jk = t + lane;
-            if (jk < nj) {
-                const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                if (F64) {
-                    const dbl4 p = a.j_pm[j], v = a.j_vel[j], g1 = a.j_h1[j], g2 = a.j_h2[j];
-                    const double2 g3 = a.j_h3[j];
-                    s_a[wid][lane] = Real<F64>::make4(p.x, p.y, p.z, p.w);
-                    s_b[wid][lane] = Real<F64>::make4(v.x, v.y, v.z, g1.x);
-                    s_c[wid][lane] = Real<F64>::make4(g1.y, g1.z, g1.w, g2.x);
-                    s_d[wid][lane] = Real<F64>::make4(g2.y, g2.z, g2.w, g3.x);
-                    s_e[wid][lane] = Real<F64>::make4(g3.y, g1.x * g1.x * g1.x * g1.x, 0.0, 0.0);
-                } else {
-                    const float4 ph = a.fj.phi[j], pl = a.fj.plo[j], vh = a.fj.vhi[j], vl = a.fj.vlo[j];
-                    const float4 g1 = a.fj_g1[j], g2 = a.fj_g2[j], g3 = a.fj_g3[j];
-                    s_a[wid][lane] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y),
-                                                      (R)(ph.z - cph.z), (R)ph.w);
-                    s_g[wid][lane] = make_float4(pl.x - cpl.x, pl.y - cpl.y, pl.z - cpl.z, 0.0f);
-                    s_b[wid][lane] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vh.w);
-                    s_c[wid][lane] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
-                    s_d[wid][lane] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)g3.x);
-                    s_e[wid][lane] = Real<F64>::make4((R)g3.z, (R)vl.w, (R)vl.x, (R)vl.y);
-                    s_f[wid][lane] = make_float4(vl.z, g1.y, g3.y, 0.0f);
-                }
-                s_id[wid][lane] = a.j_id[j];
+        int nhead = 0, nfill = 0, fhead = 0, ffill = 0;
+        R pax = 0, pay = 0, paz = 0, pud = 0, pdf = 0, pgx = 0, pgy = 0, pgz = 0;
+        auto pair = [&](int k) {
+            const R4 A = s_a[wid][k];
+            const R4 B = s_b[wid][k];
+            const R4 C = s_c[wid][k];
+            const R4 D = s_d[wid][k];
+            const R4 E = s_e[wid][k];
+            R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
+            R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
+            R dp = pp_i - C.x, du = eg_i - D.w;
+            if (!F64) {
+                const float4 F = s_f[wid][k];
+                const float4 Gl = s_g[wid][k];
+                dx += (R)(xlo - Gl.x);
+                dy += (R)(ylo - Gl.y);
+                dz += (R)(zlo - Gl.z);
+                ux += (R)(lxi - (float)E.z);
+                uy += (R)(lyi - (float)E.w);
+                uz += (R)(lzi - F.x);
+                dp += (R)(plo_i - F.y);
+                du += (R)(elo_i - F.z);
             }
-            __syncwarp();
-            const int n = min(32, nj - t);
-            R pax = 0, pay = 0, paz = 0, pud = 0, pdf = 0, pgx = 0, pgy = 0, pgz = 0;
-            auto pair = [&](int k) {
-                const R4 A = s_a[wid][k];
-                const R4 B = s_b[wid][k];
-                const R4 C = s_c[wid][k];
-                const R4 D = s_d[wid][k];
-                const R4 E = s_e[wid][k];
-                R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
-                R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
-                R dp = pp_i - C.x, du = eg_i - D.w;
-                if (!F64) {
-                    const float4 F = s_f[wid][k];
-                    const float4 Gl = s_g[wid][k];
-                    dx += (R)(xlo - Gl.x);
-                    dy += (R)(ylo - Gl.y);
-                    dz += (R)(zlo - Gl.z);
-                    ux += (R)(lxi - (float)E.z);
-                    uy += (R)(lyi - (float)E.w);
-                    uz += (R)(lzi - F.x);
-                    dp += (R)(plo_i - F.y);
-                    du += (R)(elo_i - F.z);
-                }
-                const R r2 = dx * dx + dy * dy + dz * dz;
-                const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
-                const R rr = r2 * ri;
-                // kernel gradients W1(q) for both smoothing lengths
-                const R qi = rr * hi_i, qj = rr * B.w;
-                const R ui = max0((R)1 - qi), uj = max0((R)1 - qj);
-                const R ui2 = ui * ui, uj2 = uj * uj;
-                const R w1i = w1_term(qi, ui, ui2, ui2 * ui, (R)1 + (R)4 * qi);
-                const R w1j = w1_term(qj, uj, uj2, uj2 * uj, (R)1 + (R)4 * qj);
-                const R dw_i = (R)CEFF1 * hi4_i * w1i;
-                const R dw_j = (R)CEFF1 * E.y * w1j;
-                const R ka = (dw_i + dw_j) * A.w;
-                // viscosity, hdr_hydro.hpp:368-376
-                const R w = (dx * ux + dy * uy + dz * uz) * ri;
-                const R wneg = w < (R)0 ? w : (R)0;
-                const R vs = cs_i + D.x - (R)3 * wneg;
-                const R rhi = rcp_r(dn_i + C.w);
-                const R av = (bs_i + C.z) * (al_i + D.y) * vs * wneg;
-                vsmx = vs > vsmx ? vs : vsmx;
-                // pressure gradient, :378-382
-                const R ta = (pc_i + C.y - (R)0.5 * av * rhi) * ka * ri;
-                pax -= ta * dx;
-                pay -= ta * dy;
-                paz -= ta * dz;
-                // energy equation with conduction, :384-393
-                const R vsu2 = fabs(dp) * rhi * (R)2;
-                const R vsu = vsu2 > (R)0 ? vsu2 * rsqrt_r(vsu2) : (R)0;
-                pud += ka * (pc_i * w - rhi * ((R)0.25 * av * wneg - (au_i + D.z) * vsu * du));
-                pdf += rhi * du * ka * ri;
-                // softening correction, :395-398
-                const R dg = A.w * ri * (et_i * dw_i + E.x * dw_j);
-                pgx += dg * dx;
-                pgy += dg * dy;
-                pgz += dg * dz;
-            };
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
+            const R rr = r2 * ri;
+            // kernel gradients W1(q) for both smoothing lengths
+            const R qi = rr * hi_i, qj = rr * B.w;
+            const R ui = max0((R)1 - qi), uj = max0((R)1 - qj);
+            const R ui2 = ui * ui, uj2 = uj * uj;
+            const R w1i = w1_term(qi, ui, ui2, ui2 * ui, (R)1 + (R)4 * qi);
+            const R w1j = w1_term(qj, uj, uj2, uj2 * uj, (R)1 + (R)4 * qj);
+            const R dw_i = (R)CEFF1 * hi4_i * w1i;
+            const R dw_j = (R)CEFF1 * E.y * w1j;
+            const R ka = (dw_i + dw_j) * A.w;
+            // viscosity, hdr_hydro.hpp:368-376
+            const R w = (dx * ux + dy * uy + dz * uz) * ri;
+            const R wneg = w < (R)0 ? w : (R)0;
+            const R vs = cs_i + D.x - (R)3 * wneg;
+            const R rhi = rcp_r(dn_i + C.w);
+            const R av = (bs_i + C.z) * (al_i + D.y) * vs * wneg;
+            vsmx = vs > vsmx ? vs : vsmx;
+            // pressure gradient, :378-382
+            const R ta = (pc_i + C.y - (R)0.5 * av * rhi) * ka * ri;
+            pax -= ta * dx;
+            pay -= ta * dy;
+            paz -= ta * dz;
+            // energy equation with conduction, :384-393
+            const R vsu2 = fabs(dp) * rhi * (R)2;
+            const R vsu = vsu2 > (R)0 ? vsu2 * rsqrt_r(vsu2) : (R)0;
+            pud += ka * (pc_i * w - rhi * ((R)0.25 * av * wneg - (au_i + D.z) * vsu * du));
+            pdf += rhi * du * ka * ri;
+            // softening correction, :395-398
+            const R dg = A.w * ri * (et_i * dw_i + E.x * dw_j);
+            pgx += dg * dx;
+            pgy += dg * dy;
+            pgz += dg * dz;
+        };
+        // a j beyond both supports: only the signal velocity (r > 0 here)
+        auto far_pair = [&](int k) {
+            const R4 P = s_fp[wid][k];
+            const R4 V = s_fv[wid][k];
+            const R dx = xc - P.x, dy = yc - P.y, dz = zc - P.z;
+            const R ux = vxi - V.x, uy = vyi - V.y, uz = vzi - V.z;
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            const R w = (dx * ux + dy * uy + dz * uz) * rsqrt_r(r2);
+            const R wneg = w < (R)0 ? w : (R)0;
+            const R vs = cs_i + P.w - (R)3 * wneg;
+            vsmx = vs > vsmx ? vs : vsmx;
+        };
+        auto run_near = [&](int n) {
+            pax = 0; pay = 0; paz = 0; pud = 0; pdf = 0; pgx = 0; pgy = 0; pgz = 0;
             if (tpi == 1 && n == 32) {
 #pragma unroll 2
-                for (int k = 0; k < 32; ++k) pair(k);
+                for (int k = 0; k < 32; ++k) pair(nhead + k);
             } else {
-                for (int k = sub; k < n; k += tpi) pair(k);
+                for (int k = sub; k < n; k += tpi) pair(nhead + k);
             }
             ax.add(pax);
             ay.add(pay);
@@ -525,7 +566,98 @@ hydro_kernel(const HydroArgs a) {
             gy.add(pgy);
             gz.add(pgz);
             __syncwarp();
+        };
+        auto run_far = [&](int n) {
+            if (tpi == 1 && n == 32) {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) far_pair(fhead + k);
+            } else {
+                for (int k = sub; k < n; k += tpi) far_pair(fhead + k);
+            }
+            __syncwarp();
+        };
+        for (int t = 0; t < nj; t += 32) {
+            const int jk = t + lane;
+            bool near = false, far = false;
+            int j = 0;
+            float4 ph, pl, vh, g2;
+            double4_32a p64, v64, g1_64, g2_64;
+            R px = 0, py = 0, pz = 0, hj_inv = 0;
+            if (jk < nj) {
+                j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
+                if (F64) {
+                    p64 = a.j_pm[j];
+                    v64 = a.j_vel[j];
+                    g1_64 = a.j_h1[j];
+                    g2_64 = a.j_h2[j];
+                    px = p64.x; py = p64.y; pz = p64.z; hj_inv = g1_64.x;
+                } else {
+                    ph = a.fj.phi[j];
+                    pl = a.fj.plo[j];
+                    vh = a.fj.vhi[j];
+                    g2 = a.fj_g2[j];
+                    px = df_diff(ph.x, pl.x, cph.x, cpl.x);
+                    py = df_diff(ph.y, pl.y, cph.y, cpl.y);
+                    pz = df_diff(ph.z, pl.z, cph.z, cpl.z);
+                    hj_inv = vh.w;
+                }
+                const R hj = (R)1 / hj_inv;
+                const R hj2 = hj * hj * (R)1.0002;
+                const R rf2 = hj2 > hm2 ? hj2 : hm2;
+                near = !(box.d2(px, py, pz) > rf2) || !(hj2 >= (R)0);
+                far = !near;
+            }
+            const unsigned mn = __ballot_sync(FULL, near);
+            const unsigned mf = __ballot_sync(FULL, far);
+            if (near) {
+                const int k = (nhead + nfill + __popc(mn & lt)) & 63;
+                if (F64) {
+                    const dbl4 g1 = g1_64, g2d = g2_64;
+                    const double2 g3 = a.j_h3[j];
+                    s_a[wid][k] = Real<F64>::make4(p64.x, p64.y, p64.z, p64.w);
+                    s_b[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z, g1.x);
+                    s_c[wid][k] = Real<F64>::make4(g1.y, g1.z, g1.w, g2d.x);
+                    s_d[wid][k] = Real<F64>::make4(g2d.y, g2d.z, g2d.w, g3.x);
+                    s_e[wid][k] = Real<F64>::make4(g3.y, g1.x * g1.x * g1.x * g1.x, 0.0, 0.0);
+                } else {
+                    const float4 vl = a.fj.vlo[j], g1 = a.fj_g1[j], g3 = a.fj_g3[j];
+                    s_a[wid][k] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y),
+                                                   (R)(ph.z - cph.z), (R)ph.w);
+                    s_g[wid][k] = make_float4(pl.x - cpl.x, pl.y - cpl.y, pl.z - cpl.z, 0.0f);
+                    s_b[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vh.w);
+                    s_c[wid][k] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
+                    s_d[wid][k] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)g3.x);
+                    s_e[wid][k] = Real<F64>::make4((R)g3.z, (R)vl.w, (R)vl.x, (R)vl.y);
+                    s_f[wid][k] = make_float4(vl.z, g1.y, g3.y, 0.0f);
+                }
+                s_id[wid][k] = a.j_id[j];
+            }
+            if (far) {
+                const int k = (fhead + ffill + __popc(mf & lt)) & 63;
+                if (F64) {
+                    s_fp[wid][k] = Real<F64>::make4(px, py, pz, g2_64.y);
+                    s_fv[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z, 0.0);
+                } else {
+                    s_fp[wid][k] = Real<F64>::make4(px, py, pz, (R)g2.y);
+                    s_fv[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)0);
+                }
+            }
+            nfill += __popc(mn);
+            ffill += __popc(mf);
+            __syncwarp();
+            if (nfill >= 32) {
+                run_near(32);
+                nhead ^= 32;
+                nfill -= 32;
+            }
+            if (ffill >= 32) {
+                run_far(32);
+                fhead ^= 32;
+                ffill -= 32;
+            }
         }
+        if (nfill > 0) run_near(nfill);
+        if (ffill > 0) run_far(ffill);
         const double sax = seg_sum(ax.value(), tpi), say = seg_sum(ay.value(), tpi);
         const double saz = seg_sum(az.value(), tpi), sud = seg_sum(ud.value(), tpi);
         const double sdf = seg_sum(df.value(), tpi), sgx = seg_sum(gx.value(), tpi);

@@ -138,4 +138,58 @@ __device__ __forceinline__ int lanes_per_i(int n_i) {
 
 __device__ __forceinline__ int ilog2_pow2(int x) { return __ffs(x) - 1; }
 
+// Minimum / maximum over the 32 lanes of a warp (NaN lanes are ignored).
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+
+// Bit mask of the lanes below this one.
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Axis-aligned box of a work item's i-particles, in the item's frame.
+template <typename R>
+struct IBox {
+    R xl, yl, zl, xh, yh, zh;
+    __device__ __forceinline__ void from_lanes(R x, R y, R z) {
+        xl = warp_min(x); yl = warp_min(y); zl = warp_min(z);
+        xh = warp_max(x); yh = warp_max(y); zh = warp_max(z);
+    }
+    // squared distance from (x, y, z) to the box (0 inside)
+    __device__ __forceinline__ R d2(R x, R y, R z) const {
+        const R dx = max0(fmax(xl - x, x - xh));
+        const R dy = max0(fmax(yl - y, y - yh));
+        const R dz = max0(fmax(zl - z, z - zh));
+        return dx * dx + dy * dy + dz * dz;
+    }
+};
+
+// Squared support radius beyond which no i-particle of the item interacts
+// with a j-particle, from the lanes' h: (max h)^2 widened by 2e-4 so that the
+// FP32 rounding of the pair distance cannot turn a kept pair into a dropped
+// one.  Any lane with an h that is not a non-negative number makes the radius
+// infinite (nothing is dropped, the pair arithmetic decides as without it).
+template <typename R>
+__device__ __forceinline__ R support2(double h) {
+    const bool bad = __any_sync(FULL, !(h >= 0.0));
+    const R hm = warp_max((R)h);
+    return bad ? (R)INFINITY : hm * hm * (R)1.0002;
+}
+
 }  // namespace sphk

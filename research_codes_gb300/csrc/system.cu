@@ -27,13 +27,15 @@ using sphrt::HostBuf;
 namespace {
 
 constexpr double KSRH = sphk::KSRH;
+constexpr int ITEM_SPLIT_NJ = 4096;   // list length above which a walk's items are halved (down to 4 i)
 constexpr int RED_BLOCKS = 296;   // 2 x 148..152 SMs; fixed for deterministic sums
 constexpr int RED_THREADS = 256;
 constexpr int MAX_RED = 8;
 
 // int scalars
+constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_NI };
+       S_BKT, S_NI = S_BKT + 2 * NBKT };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -294,28 +296,74 @@ __global__ void list_total(int n, const int *cnt, const int *off, long long cap,
 // work items: walk k gets ceil(n_i/chunk) items over its i-segment
 // [i_first[k], i_first[k] + i_count[k]) (particle indices or positions in
 // an index list)
-__global__ void item_counts(int n, const int *n_walks, const int *i_count, int chunk, int *c) {
-    const int nw = *n_walks;
-    GRID_STRIDE(k, n) { c[k] = (k < nw) ? (i_count[k] + chunk - 1) / chunk : 0; }
+// Item size of a walk: walks with long lists are cut into items of fewer
+// i-particles (several lanes per i-particle, each lane a share of the list),
+// so that no single item runs much longer than a warp's share of the phase.
+__device__ __forceinline__ int item_chunk(int nj, int chunk, int split_nj) {
+    int c = chunk;
+    long long lim = split_nj;
+    while (c > 4 && nj > lim) {
+        c >>= 1;
+        lim <<= 1;
+    }
+    return c;
 }
 
+// Cost class of an item of sz i-particles against nj j-entries: staging
+// grows with nj, the pair loops with nj * sz.
+__device__ __forceinline__ int cost_bucket(int nj, int sz) {
+    const long long c = (long long)nj * (sz + 2) + 1;
+    return min(NBKT - 1, 63 - __clzll(c));
+}
+
+// Histogram of the items of all walks over the cost classes (bkt[0..NBKT),
+// zero on entry).
+__global__ void item_buckets(int n, const int *n_walks, const int *i_count, const int *j_cnt, int chunk,
+                             int split_nj, int *bkt) {
+    const int nw = *n_walks;
+    GRID_STRIDE(k, n) {
+        if (k < nw) {
+            const int ni = i_count[k], nj = j_cnt[k];
+            const int ch = item_chunk(nj, chunk, split_nj);
+            const int full = ni / ch, rest = ni - full * ch;
+            if (full) atomicAdd(&bkt[cost_bucket(nj, ch)], full);
+            if (rest) atomicAdd(&bkt[cost_bucket(nj, rest)], 1);
+        }
+    }
+}
+
+// Start of each cost class in the item array, most expensive class first
+// (bkt[NBKT + b]), and the item count.
+__global__ void bucket_offsets(int *bkt, int *n_items) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = NBKT - 1; b >= 0; --b) {
+            bkt[NBKT + b] = acc;
+            acc += bkt[b];
+        }
+        *n_items = acc;
+    }
+}
+
+// Work items in decreasing cost class, so that the persistent kernels take
+// the longest items first and finish on short ones.  The order of items
+// inside a class does not affect any result (every item owns its outputs).
 __global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count, int chunk,
-                           const int *item_off, const int *item_cnt, const int *j_off, const int *j_cnt,
-                           WorkItem *items, int *n_items, long long *pairs) {
+                           int split_nj, const int *j_cnt, int *cursor, WorkItem *items, long long *pairs) {
     const int nw = *n_walks;
     long long local = 0;
     GRID_STRIDE(k, n) {
         if (k < nw) {
-            const int base = item_off[k];
             const int ni = i_count[k];
             const int nj = j_cnt[k];
-            for (int c = 0; c < item_cnt[k]; ++c) {
-                const int sz = min(chunk, ni - chunk * c);
-                items[base + c] = make_int4(k, i_first[k] + chunk * c, sz, nj * sz);
+            const int ch = item_chunk(nj, chunk, split_nj);
+            for (int c0 = 0; c0 < ni; c0 += ch) {
+                const int sz = min(ch, ni - c0);
+                const int pos = atomicAdd(&cursor[cost_bucket(nj, sz)], 1);
+                items[pos] = make_int4(k, i_first[k] + c0, sz, nj * sz);
             }
             local += (long long)ni * nj;
         }
-        if (k == n - 1) *n_items = item_off[k] + item_cnt[k];
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd((unsigned long long *)pairs, (unsigned long long)local);
@@ -632,7 +680,6 @@ struct sph_system {
     int *walk_first[4] = {nullptr, nullptr, nullptr, nullptr};
     int *walk_count[4] = {nullptr, nullptr, nullptr, nullptr};
     int *walk_num[4] = {nullptr, nullptr, nullptr, nullptr};   // device count of walks
-    DevBuf<int> icnt, ioff;
     DevBuf<WorkItem> items;
     // scalars
     DevBuf<int> scal;
@@ -651,6 +698,7 @@ struct sph_system {
     cudaGraphExec_t force_exec = nullptr;
     bool force_graph_valid = false;
     int force_graph_precision = -1;
+    long long graph_kernels[2] = {-1, -1};   // kernel nodes of the force / step graph
     // phase events
     cudaEvent_t ev[16] = {nullptr};
     long long steps = 0;
@@ -705,7 +753,7 @@ int alloc_all(sph_system *s) {
     s->amb_cap = std::max<int>(1024, s->n / 16);
     e |= s->amb_i.ensure(s->amb_cap) | s->amb_w.ensure(s->amb_cap) | s->fitems.ensure(s->amb_cap);
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
-                         &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff};
+                         &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count};
     for (auto *b : i1) e |= b->ensure(n);
     for (int k = 0; k < 4; ++k) e |= s->lcnt[k].ensure(n) | s->loff[k].ensure(n);
     e |= s->items.ensure(n);
@@ -848,12 +896,15 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
     const int *icount = item_count ? item_count : s->walk_count[kind];
-    item_counts<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, chunk, s->icnt.p);
-    r = exclusive_scan(s, s->icnt.p, s->ioff.p);
-    if (r) return r;
-    fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], ifirst, icount, chunk, s->ioff.p, s->icnt.p,
-                                            s->loff[kind].p, s->lcnt[kind].p, s->items.p, s->scal.p + S_NITEMS,
-                                            pairs);
+    // density and hydro walks with long lists are split (their pair loops
+    // drop most of the list); gravity lists are uniform and kept whole
+    const int split_nj = (kind == 2) ? (1 << 30) : ITEM_SPLIT_NJ;
+    int *bkt = s->scal.p + S_BKT;
+    CUDA_TRY(cudaMemsetAsync(bkt, 0, sizeof(int) * 2 * NBKT, st));
+    item_buckets<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj, bkt);
+    bucket_offsets<<<1, 32, 0, st>>>(bkt, s->scal.p + S_NITEMS);
+    fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], ifirst, icount, chunk, split_nj, s->lcnt[kind].p,
+                                            bkt + NBKT, s->items.p, pairs);
     return SPH_OK;
 }
 
@@ -1170,7 +1221,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
     s->uflag.release(); s->uscan.release(); s->ulist.release(); s->a_sfirst.release(); s->a_scount.release();
     s->amb_i.release(); s->amb_w.release(); s->fitems.release();
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
-                         &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count, &s->icnt, &s->ioff,
+                         &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count,
                          &s->scal};
     for (auto *b : i1) b->release();
     for (int k = 0; k < 4; ++k) {
@@ -1254,6 +1305,21 @@ extern "C" int sph_system_upload(sph_system *s, double t0, const int64_t *id, co
 }
 
 namespace {
+// Number of kernel nodes of a captured graph (one launch each per replay).
+long long count_kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return -1;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n && cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return -1;
+    long long k = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess) return -1;
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
 int capture(sph_system *s, bool step, cudaGraphExec_t *exec) {
     cudaStream_t st = s->st();
     if (*exec) {
@@ -1269,6 +1335,7 @@ int capture(sph_system *s, bool step, cudaGraphExec_t *exec) {
         return rc;
     }
     if (ec != cudaSuccess) return sphrt::cuda_error(s->ctx, ec, "cudaStreamEndCapture");
+    s->graph_kernels[step ? 1 : 0] = count_kernel_nodes(g);
     const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     if (ei != cudaSuccess) return sphrt::cuda_error(s->ctx, ei, "cudaGraphInstantiate");
@@ -1299,6 +1366,15 @@ extern "C" int sph_system_compute_forces(sph_system *s) {
     }
     s->last_status = r;
     return r;
+}
+
+extern "C" int sph_system_graph_kernels(sph_system *s, int32_t step, int64_t *kernels) {
+    if (!s || !kernels) return SPH_ERR_INVALID_ARGUMENT;
+    const bool valid = step ? s->graph_valid : s->force_graph_valid;
+    const long long k = s->graph_kernels[step ? 1 : 0];
+    if (!valid || k < 0) return SPH_ERR_STATE;
+    *kernels = k;
+    return SPH_OK;
 }
 
 extern "C" int sph_system_set_graph(sph_system *s, int32_t use_graph) {

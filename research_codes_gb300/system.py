@@ -64,6 +64,7 @@ def _declare(lib):
         "sph_system_get_nodes": (ctypes.c_int, [_P, _P, _P]),
         "sph_system_phase_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), _I32]),
         "sph_system_set_graph": (ctypes.c_int, [_P, _I32]),
+        "sph_system_graph_kernels": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_int64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -130,6 +131,13 @@ class ParticleSystem:
 
     def set_graph(self, on):
         check(self.lib.sph_system_set_graph(self.handle, 1 if on else 0), self.ctx.handle, "set_graph")
+
+    def graph_kernels(self, step=True):
+        """Kernel launches per replay of the captured step (or force) graph."""
+        k = ctypes.c_int64(0)
+        check(self.lib.sph_system_graph_kernels(self.handle, 1 if step else 0, ctypes.byref(k)),
+              self.ctx.handle, "graph_kernels")
+        return int(k.value)
 
     def step(self, n_steps=1):
         check(self.lib.sph_system_step(self.handle, n_steps), self.ctx.handle, "step")

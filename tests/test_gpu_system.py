@@ -197,6 +197,13 @@ def test_graph_replay_equals_eager_steps():
             sys.upload(s)
             sys.compute_forces()
             sys.step(4)
+            if use_graph:
+                # both graphs captured; the step graph holds the force graph's kernels and the step glue
+                kf, ks = sys.graph_kernels(step=False), sys.graph_kernels(step=True)
+                assert 0 < kf < ks, (kf, ks)
+            else:
+                with pytest.raises(abi.SPHError):
+                    sys.graph_kernels(step=True)
             out[use_graph] = (sys.download("pos"), sys.download("vel"), sys.download("uene"), sys.stats())
             sys.close()
     assert np.array_equal(out[0][0], out[1][0])
