@@ -24,6 +24,15 @@
 
 #include "sph_device.cuh"
 
+// Minimum resident blocks per SM requested from the compiler for the FP32C
+// density and hydro kernels (register budget 65536 / (128 threads x blocks)).
+#ifndef SPH_DENSITY_MIN_BLOCKS
+#define SPH_DENSITY_MIN_BLOCKS 5
+#endif
+#ifndef SPH_HYDRO_MIN_BLOCKS
+#define SPH_HYDRO_MIN_BLOCKS 4
+#endif
+
 namespace sphk {
 
 // Double-float particle records of FP32C mode.
@@ -104,7 +113,7 @@ struct DensityArgs {
 };
 
 template <bool F64, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_DENSITY_MIN_BLOCKS)
 density_kernel(const DensityArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
@@ -160,47 +169,80 @@ density_kernel(const DensityArgs a) {
         long long np = 0;
         bool itr = false;
 
-        // Stages the j-entries [t, t+32) of the list that can lie within
-        // sqrt(rf2) of the box into the ring at (head + fill); with_v also
-        // stages velocities and ids (gradient pass).
-        auto stage = [&](int t, R rf2, int head, int &fill, bool with_v) {
-            const int jk = t + lane;
-            bool keep = false;
-            R4 p4;
-            float4 vh = make_float4(0, 0, 0, 0), vl = vh;
-            dbl4 v64;
-            int j = 0;
-            if (jk < nj) {
-                j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
-                if (F64) {
-                    const dbl4 p = a.j_pm[j];
-                    p4 = Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
-                } else {
-                    const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
-                    p4 = Real<F64>::make4((R)df_diff(ph.x, pl.x, cph.x, cpl.x), (R)df_diff(ph.y, pl.y, cph.y, cpl.y),
-                                          (R)df_diff(ph.z, pl.z, cph.z, cpl.z), (R)ph.w);
-                }
-                keep = !(box.d2(p4.x, p4.y, p4.z) > rf2);
-            }
-            const unsigned m = __ballot_sync(FULL, keep);
-            if (keep) {
-                const int slot = (head + fill + __popc(m & lt)) & 63;
-                s_p[wid][slot] = p4;
+        // One j record as loaded from memory (FP32C double-float or FP64).
+        struct JRec {
+            float4 ph, pl, vh, vl;
+            dbl4 p, v;
+            long long id;
+        };
+        auto jlist = [&](int k) -> int { return a.j_idx ? a.j_idx[jb + k] : jb + k; };
+        auto load = [&](int j, bool with_v, JRec &q) {
+            if constexpr (F64) {
+                q.p = a.j_pm[j];
+                if (with_v) q.v = a.j_vel[j];
+            } else {
+                q.ph = a.fj.phi[j];
+                q.pl = a.fj.plo[j];
                 if (with_v) {
-                    if (F64) {
-                        v64 = a.j_vel[j];
-                        s_v[wid][slot] = Real<F64>::make4((R)v64.x, (R)v64.y, (R)v64.z, (R)0);
-                    } else {
-                        vh = a.fj.vhi[j];
-                        vl = a.fj.vlo[j];
-                        s_v[wid][slot] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vl.x);
-                        s_vl[wid][slot] = make_float2(vl.y, vl.z);
-                    }
-                    s_id[wid][slot] = a.j_id[j];
+                    q.vh = a.fj.vhi[j];
+                    q.vl = a.fj.vlo[j];
                 }
             }
-            fill += __popc(m);
-            __syncwarp();
+            if (with_v) q.id = a.j_id[j];
+        };
+        // Streams the walk's list through the ring: lane k takes entry t+k,
+        // entries that can lie within sqrt(rf2) of the item box are
+        // compacted into the ring, and consume(base, n) runs whenever 32 are
+        // ready (and once more for the rest).  Loads run one 32-entry chunk
+        // ahead of their use (the list index two chunks ahead) so that their
+        // latency overlaps the box test and the pair loops.  with_v also
+        // stages velocities and ids (gradient pass).
+        auto sweep = [&](const R rf2, const bool with_v, auto &&consume) {
+            int head = 0, fill = 0;
+            JRec cur, nxt;
+            int jn = 0;
+            if (lane < nj) load(jlist(lane), with_v, nxt);
+            if (32 + lane < nj) jn = jlist(32 + lane);
+            for (int t = 0; t < nj; t += 32) {
+                cur = nxt;
+                const bool valid = t + lane < nj;
+                if (t + 32 + lane < nj) load(jn, with_v, nxt);
+                if (t + 64 + lane < nj) jn = jlist(t + 64 + lane);
+                bool keep = false;
+                R4 p4;
+                if (valid) {
+                    if constexpr (F64) {
+                        p4 = Real<F64>::make4((R)cur.p.x, (R)cur.p.y, (R)cur.p.z, (R)cur.p.w);
+                    } else {
+                        p4 = Real<F64>::make4((R)df_diff(cur.ph.x, cur.pl.x, cph.x, cpl.x),
+                                              (R)df_diff(cur.ph.y, cur.pl.y, cph.y, cpl.y),
+                                              (R)df_diff(cur.ph.z, cur.pl.z, cph.z, cpl.z), (R)cur.ph.w);
+                    }
+                    keep = !(box.d2(p4.x, p4.y, p4.z) > rf2);
+                }
+                const unsigned m = __ballot_sync(FULL, keep);
+                if (keep) {
+                    const int slot = (head + fill + __popc(m & lt)) & 63;
+                    s_p[wid][slot] = p4;
+                    if (with_v) {
+                        if constexpr (F64) {
+                            s_v[wid][slot] = Real<F64>::make4((R)cur.v.x, (R)cur.v.y, (R)cur.v.z, (R)0);
+                        } else {
+                            s_v[wid][slot] = Real<F64>::make4((R)cur.vh.x, (R)cur.vh.y, (R)cur.vh.z, (R)cur.vl.x);
+                            s_vl[wid][slot] = make_float2(cur.vl.y, cur.vl.z);
+                        }
+                        s_id[wid][slot] = cur.id;
+                    }
+                }
+                fill += __popc(m);
+                __syncwarp();
+                if (fill >= 32) {
+                    consume(head, 32);
+                    head ^= 32;
+                    fill -= 32;
+                }
+            }
+            if (fill > 0) consume(head, fill);
         };
 
         // three fixed-point passes, hdr_density.hpp:264-302
@@ -210,7 +252,6 @@ density_kernel(const DensityArgs a) {
             const R rf2 = support2<R>(h);
             Acc<F64> acc;
             int cnt = 0;
-            int head = 0, fill = 0;
             R part = 0;
             // rho pair term m_j W0(q)/c0; neighbour count only in the last
             // pass (the only np the reference stores, :297)
@@ -224,7 +265,7 @@ density_kernel(const DensityArgs a) {
                 part += pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
                 if (count) cnt += (q < (R)1) ? 1 : 0;
             };
-            auto run = [&](int n) {
+            auto run = [&](int head, int n) {
                 const R4 *tile = &s_p[wid][head];
                 part = 0;
                 if (tpi == 1 && n == 32) {
@@ -241,15 +282,7 @@ density_kernel(const DensityArgs a) {
                 acc.add(part);
                 __syncwarp();
             };
-            for (int t = 0; t < nj; t += 32) {
-                stage(t, rf2, head, fill, false);
-                if (fill >= 32) {
-                    run(32);
-                    head ^= 32;
-                    fill -= 32;
-                }
-            }
-            if (fill > 0) run(fill);
+            sweep(rf2, false, run);
             const double sum = seg_sum(acc.value(), tpi);
             const long long c = seg_sum((long long)cnt, tpi);
             double hn;
@@ -283,7 +316,6 @@ density_kernel(const DensityArgs a) {
             const R hinv = (R)1 / (R)h;
             const R rf2 = support2<R>(h);
             Acc<F64> g_acc, d_acc, rx_acc, ry_acc, rz_acc;
-            int head = 0, fill = 0;
             R pg = 0, pd = 0, prx = 0, pry = 0, prz = 0;
             auto pair = [&](int k) {
                 const R4 pj = s_p[wid][k];
@@ -312,7 +344,7 @@ density_kernel(const DensityArgs a) {
                 pry += (uz * dx - ux * dz) * dw;
                 prz += (ux * dy - uy * dx) * dw;
             };
-            auto run = [&](int n) {
+            auto run = [&](int head, int n) {
                 pg = 0; pd = 0; prx = 0; pry = 0; prz = 0;
                 if (tpi == 1 && n == 32) {
 #pragma unroll 4
@@ -327,15 +359,7 @@ density_kernel(const DensityArgs a) {
                 rz_acc.add(prz);
                 __syncwarp();
             };
-            for (int t = 0; t < nj; t += 32) {
-                stage(t, rf2, head, fill, true);
-                if (fill >= 32) {
-                    run(32);
-                    head ^= 32;
-                    fill -= 32;
-                }
-            }
-            if (fill > 0) run(fill);
+            sweep(rf2, true, run);
             const double sg = seg_sum(g_acc.value(), tpi);
             const double sd = seg_sum(d_acc.value(), tpi);
             const double sx = seg_sum(rx_acc.value(), tpi);
@@ -414,7 +438,7 @@ struct HydroArgs {
 };
 
 template <bool F64, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_HYDRO_MIN_BLOCKS)
 hydro_kernel(const HydroArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
@@ -601,7 +625,7 @@ hydro_kernel(const HydroArgs a) {
                     pz = df_diff(ph.z, pl.z, cph.z, cpl.z);
                     hj_inv = vh.w;
                 }
-                const R hj = (R)1 / hj_inv;
+                const R hj = rcp_r(hj_inv);
                 const R hj2 = hj * hj * (R)1.0002;
                 const R rf2 = hj2 > hm2 ? hj2 : hm2;
                 near = !(box.d2(px, py, pz) > rf2) || !(hj2 >= (R)0);

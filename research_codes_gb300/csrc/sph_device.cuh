@@ -51,8 +51,14 @@ struct Real<true> {
 };
 
 // 1/sqrt in the working precision.  FP32 uses the hardware approximation
-// (rsqrt.approx, relative error ~2^-23); FP64 the library's double rsqrt.
-__device__ __forceinline__ float rsqrt_r(float x) { return rsqrtf(x); }
+// rsqrt.approx.ftz.f32 (relative error ~2^-23; subnormal arguments, which
+// squared distances in code units never are, flush to zero and give +inf
+// like an exact 0); FP64 the library's double rsqrt.
+__device__ __forceinline__ float rsqrt_r(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ double rsqrt_r(double x) { return rsqrt(x); }
 
 // 1/x: FP32 via rcp.approx.ftz.f32 (relative error <= 2^-23), FP64 exact.
