@@ -35,7 +35,7 @@ constexpr int MAX_RED = 8;
 // int scalars
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_BKT, S_NI = S_BKT + 2 * NBKT };
+       S_NTASKS, S_NROOTS, S_BKT, S_NI = S_BKT + 2 * NBKT };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -285,6 +285,13 @@ __global__ void accumulate_int(const int *src, int *dst) { *dst += *src; }
 __global__ void copy_int(const int *src, int *dst) { *dst = *src; }
 
 // list totals: offset[n-1] + count[n-1] (counts beyond the walk count are 0)
+// Task count of a list build (clamped to the task capacity, error bit beyond).
+__global__ void task_total(int n, const int *toff, int cap, int *scal) {
+    const int t = toff[n];
+    scal[S_NTASKS] = t < cap ? t : cap;
+    if (t > cap) atomicOr(&scal[S_ERROR], E_LISTCAP);
+}
+
 __global__ void list_total(int n, const int *cnt, const int *off, long long cap, int *scal, long long *lscal,
                            int lslot) {
     const long long tot = (long long)off[n - 1] + cnt[n - 1];
@@ -658,7 +665,7 @@ struct sph_system {
     DevBuf<int> perm[2];
     DevBuf<int2> child;
     DevBuf<int> parent, first, count, visit;
-    DevBuf<dbl4> lo, hi, mom;
+    DevBuf<dbl4> mom;
     DevBuf<double> neps2;
     DevBuf<float4> flo, fhi, fmom, ptest;
     // FP32C double-float records (particles, hydro fields, tree monopoles)
@@ -676,6 +683,12 @@ struct sph_system {
     // lists per kind: 0 density (first walk), 1 hydro, 2 gravity,
     // 3 density re-walks (search radius expanded)
     DevBuf<int> lcnt[4], loff[4], jidx[4];
+    // list traversal tasks: per group count/offset (n + 1), per task
+    // (group, start node) and list count/offset (task_cap + 1)
+    DevBuf<int> tcnt, toff, tlcnt, tloff;
+    DevBuf<int2> tasks;
+    int task_cap = 0;
+    DevBuf<int> roots;   // roots of the refit's bottom subtrees
     long long lcap[4] = {0, 0, 0, 0};
     int *walk_first[4] = {nullptr, nullptr, nullptr, nullptr};
     int *walk_count[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -714,8 +727,8 @@ struct sph_system {
     }
     sphtree::Nodes nodes() {
         sphtree::Nodes t;
-        t.child = child.p; t.parent = parent.p; t.first = first.p; t.count = count.p; t.lo = lo.p;
-        t.hi = hi.p; t.mom = mom.p; t.eps2 = neps2.p; t.visit = visit.p;
+        t.child = child.p; t.parent = parent.p; t.first = first.p; t.count = count.p;
+        t.mom = mom.p; t.eps2 = neps2.p; t.visit = visit.p;
         t.flo = flo.p; t.fhi = fhi.p; t.fmom = fmom.p; t.ptest = ptest.p;
         return t;
     }
@@ -744,7 +757,7 @@ int alloc_all(sph_system *s) {
     e |= s->np.ensure(n) | s->t_np.ensure(n) | s->t_itr.ensure(n);
     e |= s->pe.ensure(n) | s->h1.ensure(n) | s->h2.ensure(n) | s->h3.ensure(n);
     e |= s->child.ensure(n) | s->parent.ensure(nn) | s->first.ensure(nn) | s->count.ensure(nn);
-    e |= s->visit.ensure(n) | s->lo.ensure(nn) | s->hi.ensure(nn) | s->mom.ensure(nn) | s->neps2.ensure(nn);
+    e |= s->visit.ensure(n) | s->mom.ensure(nn) | s->neps2.ensure(nn);
     e |= s->flo.ensure(nn) | s->fhi.ensure(nn) | s->fmom.ensure(nn) | s->ptest.ensure(n);
     DevBuf<float4> *f1[] = {&s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo, &s->f_g1, &s->f_g2, &s->f_g3};
     for (auto *b : f1) e |= b->ensure(n);
@@ -755,7 +768,10 @@ int alloc_all(sph_system *s) {
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count};
     for (auto *b : i1) e |= b->ensure(n);
-    for (int k = 0; k < 4; ++k) e |= s->lcnt[k].ensure(n) | s->loff[k].ensure(n);
+    for (int k = 0; k < 4; ++k) e |= s->lcnt[k].ensure(n + 1) | s->loff[k].ensure(n + 1);
+    e |= s->tcnt.ensure(n + 1) | s->toff.ensure(n + 1) | s->roots.ensure(n);
+    s->task_cap = n / 16 + 4096;
+    e |= s->tasks.ensure(s->task_cap) | s->tlcnt.ensure(s->task_cap + 1) | s->tloff.ensure(s->task_cap + 1);
     e |= s->items.ensure(n);
     e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
     e |= s->partial.ensure(RED_BLOCKS * MAX_RED) | s->box.ensure(8);
@@ -765,7 +781,7 @@ int alloc_all(sph_system *s) {
     cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
     cub::DoubleBuffer<int> vb(s->perm[0].p, s->perm[1].p);
     cub::DeviceRadixSort::SortPairs(nullptr, b1, kb, vb, s->n, 0, 63);
-    cub::DeviceScan::ExclusiveSum(nullptr, b2, s->gflag.p, s->gscan.p, s->n);
+    cub::DeviceScan::ExclusiveSum(nullptr, b2, s->gflag.p, s->gscan.p, std::max(s->n, s->task_cap) + 1);
     s->cub_bytes = std::max(b1, b2);
     e |= s->cub_tmp.ensure(s->cub_bytes);
     // the first density walk covers every group, in group order
@@ -782,9 +798,9 @@ int alloc_all(sph_system *s) {
         if (e__ != cudaSuccess) return sphrt::cuda_error(s->ctx, e__, #x); \
     } while (0)
 
-int exclusive_scan(sph_system *s, const int *in, int *out) {
+int exclusive_scan(sph_system *s, const int *in, int *out, int count = -1) {
     size_t bytes = s->cub_bytes;
-    CUDA_TRY(cub::DeviceScan::ExclusiveSum(s->cub_tmp.p, bytes, in, out, s->n, s->st()));
+    CUDA_TRY(cub::DeviceScan::ExclusiveSum(s->cub_tmp.p, bytes, in, out, count < 0 ? s->n : count, s->st()));
     return SPH_OK;
 }
 
@@ -795,7 +811,21 @@ void reduce(sph_system *s, F f, double *out) {
 }
 
 // Morton sort + permutation + radix tree + refit + groups.
+// Bottom-up refit of the node data (after the tree build, and again when h
+// changed).
+int refit_tree(sph_system *s) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    sphtree::Nodes t = s->nodes();
+    CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
+    sphtree::refit_bottom<<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
+        s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
+    sphtree::refit_top<<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+    return SPH_OK;
+}
+
 int build_tree(sph_system *s) {
+    int r0 = SPH_OK;
     const int n = s->n;
     cudaStream_t st = s->st();
     cudaEventRecord(s->ev[EV_TREE_B], st);
@@ -824,14 +854,12 @@ int build_tree(sph_system *s) {
     for (auto &d : dd)
         CUDA_TRY(cudaMemcpyAsync(d[0]->p, d[1]->p, nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
     sphtree::Nodes t = s->nodes();
-    if (n >= 2) {
-        sphtree::build_radix_tree<<<grid_for(n - 1), 256, 0, st>>>(keys, n, t);
-    } else {
-        set_int<<<1, 1, 0, st>>>(t.parent, -1);
-    }
+    sphtree::build_radix_tree<<<grid_for(n), 256, 0, st>>>(keys, n, t);
+    set_int<<<1, 1, 0, st>>>(s->scal.p + S_NROOTS, 0);
+    sphtree::mark_subtrees<<<grid_for(2LL * n - 1), 256, 0, st>>>(t, n, s->roots.p, s->scal.p + S_NROOTS);
     eps2_from_h<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->eps2.p);
-    CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
-    sphtree::refit<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t);
+    r0 = refit_tree(s);
+    if (r0) return r0;
     // groups
     CUDA_TRY(cudaMemsetAsync(s->gflag.p, 0, sizeof(int) * nb, st));
     sphtree::mark_groups<<<grid_for(2LL * n - 1), 256, 0, st>>>(t, n, s->prm.n_group, s->gflag.p, s->groot.p);
@@ -841,6 +869,52 @@ int build_tree(sph_system *s) {
                                                 s->group_first.p, s->group_count.p, s->scal.p);
     cudaEventRecord(s->ev[EV_TREE_E], st);
     return SPH_OK;
+}
+
+// Grows the task buffers (eager evaluations only) and the CUB scratch that
+// scans them.
+int grow_tasks(sph_system *s, int cap) {
+    int e = s->tasks.ensure(cap) | s->tlcnt.ensure((size_t)cap + 1) | s->tloff.ensure((size_t)cap + 1);
+    if (e) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "task allocation of %d entries failed", cap);
+    s->task_cap = cap;
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, s->tlcnt.p, s->tloff.p, cap + 1);
+    if (b > s->cub_bytes) {
+        if (s->cub_tmp.ensure(b)) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "CUB scratch allocation failed");
+        s->cub_bytes = b;
+    }
+    s->graph_valid = false;
+    s->force_graph_valid = false;
+    return SPH_OK;
+}
+
+void launch_tasks(int mode, bool write, int grid, const sphtree::ListArgs &a, int *cnt, const int *off, int2 *tasks,
+                  int cap, cudaStream_t st) {
+    const int th = sphtree::TRAV_WARPS * 32;
+    if (mode == sphtree::GATHER) {
+        if (write) sphtree::list_tasks<sphtree::GATHER, true><<<grid, th, 0, st>>>(a, cnt, off, tasks, cap);
+        else sphtree::list_tasks<sphtree::GATHER, false><<<grid, th, 0, st>>>(a, cnt, off, tasks, cap);
+    } else if (mode == sphtree::SYMMETRIC) {
+        if (write) sphtree::list_tasks<sphtree::SYMMETRIC, true><<<grid, th, 0, st>>>(a, cnt, off, tasks, cap);
+        else sphtree::list_tasks<sphtree::SYMMETRIC, false><<<grid, th, 0, st>>>(a, cnt, off, tasks, cap);
+    } else {
+        if (write) sphtree::list_tasks<sphtree::GRAVITY, true><<<grid, th, 0, st>>>(a, cnt, off, tasks, cap);
+        else sphtree::list_tasks<sphtree::GRAVITY, false><<<grid, th, 0, st>>>(a, cnt, off, tasks, cap);
+    }
+}
+
+void launch_lists(int mode, bool fill, int grid, const sphtree::ListArgs &a, cudaStream_t st) {
+    const int th = sphtree::TRAV_WARPS * 32;
+    if (mode == sphtree::GATHER) {
+        if (fill) sphtree::build_lists<sphtree::GATHER, true><<<grid, th, 0, st>>>(a);
+        else sphtree::build_lists<sphtree::GATHER, false><<<grid, th, 0, st>>>(a);
+    } else if (mode == sphtree::SYMMETRIC) {
+        if (fill) sphtree::build_lists<sphtree::SYMMETRIC, true><<<grid, th, 0, st>>>(a);
+        else sphtree::build_lists<sphtree::SYMMETRIC, false><<<grid, th, 0, st>>>(a);
+    } else {
+        if (fill) sphtree::build_lists<sphtree::GRAVITY, true><<<grid, th, 0, st>>>(a);
+        else sphtree::build_lists<sphtree::GRAVITY, false><<<grid, th, 0, st>>>(a);
+    }
 }
 
 // Builds the lists of `kind` over the walks (group nodes + radii) and the
@@ -861,17 +935,36 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.r_group = walk_r;
     a.n_leaf = s->prm.n_leaf;
     a.inv_theta2 = (float)(1.0 / (s->prm.theta * s->prm.theta));
-    a.count_out = s->lcnt[kind].p;
-    a.offset = s->loff[kind].p;
     a.error = s->scal.p + S_ERROR;
     const int tgrid = s->ctx->sm_count * 8;
-    CUDA_TRY(cudaMemsetAsync(s->lcnt[kind].p, 0, sizeof(int) * (size_t)n, st));
     const int mode = (kind == 0 || kind == 3) ? sphtree::GATHER : (kind == 1 ? sphtree::SYMMETRIC : sphtree::GRAVITY);
-    if (mode == sphtree::GATHER) sphtree::build_lists<sphtree::GATHER, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
-    if (mode == sphtree::SYMMETRIC) sphtree::build_lists<sphtree::SYMMETRIC, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
-    if (mode == sphtree::GRAVITY) sphtree::build_lists<sphtree::GRAVITY, false><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
-    int r = exclusive_scan(s, s->lcnt[kind].p, s->loff[kind].p);
+    // 1. traversal tasks per group (count, scan, grow in eager mode, write)
+    CUDA_TRY(cudaMemsetAsync(s->tcnt.p, 0, sizeof(int) * (size_t)(n + 1), st));
+    launch_tasks(mode, false, tgrid, a, s->tcnt.p, s->toff.p, s->tasks.p, s->task_cap, st);
+    int r = exclusive_scan(s, s->tcnt.p, s->toff.p, n + 1);
     if (r) return r;
+    if (eager) {
+        int nt = 0;
+        CUDA_TRY(cudaMemcpyAsync(&nt, s->toff.p + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (nt > s->task_cap) {
+            r = grow_tasks(s, nt + nt / 2 + 1024);
+            if (r) return r;
+        }
+    }
+    task_total<<<1, 1, 0, st>>>(n, s->toff.p, s->task_cap, s->scal.p);
+    launch_tasks(mode, true, tgrid, a, s->tcnt.p, s->toff.p, s->tasks.p, s->task_cap, st);
+    // 2. list lengths per task, offsets per task and per group
+    a.tasks = s->tasks.p;
+    a.n_tasks = s->scal.p + S_NTASKS;
+    a.count_out = s->tlcnt.p;
+    a.offset = s->tloff.p;
+    CUDA_TRY(cudaMemsetAsync(s->tlcnt.p, 0, sizeof(int) * (size_t)(s->task_cap + 1), st));
+    launch_lists(mode, false, tgrid, a, st);
+    r = exclusive_scan(s, s->tlcnt.p, s->tloff.p, s->task_cap + 1);
+    if (r) return r;
+    sphtree::group_lists<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], s->toff.p, s->tloff.p,
+                                                         s->task_cap, s->loff[kind].p, s->lcnt[kind].p);
     const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : (kind == 2 ? L_LIST_G : L_LIST_R));
     if (eager) {
         list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, (long long)1 << 62, s->scal.p, s->lscal.p, lslot);
@@ -884,15 +977,16 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
             if (s->jidx[kind].ensure((size_t)want))
                 return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list allocation of %lld entries failed", tot);
             s->lcap[kind] = (long long)s->jidx[kind].cap;
+            // both captured graphs hold the old buffer
             s->graph_valid = false;
+            s->force_graph_valid = false;
         }
     }
     list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, s->lcap[kind], s->scal.p, s->lscal.p, lslot);
+    // 3. fill
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
-    if (mode == sphtree::GATHER) sphtree::build_lists<sphtree::GATHER, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
-    if (mode == sphtree::SYMMETRIC) sphtree::build_lists<sphtree::SYMMETRIC, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
-    if (mode == sphtree::GRAVITY) sphtree::build_lists<sphtree::GRAVITY, true><<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    launch_lists(mode, true, tgrid, a, st);
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
     const int *icount = item_count ? item_count : s->walk_count[kind];
@@ -1080,9 +1174,8 @@ int force_body(sph_system *s, bool eager) {
     if (r) return r;
     post_density<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->dens.p, s->uene[0].p, s->divv.p, s->rotv.p,
                                               s->ksr[0].p, s->pres.p, s->vsnd.p, s->bswt.p, s->eps2.p, s->pe.p);
-    sphtree::Nodes t = s->nodes();
-    CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
-    sphtree::refit<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t);
+    r = refit_tree(s);   // h (max h, softening) changed in the density phase
+    if (r) return r;
     r = gravity_phase(s, eager);
     if (r) return r;
     r = hydro_phase(s, eager);
@@ -1214,7 +1307,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
     for (auto *b : d1) b->release();
     s->np.release(); s->t_np.release(); s->t_itr.release(); s->pe.release(); s->h1.release();
     s->h2.release(); s->h3.release(); s->child.release(); s->parent.release(); s->first.release();
-    s->count.release(); s->visit.release(); s->lo.release(); s->hi.release(); s->mom.release();
+    s->count.release(); s->visit.release(); s->mom.release();
     DevBuf<float4> *f1[] = {&s->flo, &s->fhi, &s->fmom, &s->ptest, &s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo,
                             &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
     for (auto *b : f1) b->release();
@@ -1226,6 +1319,10 @@ extern "C" int sph_system_destroy(sph_system *s) {
     for (auto *b : i1) b->release();
     for (int k = 0; k < 4; ++k) {
         s->lcnt[k].release(); s->loff[k].release(); s->jidx[k].release();
+        if (k == 0) {
+            s->tcnt.release(); s->toff.release(); s->tlcnt.release(); s->tloff.release(); s->tasks.release();
+            s->roots.release();
+        }
     }
     s->items.release(); s->lscal.release(); s->cub_tmp.release();
     s->h_scal.release(); s->h_dscal.release(); s->h_lscal.release();

@@ -7,13 +7,16 @@
 //      CUB radix sort; particles permuted into key order.
 //   2. Binary radix tree over the sorted keys (Karras 2012): internal nodes
 //      0..n-2, leaf node n-1+p for particle p; one thread per internal node.
-//   3. Bottom-up refit (one thread per leaf, second arrival combines): FP64
-//      bounding box, particle range, max h, monopole (mass, centre of mass,
-//      mass-weighted eps^2 as GravityMonopole, hdr_gravity.hpp:37-49).
+//   3. Bottom-up refit (second arrival at a node combines its children):
+//      FP32 outward-rounded bounding box, max h, monopole in FP64 (mass,
+//      centre of mass, mass-weighted eps^2 as GravityMonopole,
+//      hdr_gravity.hpp:37-49).  Particle ranges come from the tree build.
 //   4. i-groups ("walks"): maximal subtrees with <= n_group particles.
-//   5. Lists, one warp per group, warp-cooperative batched-DFS traversal with a
-//      shared-memory stack; two passes (count, then fill at scanned offsets)
-//      so list order is deterministic:
+//   5. Lists: each group's region is first expanded breadth-first into
+//      traversal tasks (subtrees), then one warp per task runs a
+//      warp-cooperative batched-DFS traversal with a shared-memory stack;
+//      two passes (count, then fill at scanned offsets) so list order is
+//      deterministic:
 //        gather    : j with dist(x_j, box_g) <= max_{i in g, unconverged} rs_i
 //        symmetric : j with dist(x_j, box_g) <= max(max_{i in g} h_i, h_j)
 //        gravity   : node accepted as a monopole when
@@ -39,8 +42,6 @@ struct Nodes {
     int *parent;
     int *first;       // first particle (sorted index)
     int *count;
-    dbl4 *lo;         // bbox min; w = max h in the subtree
-    dbl4 *hi;         // bbox max; w = unused
     dbl4 *mom;        // centre of mass x, y, z; w = mass
     double *eps2;     // mass-weighted eps^2
     int *visit;       // refit arrival counters
@@ -85,9 +86,7 @@ __device__ __forceinline__ int prefix_len(const uint64_t *k, int n, int i, int j
     return __clzll(a ^ b);
 }
 
-__global__ void build_radix_tree(const uint64_t *k, int n, Nodes t) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n - 1) return;
+__device__ __forceinline__ void radix_node(const uint64_t *k, int n, Nodes t, int i) {
     const int d = (prefix_len(k, n, i, i + 1) - prefix_len(k, n, i, i - 1)) >= 0 ? 1 : -1;
     const int dmin = prefix_len(k, n, i, i - d);
     int lmax = 2;
@@ -107,95 +106,190 @@ __global__ void build_radix_tree(const uint64_t *k, int n, Nodes t) {
     const int left = (min(i, j) == gamma) ? (n - 1 + gamma) : gamma;
     const int right = (max(i, j) == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
     t.child[i] = make_int2(left, right);
+    t.first[i] = min(i, j);
+    t.count[i] = abs(j - i) + 1;
     t.parent[left] = i;
     t.parent[right] = i;
     if (i == 0) t.parent[0] = -1;
 }
 
-// ---- 3. refit ----------------------------------------------------------------
-// L1-bypassing load: another thread (another SM) wrote the child nodes.
-__device__ __forceinline__ dbl4 ldcg4(const dbl4 *p) {
-    const double2 *q = reinterpret_cast<const double2 *>(p);
-    const double2 a = __ldcg(q), b = __ldcg(q + 1);
-    return make_dbl4(a.x, a.y, b.x, b.y);
+// Internal node i covers the particle range between i and j (Karras's
+// determineRange); its first particle and count are written here, the
+// leaves' trivially.
+__global__ void build_radix_tree(const uint64_t *k, int n, Nodes t) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        t.first[n - 1 + p] = p;
+        t.count[n - 1 + p] = 1;
+        if (n == 1) t.parent[0] = -1;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x)
+        radix_node(k, n, t, i);
 }
 
-// FP32 copies of the node geometry for the traversal: boxes rounded outwards,
-// h_max and size rounded up, so that FP32 tests are conservative.
-__device__ __forceinline__ void write_fgeom(const Nodes &t, int node, const dbl4 &lo, const dbl4 &hi,
-                                            const dbl4 &m) {
-    const double size = fmax(fmax(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
-    t.flo[node] = make_float4(__double2float_rd(lo.x), __double2float_rd(lo.y), __double2float_rd(lo.z),
-                              __double2float_ru(lo.w));
-    t.fhi[node] = make_float4(__double2float_ru(hi.x), __double2float_ru(hi.y), __double2float_ru(hi.z),
-                              __double2float_ru(size));
+// ---- 3. refit ----------------------------------------------------------------
+// Refit data of a node.  The traversal uses FP32 boxes rounded outwards
+// (flo.w = max h rounded up; fhi.w = largest box side, filled at store
+// time), so the boxes are merged in FP32 (min/max of conservative boxes stays
+// conservative) and no FP64 box is kept.  The monopole is accumulated in FP64
+// as unnormalised sums: sm = (sum m x, sum m y, sum m z, sum m), se = sum m eps^2.
+struct NodeData {
+    dbl4 sm;
+    float4 flo, fhi;
+    double se;
+};
+
+__device__ __forceinline__ NodeData combine(const NodeData &a, const NodeData &b) {
+    NodeData r;
+    r.sm = make_dbl4(a.sm.x + b.sm.x, a.sm.y + b.sm.y, a.sm.z + b.sm.z, a.sm.w + b.sm.w);
+    r.se = a.se + b.se;
+    r.flo = make_float4(fminf(a.flo.x, b.flo.x), fminf(a.flo.y, b.flo.y), fminf(a.flo.z, b.flo.z),
+                        fmaxf(a.flo.w, b.flo.w));
+    r.fhi = make_float4(fmaxf(a.fhi.x, b.fhi.x), fmaxf(a.fhi.y, b.fhi.y), fmaxf(a.fhi.z, b.fhi.z), 0.0f);
+    return r;
+}
+
+__device__ __forceinline__ NodeData leaf_data(const dbl4 &x, double h, double eps2) {
+    NodeData d;
+    d.sm = make_dbl4(x.w * x.x, x.w * x.y, x.w * x.z, x.w);
+    d.se = x.w * eps2;
+    d.flo = make_float4(__double2float_rd(x.x), __double2float_rd(x.y), __double2float_rd(x.z),
+                        __double2float_ru(h));
+    d.fhi = make_float4(__double2float_ru(x.x), __double2float_ru(x.y), __double2float_ru(x.z), 0.0f);
+    return d;
+}
+
+// Writes a node: FP32 boxes with the side length (rounded up), the monopole
+// (centre of mass, mass; mass-weighted eps^2) in FP64 and its FP32 copy.
+__device__ __forceinline__ void store_node(const Nodes &t, int node, const NodeData &d) {
+    const float size = fmaxf(fmaxf(__fsub_ru(d.fhi.x, d.flo.x), __fsub_ru(d.fhi.y, d.flo.y)),
+                             __fsub_ru(d.fhi.z, d.flo.z));
+    t.flo[node] = d.flo;
+    t.fhi[node] = make_float4(d.fhi.x, d.fhi.y, d.fhi.z, size);
+    dbl4 m;
+    double e2;
+    if (d.sm.w > 0.0) {
+        const double mi = 1.0 / d.sm.w;
+        m = make_dbl4(d.sm.x * mi, d.sm.y * mi, d.sm.z * mi, d.sm.w);
+        e2 = d.se * mi;
+    } else {
+        m = make_dbl4(0.5 * ((double)d.flo.x + d.fhi.x), 0.5 * ((double)d.flo.y + d.fhi.y),
+                      0.5 * ((double)d.flo.z + d.fhi.z), 0.0);
+        e2 = 0.0;
+    }
+    t.mom[node] = m;
+    t.eps2[node] = e2;
     t.fmom[node] = make_float4((float)m.x, (float)m.y, (float)m.z, (float)m.w);
 }
 
-__global__ void refit(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes t) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int node = n - 1 + p;
-    const dbl4 x = pos[p];
-    t.first[node] = p;
-    t.count[node] = 1;
-    const dbl4 l0 = make_dbl4(x.x, x.y, x.z, h[p]);
-    const dbl4 h0 = make_dbl4(x.x, x.y, x.z, 0.0);
-    const dbl4 m0 = make_dbl4(x.x, x.y, x.z, x.w);
-    t.lo[node] = l0;
-    t.hi[node] = h0;
-    t.mom[node] = m0;
-    t.eps2[node] = eps2[p];
-    write_fgeom(t, node, l0, h0, m0);
-    t.ptest[p] = make_float4((float)x.x, (float)x.y, (float)x.z, __double2float_ru(h[p]));
-    if (n == 1) return;
-    node = t.parent[node];
-    while (node >= 0) {
-        __threadfence();
-        if (atomicAdd(&t.visit[node], 1) == 0) return;   // sibling not finished yet
-        __threadfence();
-        const int2 c = t.child[node];
-        const dbl4 la = ldcg4(&t.lo[c.x]), lb = ldcg4(&t.lo[c.y]);
-        const dbl4 ha = ldcg4(&t.hi[c.x]), hb = ldcg4(&t.hi[c.y]);
-        const dbl4 ma = ldcg4(&t.mom[c.x]), mb = ldcg4(&t.mom[c.y]);
-        const double ea = __ldcg(&t.eps2[c.x]), eb = __ldcg(&t.eps2[c.y]);
-        const int ca = __ldcg(&t.count[c.x]), cb = __ldcg(&t.count[c.y]);
-        const int fa = __ldcg(&t.first[c.x]);
-        t.first[node] = fa;
-        t.count[node] = ca + cb;
-        const dbl4 lo = make_dbl4(fmin(la.x, lb.x), fmin(la.y, lb.y), fmin(la.z, lb.z), fmax(la.w, lb.w));
-        const dbl4 hi = make_dbl4(fmax(ha.x, hb.x), fmax(ha.y, hb.y), fmax(ha.z, hb.z), 0.0);
-        t.lo[node] = lo;
-        t.hi[node] = hi;
-        const double m = ma.w + mb.w;
-        dbl4 mom;
-        if (m > 0.0) {
-            const double mi = 1.0 / m;
-            mom = make_dbl4((ma.w * ma.x + mb.w * mb.x) * mi, (ma.w * ma.y + mb.w * mb.y) * mi,
-                            (ma.w * ma.z + mb.w * mb.z) * mi, m);
-            t.eps2[node] = (ma.w * ea + mb.w * eb) * mi;
-        } else {
-            mom = make_dbl4(0.5 * (lo.x + hi.x), 0.5 * (lo.y + hi.y), 0.5 * (lo.z + hi.z), 0.0);
-            t.eps2[node] = 0.5 * (ea + eb);
+// A node written by another SM, back as refit data (L1 bypassed).
+__device__ __forceinline__ NodeData load_node_cg(const Nodes &t, int node) {
+    NodeData d;
+    const double2 *q = reinterpret_cast<const double2 *>(&t.mom[node]);
+    const double2 a = __ldcg(q), b = __ldcg(q + 1);
+    d.sm = make_dbl4(b.y * a.x, b.y * a.y, b.y * b.x, b.y);
+    d.se = b.y * __ldcg(&t.eps2[node]);
+    d.flo = __ldcg(&t.flo[node]);
+    d.fhi = __ldcg(&t.fhi[node]);
+    return d;
+}
+
+// The refit runs in two parts.  Bottom: every maximal subtree of at most
+// REFIT_B particles is refitted by one block in shared memory (one thread per
+// leaf climbing while it is the second arrival at a node, block-scope
+// counters).  Top: one thread per such subtree climbs the few nodes above
+// them with device-scope arrival counters.  Threads therefore never hold a
+// warp for a climb through the whole tree.
+constexpr int REFIT_B = 128;
+
+// Roots of the bottom subtrees: count <= REFIT_B, parent's count > REFIT_B.
+__global__ void mark_subtrees(Nodes t, int n, int *roots, int *n_roots) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < 2 * n - 1; v += gridDim.x * blockDim.x) {
+        const int p = t.parent[v];
+        if (t.count[v] <= REFIT_B && (p < 0 || t.count[p] > REFIT_B)) roots[atomicAdd(n_roots, 1)] = v;
+    }
+}
+
+__global__ void __launch_bounds__(REFIT_B)
+refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes t, const int *roots,
+             const int *n_roots) {
+    // slots 0..B-1: internal node (index - first), B..2B-1: leaf (particle - first)
+    __shared__ NodeData sd[2 * REFIT_B];
+    __shared__ int visit[REFIT_B];
+    const int nr = *n_roots;
+    for (int r = blockIdx.x; r < nr; r += gridDim.x) {
+        const int root = roots[r];
+        const int a = t.first[root];
+        const int c = t.count[root];
+        if (c < 1 || c > REFIT_B) continue;   // not a bottom subtree (block-uniform)
+        visit[threadIdx.x] = 0;
+        __syncthreads();
+        if ((int)threadIdx.x < c) {
+            const int p = a + threadIdx.x;
+            const dbl4 x = pos[p];
+            const double hp = h[p], ep = eps2[p];
+            NodeData d = leaf_data(x, hp, ep);
+            int node = n - 1 + p;
+            // leaf: exact position, mass and eps^2
+            t.flo[node] = d.flo;
+            t.fhi[node] = make_float4(d.fhi.x, d.fhi.y, d.fhi.z,
+                                      fmaxf(fmaxf(__fsub_ru(d.fhi.x, d.flo.x), __fsub_ru(d.fhi.y, d.flo.y)),
+                                            __fsub_ru(d.fhi.z, d.flo.z)));
+            t.mom[node] = x;
+            t.eps2[node] = ep;
+            t.fmom[node] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)x.w);
+            t.ptest[p] = make_float4((float)x.x, (float)x.y, (float)x.z, __double2float_ru(hp));
+            sd[REFIT_B + threadIdx.x] = d;
+            while (node != root) {
+                node = t.parent[node];
+                // internal nodes of the subtree have indices in [a, a + c)
+                if (node < a || node >= a + c) break;
+                __threadfence_block();
+                if (atomicAdd(&visit[node - a], 1) == 0) break;   // sibling not finished yet
+                __threadfence_block();
+                const int2 ch = t.child[node];
+                const int sa = (ch.x >= n - 1) ? REFIT_B + (ch.x - (n - 1) - a) : ch.x - a;
+                const int sb = (ch.y >= n - 1) ? REFIT_B + (ch.y - (n - 1) - a) : ch.y - a;
+                if (sa < 0 || sa >= 2 * REFIT_B || sb < 0 || sb >= 2 * REFIT_B) break;
+                d = combine(sd[sa], sd[sb]);
+                sd[node - a] = d;
+                store_node(t, node, d);
+            }
         }
-        t.mom[node] = mom;
-        write_fgeom(t, node, lo, hi, mom);
-        node = t.parent[node];
+        __syncthreads();
+    }
+}
+
+// visit[] (internal nodes) is zero on entry.
+__global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots) {
+    const int nr = *n_roots;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+        int node = t.parent[roots[r]];
+        while (node >= 0) {
+            // acq_rel arrival: the first arriver's node writes are released by
+            // its atomic, the second arriver acquires them with its own
+            int arrived;
+            asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;"
+                         : "=r"(arrived) : "l"(&t.visit[node]) : "memory");
+            if (arrived == 0) break;   // sibling not finished yet
+            const int2 ch = t.child[node];
+            store_node(t, node, combine(load_node_cg(t, ch.x), load_node_cg(t, ch.y)));
+            node = t.parent[node];
+        }
     }
 }
 
 // ---- 4. groups -------------------------------------------------------------
 // flag[first particle of a group root] = 1, root_at[first] = node.
 __global__ void mark_groups(Nodes t, int n, int n_group, int *flag, int *root_at) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= 2 * n - 1) return;
-    const int c = t.count[v];
-    const int p = t.parent[v];
-    const int pc = (p >= 0) ? t.count[p] : 0x7fffffff;
-    if (c <= n_group && pc > n_group) {
-        const int f = t.first[v];
-        flag[f] = 1;
-        root_at[f] = v;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < 2 * n - 1; v += gridDim.x * blockDim.x) {
+        const int c = t.count[v];
+        const int p = t.parent[v];
+        const int pc = (p >= 0) ? t.count[p] : 0x7fffffff;
+        if (c <= n_group && pc > n_group) {
+            const int f = t.first[v];
+            flag[f] = 1;
+            root_at[f] = v;
+        }
     }
 }
 
@@ -215,9 +309,12 @@ struct ListArgs {
     const double *r_group;  // gather: search radius of the group
     int n_leaf;             // <= MAX_LEAF
     float inv_theta2;
-    // pass 1 writes counts, pass 2 fills at offsets
+    // traversal tasks: (group, start node); see list_tasks
+    const int2 *tasks;
+    const int *n_tasks;     // device count of tasks
+    // pass 1 writes counts per task, pass 2 fills at offsets
     int *count_out;
-    const int *offset;      // exclusive scan of counts (fill pass)
+    const int *offset;      // exclusive scan of the task counts (fill pass)
     int *j_idx;
     long long capacity;     // entries available in j_idx
     int *error;             // bit 1: stack overflow, bit 2: capacity exceeded
@@ -242,6 +339,157 @@ __device__ __forceinline__ float point_box_d2f(float x, float y, float z, const 
 // plus an absolute term covering the rounding of coordinates to FP32.
 __device__ __forceinline__ float widen(float r, float slack) { return r * 1.000002f + slack; }
 
+// Region of group g for the node and particle tests: box (FP32, outward
+// rounded) and radius.
+__device__ __forceinline__ float group_radius(const ListArgs &a, int mode, int g, const float4 &glo) {
+    if (mode == GATHER) return __double2float_ru(a.r_group[g]);
+    if (mode == SYMMETRIC) return glo.w;   // max h of the group (rounded up)
+    return 0.0f;
+}
+
+// Node test of the traversal: 0 = reject, 1 = bucket (test its particles),
+// 2 = open (descend), 3 = accept as a monopole (gravity).
+template <int MODE>
+__device__ __forceinline__ int node_class(const ListArgs &a, int node, const float4 &glo, const float4 &ghi,
+                                          float rg, float slack) {
+    const float4 lo = a.t.flo[node];
+    const float4 hi = a.t.fhi[node];
+    const bool leafish = (node >= a.n - 1) || a.t.count[node] <= a.n_leaf;
+    if (MODE == GRAVITY) {
+        const float4 m = a.t.fmom[node];
+        const float d2 = point_box_d2f(m.x, m.y, m.z, glo, ghi);
+        if (d2 > hi.w * hi.w * a.inv_theta2) return 3;
+        return leafish ? 1 : 2;
+    }
+    const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, lo.w) : rg, slack);
+    if (box_box_d2f(glo, ghi, lo, hi) > r * r) return 0;
+    return leafish ? 1 : 2;
+}
+
+__device__ __forceinline__ float coord_slack(const double *box) {
+    // coordinates were rounded to FP32: |error| <= 2^-24 max|x| per axis
+    const double cmax = fmax(fmax(fmax(fabs(box[0]), fabs(box[3])), fmax(fabs(box[1]), fabs(box[4]))),
+                             fmax(fabs(box[2]), fabs(box[5])));
+    return (float)(4.0e-7 * cmax);
+}
+
+// Traversal tasks.  One warp per group expands the nodes its region reaches
+// breadth-first, opening only nodes of more than TASK_SPLIT particles, up to
+// TASK_CAP nodes; each remaining node becomes a task (group, start node) that
+// one warp traverses depth-first.  A group whose region covers many
+// particles is thereby spread over many warps instead of one long traversal,
+// and the order of its list (tasks in frontier order, each in depth-first
+// order) stays deterministic.  WRITE = false counts tasks per group,
+// WRITE = true writes them at the scanned offsets.
+constexpr int TASK_CAP = 64;
+constexpr int TASK_SPLIT = 2048;
+
+template <int MODE, bool WRITE>
+__global__ void __launch_bounds__(TRAV_WARPS * 32)
+list_tasks(ListArgs a, int *task_count, const int *task_off, int2 *tasks, int task_cap) {
+    __shared__ int fr[TRAV_WARPS][2][TASK_CAP];
+    const int lane = threadIdx.x & 31;
+    const int wid = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int n_groups = *a.n_groups;
+    const int warps = gridDim.x * TRAV_WARPS;
+    const float slack = coord_slack(a.box);
+    for (int g = blockIdx.x * TRAV_WARPS + wid; g < n_groups; g += warps) {
+        const int gn = a.group_node[g];
+        const float4 glo = a.t.flo[gn];
+        const float4 ghi = a.t.fhi[gn];
+        const float rg = group_radius(a, MODE, g, glo);
+        int cur = 0, nf = 1;
+        if (lane == 0) fr[wid][0][0] = a.root;
+        __syncwarp();
+        for (;;) {
+            // classify the frontier (two nodes per lane)
+            int nd[2], cls[2], split[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int k = lane + 32 * u;
+                nd[u] = (k < nf) ? fr[wid][cur][k] : -1;
+                cls[u] = 0;
+                split[u] = 0;
+                if (nd[u] >= 0) {
+                    cls[u] = node_class<MODE>(a, nd[u], glo, ghi, rg, slack);
+                    // gravity lists are of uniform length: one task per group
+                    split[u] = (MODE != GRAVITY && cls[u] == 2 && a.t.count[nd[u]] > TASK_SPLIT) ? 1 : 0;
+                }
+            }
+            // size of the next frontier: split nodes give two, kept nodes one
+            int w0 = (cls[0] == 0) ? 0 : 1 + split[0];
+            int w1 = (cls[1] == 0) ? 0 : 1 + split[1];
+            int inc = w0 + w1;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, inc, o);
+                if (lane >= o) inc += v;
+            }
+            const int next = __shfl_sync(FULL, inc, 31);
+            const bool any_split = __any_sync(FULL, split[0] | split[1]);
+            const bool expand = any_split && next <= TASK_CAP;
+            if (!expand) {
+                // final frontier: the nodes not rejected, in order
+                const unsigned m0 = __ballot_sync(FULL, cls[0] != 0);
+                const unsigned m1 = __ballot_sync(FULL, cls[1] != 0);
+                const int c0 = __popc(m0);
+                if (WRITE) {
+                    const long long base = task_off[g];
+                    if (cls[0] != 0) {
+                        const long long w = base + __popc(m0 & lt_mask);
+                        if (w < task_cap) tasks[w] = make_int2(g, nd[0]);
+                        else atomicOr(a.error, 2);
+                    }
+                    if (cls[1] != 0) {
+                        const long long w = base + c0 + __popc(m1 & lt_mask);
+                        if (w < task_cap) tasks[w] = make_int2(g, nd[1]);
+                        else atomicOr(a.error, 2);
+                    }
+                } else if (lane == 0) {
+                    task_count[g] = c0 + __popc(m1);
+                }
+                break;
+            }
+            const int nxt = cur ^ 1;
+            int pos = inc - w0 - w1;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (cls[u] != 0) {
+                    if (split[u]) {
+                        const int2 c = a.t.child[nd[u]];
+                        fr[wid][nxt][pos] = c.x;
+                        fr[wid][nxt][pos + 1] = c.y;
+                        pos += 2;
+                    } else {
+                        fr[wid][nxt][pos] = nd[u];
+                        pos += 1;
+                    }
+                }
+            }
+            cur = nxt;
+            nf = next;
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+}
+
+// Groups' list offsets and lengths from their tasks' (each group's tasks are
+// consecutive): off[g] = task_loff[task_off[g]], cnt[g] = its entries.
+// Entries g in [n_groups, n] get the total and 0.
+// Task offsets beyond the task capacity (an overflow already flagged as an
+// error) are clamped to it.
+__global__ void group_lists(int n, const int *n_groups, const int *task_off, const int *task_loff, int task_cap,
+                            int *off, int *cnt) {
+    const int ng = *n_groups;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= n; g += gridDim.x * blockDim.x) {
+        const int gg = g < ng ? g : ng;
+        const int o = task_loff[min(task_off[gg], task_cap)];
+        off[g] = o;
+        cnt[g] = (g < ng) ? task_loff[min(task_off[g + 1], task_cap)] - o : 0;
+    }
+}
+
 template <int MODE, bool FILL>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
     __shared__ int stack[TRAV_WARPS][STACK];
@@ -251,23 +499,20 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const int n_groups = *a.n_groups;
+    const int n_tasks = *a.n_tasks;
     const int warps = gridDim.x * TRAV_WARPS;
-    // coordinates were rounded to FP32: |error| <= 2^-24 max|x| per axis
-    const double cmax = fmax(fmax(fmax(fabs(a.box[0]), fabs(a.box[3])), fmax(fabs(a.box[1]), fabs(a.box[4]))),
-                             fmax(fabs(a.box[2]), fabs(a.box[5])));
-    const float slack = (float)(4.0e-7 * cmax);
-    for (int g = blockIdx.x * TRAV_WARPS + wid; g < n_groups; g += warps) {
+    const float slack = coord_slack(a.box);
+    for (int task = blockIdx.x * TRAV_WARPS + wid; task < n_tasks; task += warps) {
+        const int2 tk = a.tasks[task];
+        const int g = tk.x;
         const int gn = a.group_node[g];
         const float4 glo = a.t.flo[gn];
         const float4 ghi = a.t.fhi[gn];
-        float rg = 0.0f;
-        if (MODE == GATHER) rg = __double2float_ru(a.r_group[g]);
-        if (MODE == SYMMETRIC) rg = glo.w;          // max h of the group (rounded up)
-        long long out = FILL ? (long long)a.offset[g] : 0;
+        const float rg = group_radius(a, MODE, g, glo);
+        long long out = FILL ? (long long)a.offset[task] : 0;
         int total = 0;
         int sp = 1, nc = 0;
-        if (lane == 0) stack[wid][0] = a.root;
+        if (lane == 0) stack[wid][0] = tk.y;
         __syncwarp();
         bool overflow = false;
         while (sp > 0 || nc > 0) {
@@ -279,22 +524,10 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
                 bool push = false, bucket = false, accept = false;
                 int2 ch = make_int2(0, 0);
                 if (node >= 0) {
-                    const float4 lo = a.t.flo[node];
-                    const float4 hi = a.t.fhi[node];
-                    const bool leafish = (node >= a.n - 1) || a.t.count[node] <= a.n_leaf;
-                    if (MODE == GRAVITY) {
-                        const float4 m = a.t.fmom[node];
-                        const float d2 = point_box_d2f(m.x, m.y, m.z, glo, ghi);
-                        if (d2 > hi.w * hi.w * a.inv_theta2) accept = true;
-                        else if (leafish) bucket = true;
-                        else push = true;
-                    } else {
-                        const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, lo.w) : rg, slack);
-                        if (box_box_d2f(glo, ghi, lo, hi) <= r * r) {
-                            if (leafish) bucket = true;
-                            else push = true;
-                        }
-                    }
+                    const int c = node_class<MODE>(a, node, glo, ghi, rg, slack);
+                    accept = c == 3;
+                    bucket = c == 1;
+                    push = c == 2;
                     if (push) ch = a.t.child[node];
                 }
                 // children of opened nodes
@@ -352,22 +585,37 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
                     for (int k = 0; k < c1; ++k) pidx[wid][base1 + k] = f + k;
                 }
                 __syncwarp();
-                for (int b = 0; b < tot; b += 32) {
-                    const int p = (b + lane < tot) ? pidx[wid][b + lane] : -1;
-                    bool ok = p >= 0;
-                    if (ok && MODE != GRAVITY) {
-                        const float4 x = a.t.ptest[p];
-                        const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, x.w) : rg, slack);
-                        ok = point_box_d2f(x.x, x.y, x.z, glo, ghi) <= r * r;
+                // four 32-particle batches per round: their loads are issued
+                // together, the accepted particles keep the batch order
+                for (int b = 0; b < tot; b += 128) {
+                    int p[4];
+                    float4 x[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int k = b + 32 * u + lane;
+                        p[u] = (k < tot) ? pidx[wid][k] : -1;
                     }
-                    const unsigned om = __ballot_sync(FULL, ok);
-                    if (FILL && ok) {
-                        const long long w = out + __popc(om & lt_mask);
-                        if (w < a.capacity) a.j_idx[w] = p;
-                        else atomicOr(a.error, 2);
+                    if (MODE != GRAVITY) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            if (p[u] >= 0) x[u] = a.t.ptest[p[u]];
                     }
-                    out += __popc(om);
-                    total += __popc(om);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        bool ok = p[u] >= 0;
+                        if (ok && MODE != GRAVITY) {
+                            const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, x[u].w) : rg, slack);
+                            ok = point_box_d2f(x[u].x, x[u].y, x[u].z, glo, ghi) <= r * r;
+                        }
+                        const unsigned om = __ballot_sync(FULL, ok);
+                        if (FILL && ok) {
+                            const long long w = out + __popc(om & lt_mask);
+                            if (w < a.capacity) a.j_idx[w] = p[u];
+                            else atomicOr(a.error, 2);
+                        }
+                        out += __popc(om);
+                        total += __popc(om);
+                    }
                 }
                 nc = 0;
                 __syncwarp();
@@ -375,7 +623,7 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
             if (overflow) break;
         }
         if (overflow && lane == 0) atomicOr(a.error, 1);
-        if (!FILL && lane == 0) a.count_out[g] = total;
+        if (!FILL && lane == 0) a.count_out[task] = total;
     }
 }
 
