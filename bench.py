@@ -35,6 +35,9 @@ sys.path.insert(0, ROOT)
 # = 1, fma = 2, rsqrt/sqrt/rcp = 1): density 132 (3 x 23 + 63, four passes),
 # hydro 109, gravity 29.
 FLOP_PER_PAIR = {"density": 132.0, "hydro": 109.0, "gravity": 29.0}
+# per evaluated pair: one density pass, the gradient pass, a hydro pair beyond
+# both supports (signal-velocity terms only, hdr_hydro.hpp:348-372)
+FLOP_DENS_PASS, FLOP_DENS_GRAD, FLOP_HYDRO_FAR = 23.0, 63.0, 20.0
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
 
 
@@ -233,6 +236,23 @@ def run_ours(args):
     pairs_k = {"density": st_k["pairs_density_first"], "hydro": st_k["pairs_hydro"],
                "gravity": st_k["pairs_gravity"]}
     achieved = (pairs_k[dom] * FLOP_PER_PAIR[dom] / (kern[dom] * 1e-3) / 1e12) if pairs_k[dom] else None
+    # work the kernels actually evaluated: the density and hydro kernels drop
+    # list entries beyond every i-particle's kernel support before their pair
+    # loops (those pairs contribute exactly zero); gravity evaluates all
+    useful_d = float(ps.download("np").sum())
+    flop_eval = {"density": st_k["evals_density_first"] * FLOP_DENS_PASS + st_k["evals_density_grad"] * FLOP_DENS_GRAD,
+                 "hydro": st_k["evals_hydro_near"] * FLOP_PER_PAIR["hydro"] + st_k["evals_hydro_far"] * FLOP_HYDRO_FAR,
+                 "gravity": pairs_k["gravity"] * FLOP_PER_PAIR["gravity"]}
+    per_kernel = {}
+    for k in kern:
+        per_kernel[k] = {"ms": round(kern[k], 4), "pairs_listed": int(pairs_k[k]),
+                         "achieved_listed_tflops": pairs_k[k] * FLOP_PER_PAIR[k] / (kern[k] * 1e-3) / 1e12,
+                         "achieved_evaluated_tflops": flop_eval[k] / (kern[k] * 1e-3) / 1e12}
+    per_kernel["density"]["pair_evaluations"] = {"three_passes": int(st_k["evals_density_first"]),
+                                                 "gradient_pass": int(st_k["evals_density_grad"]),
+                                                 "useful_per_pass": int(useful_d)}
+    per_kernel["hydro"]["pair_evaluations"] = {"full": int(st_k["evals_hydro_near"]),
+                                               "signal_velocity_only": int(st_k["evals_hydro_far"])}
     traffic = None
     if os.path.exists(PROFILE_TRAFFIC):
         tr = json.load(open(PROFILE_TRAFFIC))
@@ -254,7 +274,12 @@ def run_ours(args):
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
                          "traffic": traffic,
                          "peak_source": "FP32 FMA probe on this GPU (sph_probe_fp32_peak); "
-                                        "MEASURED_PEAKS.json holds no FP32 figure"},
+                                        "MEASURED_PEAKS.json holds no FP32 figure",
+                         "work": "achieved = listed pairs (sum n_i*n_j over the walk lists) x flop/pair "
+                                 "(132 density, 109 hydro, 29 gravity) / kernel time; the kernels skip "
+                                 "pairs beyond the kernel support, per_kernel gives the evaluated work",
+                         "frac_evaluated": per_kernel[dom]["achieved_evaluated_tflops"] / peak,
+                         "per_kernel": per_kernel},
             "gpu_launches": None, "clocks": clk}
 
     # kernel launches in the timed region: the kernel nodes of the captured

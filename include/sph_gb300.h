@@ -360,6 +360,14 @@ typedef struct sph_system_stats {
     int64_t steps;
     int64_t density_rechecked;            /* FP32C results re-evaluated in FP64
                                              because h fell within 4e-6 of rs    */
+    int64_t evals_density_first;          /* pair evaluations the density kernel
+                                             performed in the first walk, three
+                                             density passes (j beyond every i's
+                                             support dropped before the loop)    */
+    int64_t evals_density_grad;           /* the same for its gradient pass       */
+    int64_t evals_hydro_near;             /* hydro pairs evaluated in full        */
+    int64_t evals_hydro_far;              /* hydro pairs beyond both supports,
+                                             signal velocity only                */
     int32_t last_status;
 } sph_system_stats;
 

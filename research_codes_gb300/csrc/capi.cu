@@ -573,6 +573,7 @@ extern "C" int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_wal
                                                                              ks.f4[5].p, ks.f4[6].p, ks.f4[7].p);
     if (!ks.items.empty()) {
         sphk::DensityArgs a;
+        a.n_eval = nullptr;
         a.i_pm = ks.a4[0].p; a.i_vel = ks.a4[1].p; a.i_id = ks.id[0].p; a.i_ksr = ks.d1[0].p; a.i_rs = ks.d1[1].p;
         a.j_pm = ks.a4[2].p; a.j_vel = ks.a4[3].p; a.j_id = ks.id[1].p;
         a.fi = sphk::F32Part{ks.f4[0].p, ks.f4[1].p, ks.f4[2].p, ks.f4[3].p};
@@ -677,6 +678,8 @@ extern "C" int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
             ks.f4[7].p, ks.f4[11].p, ks.f4[12].p, ks.f4[13].p);
     if (!ks.items.empty()) {
         sphk::HydroArgs a;
+        a.n_eval_near = nullptr;
+        a.n_eval_far = nullptr;
         a.i_pm = ks.a4[0].p; a.i_vel = ks.a4[1].p; a.i_id = ks.id[0].p;
         a.i_h1 = ks.a4[4].p; a.i_h2 = ks.a4[5].p; a.i_h3 = ks.a2[0].p;
         a.j_pm = ks.a4[2].p; a.j_vel = ks.a4[3].p; a.j_id = ks.id[1].p;

@@ -54,7 +54,7 @@ __device__ __forceinline__ float2 df_split(double x) {
 }
 
 struct ItemRef {   // decoded work item
-    int walk, jb, nj, tpi, sub, li, ii, ic;
+    int walk, jb, nj, ni, tpi, sub, li, ii, ic;
     bool act;
 };
 
@@ -63,6 +63,7 @@ __device__ __forceinline__ ItemRef decode(const WorkItem &it, const int *j_off, 
     r.walk = it.x;
     r.jb = j_off[it.x];
     r.nj = j_off[it.x + 1] - r.jb;
+    r.ni = it.z;
     r.tpi = lanes_per_i(it.z);
     const int sh = ilog2_pow2(r.tpi);
     r.li = lane >> sh;
@@ -110,6 +111,9 @@ struct DensityArgs {
     int *amb_w;             // its walk
     int amb_cap;
     float amb_tol;
+    // when set: pair evaluations performed (j-entries kept by the support
+    // test x i-particles): [0] the three density passes, [1] the gradient pass
+    unsigned long long *n_eval;
 };
 
 template <bool F64, int WARPS>
@@ -197,6 +201,7 @@ density_kernel(const DensityArgs a) {
         // ahead of their use (the list index two chunks ahead) so that their
         // latency overlaps the box test and the pair loops.  with_v also
         // stages velocities and ids (gradient pass).
+        long long kept = 0;   // j-entries kept by the support test, all passes
         auto sweep = [&](const R rf2, const bool with_v, auto &&consume) {
             int head = 0, fill = 0;
             JRec cur, nxt;
@@ -235,6 +240,7 @@ density_kernel(const DensityArgs a) {
                     }
                 }
                 fill += __popc(m);
+                kept += __popc(m);
                 __syncwarp();
                 if (fill >= 32) {
                     consume(head, 32);
@@ -311,6 +317,7 @@ density_kernel(const DensityArgs a) {
             }
         }
 
+        const long long kept_rho = kept;
         // gradient pass with the final h, hdr_density.hpp:304-349
         {
             const R hinv = (R)1 / (R)h;
@@ -344,13 +351,30 @@ density_kernel(const DensityArgs a) {
                 pry += (uz * dx - ux * dz) * dw;
                 prz += (ux * dy - uy * dx) * dw;
             };
+            // Each lane first marks the tile entries inside its own support
+            // (r^2/h^2 below 1 + 2e-5, so every pair with q < 1 is marked),
+            // then evaluates the gradient terms of the marked entries only, in
+            // tile order; the unmarked pairs contribute exactly zero.
+            const R lim = hinv * hinv * (R)1.00002;
+            auto mark = [&](int k, unsigned &msk) {
+                const R4 pj = s_p[wid][k];
+                const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                if (!(r2 * lim >= (R)1)) msk |= 1u << (k & 31);
+            };
             auto run = [&](int head, int n) {
                 pg = 0; pd = 0; prx = 0; pry = 0; prz = 0;
+                unsigned msk = 0;
                 if (tpi == 1 && n == 32) {
-#pragma unroll 4
-                    for (int k = 0; k < 32; ++k) pair(head + k);
+#pragma unroll 8
+                    for (int k = 0; k < 32; ++k) mark(head + k, msk);
                 } else {
-                    for (int k = sub; k < n; k += tpi) pair(head + k);
+                    for (int k = sub; k < n; k += tpi) mark(head + k, msk);
+                }
+                while (msk) {
+                    const int k = __ffs(msk) - 1;
+                    msk &= msk - 1;
+                    pair(head + k);
                 }
                 g_acc.add(pg);
                 d_acc.add(pd);
@@ -401,6 +425,10 @@ density_kernel(const DensityArgs a) {
                 a.o_itr[ii] = itr ? 1 : 0;
             }
         }
+        if (a.n_eval && lane == 0) {
+            atomicAdd(a.n_eval, (unsigned long long)kept_rho * (unsigned long long)r.ni);
+            atomicAdd(a.n_eval + 1, (unsigned long long)(kept - kept_rho) * (unsigned long long)r.ni);
+        }
     }
 }
 
@@ -435,6 +463,9 @@ struct HydroArgs {
     double *o_acch;      // 3 per particle
     double *o_accg;      // 3 per particle
     double *o_udot, *o_vsmx, *o_diffu;
+    // when set: pair evaluations performed in full (near) and for the
+    // signal velocity only (far), j-entries x i-particles
+    unsigned long long *n_eval_near, *n_eval_far;
 };
 
 template <bool F64, int WARPS>
@@ -448,16 +479,17 @@ hydro_kernel(const HydroArgs a) {
     // Far ring: the others, whose pair terms all vanish except the
     // signal-velocity maximum (hdr_hydro.hpp:372 takes it over every j of
     // the list), kept as position + sound speed and velocity only.
-    __shared__ R4 s_a[WARPS][64];   // dx, dy, dz (exact hi parts), mass
-    __shared__ R4 s_b[WARPS][64];   // vx, vy, vz (hi), hinv
-    __shared__ R4 s_c[WARPS][64];   // P (hi), presc, bswt, dens
-    __shared__ R4 s_d[WARPS][64];   // vsnd, alph, alphu, u (hi)
-    __shared__ R4 s_e[WARPS][64];   // eta, hinv^4, vx lo, vy lo
-    __shared__ float4 s_f[WARPS][64]; // vz lo, P lo, u lo, -
-    __shared__ float4 s_g[WARPS][64]; // position lo parts (centred)
+    // Near-ring layout (FP32C; FP64 keeps the lo parts at zero):
+    __shared__ R4 s_p1[WARPS][64];    // dx, dy, dz (exact hi parts, item frame), hinv
+    __shared__ R4 s_p2[WARPS][64];    // position lo parts, vsnd
+    __shared__ R4 s_v1[WARPS][64];    // velocity hi, mass
+    __shared__ R4 s_v2[WARPS][64];    // velocity lo, hinv^4
+    __shared__ R4 s_c[WARPS][64];     // P (hi), presc, bswt, dens
+    __shared__ R4 s_d[WARPS][64];     // alph, alphu, u (hi), eta
+    __shared__ float2 s_f[WARPS][64]; // P lo, u lo
     __shared__ long long s_id[WARPS][64];
-    __shared__ R4 s_fp[WARPS][64];  // far: centred position, vsnd
-    __shared__ R4 s_fv[WARPS][64];  // far: velocity (hi)
+    __shared__ R4 s_fp[WARPS][64];    // far: centred position, vsnd
+    __shared__ R4 s_fv[WARPS][64];    // far: velocity (hi)
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
@@ -500,51 +532,79 @@ hydro_kernel(const HydroArgs a) {
         IBox<R> box;
         box.from_lanes(xc, yc, zc);
         const R hm2 = support2<R>(1.0 / (double)hi_i);
+        const R hi2_i = hi_i * hi_i;
 
         Acc<F64> ax, ay, az, ud, df, gx, gy, gz;
         R vsmx = 0;
         int nhead = 0, nfill = 0, fhead = 0, ffill = 0;
+        long long kept_n = 0, kept_f = 0;
         R pax = 0, pay = 0, paz = 0, pud = 0, pdf = 0, pgx = 0, pgy = 0, pgz = 0;
+        // pair separation and velocity difference of near entry k
+        auto diffs = [&](int k, R &dx, R &dy, R &dz, R &ux, R &uy, R &uz, R &r2, R &ri) {
+            const R4 P1 = s_p1[wid][k];
+            const R4 V1 = s_v1[wid][k];
+            dx = xi - P1.x; dy = yi - P1.y; dz = zi - P1.z;
+            ux = vxi - V1.x; uy = vyi - V1.y; uz = vzi - V1.z;
+            if (!F64) {
+                const R4 P2 = s_p2[wid][k];
+                const R4 V2 = s_v2[wid][k];
+                dx += (R)(xlo - (float)P2.x);
+                dy += (R)(ylo - (float)P2.y);
+                dz += (R)(zlo - (float)P2.z);
+                ux += (R)(lxi - (float)V2.x);
+                uy += (R)(lyi - (float)V2.y);
+                uz += (R)(lzi - (float)V2.z);
+            }
+            r2 = dx * dx + dy * dy + dz * dz;
+            ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
+        };
+        // Every near entry: the signal velocity (hdr_hydro.hpp:368-372) and
+        // a mark when the pair is inside either support (r^2 min(1/h_i^2,
+        // 1/h_j^2) below 1 + 2e-5, so every pair with q_i < 1 or q_j < 1 is
+        // marked).  Unmarked pairs add exactly zero to every sum.
+        auto signal = [&](int k, unsigned &msk) {
+            R dx, dy, dz, ux, uy, uz, r2, ri;
+            diffs(k, dx, dy, dz, ux, uy, uz, r2, ri);
+            const R w = (dx * ux + dy * uy + dz * uz) * ri;
+            const R wneg = w < (R)0 ? w : (R)0;
+            const R vs = cs_i + s_p2[wid][k].w - (R)3 * wneg;
+            vsmx = vs > vsmx ? vs : vsmx;
+            const R hj = s_p1[wid][k].w;
+            const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
+            if (!(r2 * hmin2 * (R)1.00002 >= (R)1)) msk |= 1u << (k & 31);
+        };
+        // The remaining terms of a marked pair, hdr_hydro.hpp:349-398
         auto pair = [&](int k) {
-            const R4 A = s_a[wid][k];
-            const R4 B = s_b[wid][k];
+            R dx, dy, dz, ux, uy, uz, r2, ri;
+            diffs(k, dx, dy, dz, ux, uy, uz, r2, ri);
+            const R4 P1 = s_p1[wid][k];
+            const R4 V1 = s_v1[wid][k];
             const R4 C = s_c[wid][k];
             const R4 D = s_d[wid][k];
-            const R4 E = s_e[wid][k];
-            R dx = xi - A.x, dy = yi - A.y, dz = zi - A.z;
-            R ux = vxi - B.x, uy = vyi - B.y, uz = vzi - B.z;
-            R dp = pp_i - C.x, du = eg_i - D.w;
+            const R hinv4_j = s_v2[wid][k].w;
+            const R cs_j = s_p2[wid][k].w;
+            R dp = pp_i - C.x, du = eg_i - D.z;
             if (!F64) {
-                const float4 F = s_f[wid][k];
-                const float4 Gl = s_g[wid][k];
-                dx += (R)(xlo - Gl.x);
-                dy += (R)(ylo - Gl.y);
-                dz += (R)(zlo - Gl.z);
-                ux += (R)(lxi - (float)E.z);
-                uy += (R)(lyi - (float)E.w);
-                uz += (R)(lzi - F.x);
-                dp += (R)(plo_i - F.y);
-                du += (R)(elo_i - F.z);
+                const float2 F = s_f[wid][k];
+                dp += (R)(plo_i - F.x);
+                du += (R)(elo_i - F.y);
             }
-            const R r2 = dx * dx + dy * dy + dz * dz;
-            const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
             const R rr = r2 * ri;
             // kernel gradients W1(q) for both smoothing lengths
-            const R qi = rr * hi_i, qj = rr * B.w;
+            const R qi = rr * hi_i, qj = rr * P1.w;
             const R ui = max0((R)1 - qi), uj = max0((R)1 - qj);
             const R ui2 = ui * ui, uj2 = uj * uj;
             const R w1i = w1_term(qi, ui, ui2, ui2 * ui, (R)1 + (R)4 * qi);
             const R w1j = w1_term(qj, uj, uj2, uj2 * uj, (R)1 + (R)4 * qj);
             const R dw_i = (R)CEFF1 * hi4_i * w1i;
-            const R dw_j = (R)CEFF1 * E.y * w1j;
-            const R ka = (dw_i + dw_j) * A.w;
+            const R dw_j = (R)CEFF1 * hinv4_j * w1j;
+            const R ka = (dw_i + dw_j) * V1.w;
             // viscosity, hdr_hydro.hpp:368-376
             const R w = (dx * ux + dy * uy + dz * uz) * ri;
             const R wneg = w < (R)0 ? w : (R)0;
-            const R vs = cs_i + D.x - (R)3 * wneg;
+            const R vs = cs_i + cs_j - (R)3 * wneg;
             const R rhi = rcp_r(dn_i + C.w);
-            const R av = (bs_i + C.z) * (al_i + D.y) * vs * wneg;
-            vsmx = vs > vsmx ? vs : vsmx;
+            const R av = (bs_i + C.z) * (al_i + D.x) * vs * wneg;
             // pressure gradient, :378-382
             const R ta = (pc_i + C.y - (R)0.5 * av * rhi) * ka * ri;
             pax -= ta * dx;
@@ -553,10 +613,10 @@ hydro_kernel(const HydroArgs a) {
             // energy equation with conduction, :384-393
             const R vsu2 = fabs(dp) * rhi * (R)2;
             const R vsu = vsu2 > (R)0 ? vsu2 * rsqrt_r(vsu2) : (R)0;
-            pud += ka * (pc_i * w - rhi * ((R)0.25 * av * wneg - (au_i + D.z) * vsu * du));
+            pud += ka * (pc_i * w - rhi * ((R)0.25 * av * wneg - (au_i + D.y) * vsu * du));
             pdf += rhi * du * ka * ri;
             // softening correction, :395-398
-            const R dg = A.w * ri * (et_i * dw_i + E.x * dw_j);
+            const R dg = V1.w * ri * (et_i * dw_i + D.w * dw_j);
             pgx += dg * dx;
             pgy += dg * dy;
             pgz += dg * dz;
@@ -575,11 +635,17 @@ hydro_kernel(const HydroArgs a) {
         };
         auto run_near = [&](int n) {
             pax = 0; pay = 0; paz = 0; pud = 0; pdf = 0; pgx = 0; pgy = 0; pgz = 0;
+            unsigned msk = 0;
             if (tpi == 1 && n == 32) {
-#pragma unroll 2
-                for (int k = 0; k < 32; ++k) pair(nhead + k);
+#pragma unroll 4
+                for (int k = 0; k < 32; ++k) signal(nhead + k, msk);
             } else {
-                for (int k = sub; k < n; k += tpi) pair(nhead + k);
+                for (int k = sub; k < n; k += tpi) signal(nhead + k, msk);
+            }
+            while (msk) {
+                const int k = __ffs(msk) - 1;
+                msk &= msk - 1;
+                pair(nhead + k);
             }
             ax.add(pax);
             ay.add(pay);
@@ -605,7 +671,7 @@ hydro_kernel(const HydroArgs a) {
             bool near = false, far = false;
             int j = 0;
             float4 ph, pl, vh, g2;
-            double4_32a p64, v64, g1_64, g2_64;
+            dbl4 p64, v64, g1_64, g2_64;
             R px = 0, py = 0, pz = 0, hj_inv = 0;
             if (jk < nj) {
                 j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
@@ -636,23 +702,26 @@ hydro_kernel(const HydroArgs a) {
             if (near) {
                 const int k = (nhead + nfill + __popc(mn & lt)) & 63;
                 if (F64) {
-                    const dbl4 g1 = g1_64, g2d = g2_64;
                     const double2 g3 = a.j_h3[j];
-                    s_a[wid][k] = Real<F64>::make4(p64.x, p64.y, p64.z, p64.w);
-                    s_b[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z, g1.x);
-                    s_c[wid][k] = Real<F64>::make4(g1.y, g1.z, g1.w, g2d.x);
-                    s_d[wid][k] = Real<F64>::make4(g2d.y, g2d.z, g2d.w, g3.x);
-                    s_e[wid][k] = Real<F64>::make4(g3.y, g1.x * g1.x * g1.x * g1.x, 0.0, 0.0);
+                    const double h4 = g1_64.x * g1_64.x * g1_64.x * g1_64.x;
+                    s_p1[wid][k] = Real<F64>::make4(p64.x, p64.y, p64.z, g1_64.x);
+                    s_p2[wid][k] = Real<F64>::make4(0.0, 0.0, 0.0, g2_64.y);
+                    s_v1[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z, p64.w);
+                    s_v2[wid][k] = Real<F64>::make4(0.0, 0.0, 0.0, h4);
+                    s_c[wid][k] = Real<F64>::make4(g1_64.y, g1_64.z, g1_64.w, g2_64.x);
+                    s_d[wid][k] = Real<F64>::make4(g2_64.z, g2_64.w, g3.x, g3.y);
+                    s_f[wid][k] = make_float2(0.0f, 0.0f);
                 } else {
                     const float4 vl = a.fj.vlo[j], g1 = a.fj_g1[j], g3 = a.fj_g3[j];
-                    s_a[wid][k] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y),
-                                                   (R)(ph.z - cph.z), (R)ph.w);
-                    s_g[wid][k] = make_float4(pl.x - cpl.x, pl.y - cpl.y, pl.z - cpl.z, 0.0f);
-                    s_b[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)vh.w);
+                    s_p1[wid][k] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y), (R)(ph.z - cph.z),
+                                                    (R)vh.w);
+                    s_p2[wid][k] = Real<F64>::make4((R)(pl.x - cpl.x), (R)(pl.y - cpl.y), (R)(pl.z - cpl.z),
+                                                    (R)g2.y);
+                    s_v1[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)ph.w);
+                    s_v2[wid][k] = Real<F64>::make4((R)vl.x, (R)vl.y, (R)vl.z, (R)vl.w);
                     s_c[wid][k] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
-                    s_d[wid][k] = Real<F64>::make4((R)g2.y, (R)g2.z, (R)g2.w, (R)g3.x);
-                    s_e[wid][k] = Real<F64>::make4((R)g3.z, (R)vl.w, (R)vl.x, (R)vl.y);
-                    s_f[wid][k] = make_float4(vl.z, g1.y, g3.y, 0.0f);
+                    s_d[wid][k] = Real<F64>::make4((R)g2.z, (R)g2.w, (R)g3.x, (R)g3.z);
+                    s_f[wid][k] = make_float2(g1.y, g3.y);
                 }
                 s_id[wid][k] = a.j_id[j];
             }
@@ -668,6 +737,8 @@ hydro_kernel(const HydroArgs a) {
             }
             nfill += __popc(mn);
             ffill += __popc(mf);
+            kept_n += __popc(mn);
+            kept_f += __popc(mf);
             __syncwarp();
             if (nfill >= 32) {
                 run_near(32);
@@ -697,6 +768,10 @@ hydro_kernel(const HydroArgs a) {
             a.o_udot[ii] = 0.5 * sud;
             a.o_vsmx[ii] = svs;
             a.o_diffu[ii] = 2.0 * sdf;
+        }
+        if (a.n_eval_near && lane == 0) {
+            atomicAdd(a.n_eval_near, (unsigned long long)kept_n * (unsigned long long)r.ni);
+            atomicAdd(a.n_eval_far, (unsigned long long)kept_f * (unsigned long long)r.ni);
         }
     }
 }

@@ -40,7 +40,8 @@ enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, 
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
 // 64-bit counters
-enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_NI };
+enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_EVAL_D1,
+       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_NI };
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
@@ -1040,6 +1041,7 @@ int density_phase(sph_system *s, bool eager) {
         if (r) return r;
         CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
         sphk::DensityArgs a;
+        a.n_eval = (it == 0) ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_D1) : nullptr;
         a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p; a.i_ksr = s->ksr[0].p;
         a.i_rs = s->rs.p;
         a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
@@ -1069,6 +1071,7 @@ int density_phase(sph_system *s, bool eager) {
             accumulate_int<<<1, 1, 0, st>>>(s->scal.p + S_AMB, s->scal.p + S_AMBTOT);
             CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
             sphk::DensityArgs f = a;
+            f.n_eval = nullptr;
             f.items = s->fitems.p;
             f.n_items_dev = s->scal.p + S_NFIX;
             f.i_list = s->amb_i.p;
@@ -1139,6 +1142,8 @@ int hydro_phase(sph_system *s, bool eager) {
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_HK_B], st);
     sphk::HydroArgs a;
+    a.n_eval_near = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HN);
+    a.n_eval_far = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HF);
     a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p;
     a.i_h1 = s->h1.p; a.i_h2 = s->h2.p; a.i_h3 = s->h3.p;
     a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
@@ -1602,6 +1607,10 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->list_gravity = lc[L_LIST_G];
     o->steps = s->steps;
     o->density_rechecked = sc[S_AMBTOT];
+    o->evals_density_first = lc[L_EVAL_D1];
+    o->evals_density_grad = lc[L_EVAL_DG1];
+    o->evals_hydro_near = lc[L_EVAL_HN];
+    o->evals_hydro_far = lc[L_EVAL_HF];
     o->last_status = s->last_status;
     return SPH_OK;
 }

@@ -7,6 +7,8 @@ smoothing lengths have converged (one density walk), then runs one more
 evaluation between cudaProfilerStart and cudaProfilerStop, so that
 `ncu --profile-from-start off` captures exactly the kernels of a steady
 force evaluation.  Prints the phase times (CUDA events) of that evaluation.
+With --what step the settling and the profiled call are whole steps
+(kick-drift, forces with search-radius re-walks, correction).
 """
 import argparse
 import ctypes
@@ -30,6 +32,8 @@ def main():
     ap.add_argument("--precision", default="fp32c")
     ap.add_argument("--n-group", type=int, default=256)
     ap.add_argument("--settle", type=int, default=4, help="force evaluations before the profiled one")
+    ap.add_argument("--what", choices=("forces", "step"), default="forces",
+                    help="profile one force evaluation or one whole step (after --settle steps)")
     args = ap.parse_args()
     import torch
     torch.cuda.init()
@@ -40,11 +44,17 @@ def main():
         ps = ParticleSystem(ctx, n, n_group=args.n_group, use_graph=0)
         ps.upload(s)
         for _ in range(args.settle):
-            ps.compute_forces()            # h converges in place
+            if args.what == "step":
+                ps.step(1)
+            else:
+                ps.compute_forces()        # h converges in place
         start, stop = _driver_profiler()
         torch.cuda.synchronize()
         start()
-        ps.compute_forces()
+        if args.what == "step":
+            ps.step(1)
+        else:
+            ps.compute_forces()
         torch.cuda.synchronize()
         stop()
         out = {"n": n, "stats": ps.stats(), "phases_ms": ps.phase_times()}

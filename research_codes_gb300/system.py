@@ -42,7 +42,8 @@ class SystemStats(ctypes.Structure):
                 ("e_tot", _D), ("n_groups", _I64), ("density_iterations", _I64), ("pairs_density", _I64),
                 ("pairs_density_first", _I64), ("pairs_hydro", _I64), ("pairs_gravity", _I64), ("list_density", _I64),
                 ("list_hydro", _I64), ("list_gravity", _I64), ("steps", _I64), ("density_rechecked", _I64),
-                ("last_status", _I32)]
+                ("evals_density_first", _I64), ("evals_density_grad", _I64), ("evals_hydro_near", _I64),
+                ("evals_hydro_far", _I64), ("last_status", _I32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
