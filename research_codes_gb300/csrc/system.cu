@@ -35,7 +35,7 @@ constexpr int MAX_RED = 8;
 // int scalars
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_NTASKS, S_NROOTS, S_BKT, S_NI = S_BKT + 2 * NBKT };
+       S_NTASKS, S_NROOTS, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -340,38 +340,72 @@ __global__ void item_buckets(int n, const int *n_walks, const int *i_count, cons
     }
 }
 
-// Start of each cost class in the item array, most expensive class first
-// (bkt[NBKT + b]), and the item count.
-__global__ void bucket_offsets(int *bkt, int *n_items) {
+// Item order.  The items of the SPH_HEAVY_CLASSES most expensive nonempty
+// cost classes go first, most expensive class first, so that the persistent
+// kernels start the longest items early; all other items follow in walk
+// order, so that warps running at the same time work on neighbouring walks
+// and share their j records in L2.  The order of items does not affect any
+// result (every item owns its outputs).
+#ifndef SPH_HEAVY_CLASSES
+#define SPH_HEAVY_CLASSES 2
+#endif
+
+// bkt[0..NBKT): class counts (in); bkt[NBKT + b]: cursor of heavy class b;
+// bkt[2 NBKT]: lowest heavy class; bkt[2 NBKT + 1]: number of heavy items.
+__global__ void bucket_offsets(int *bkt) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int bmax = -1;
+        for (int b = NBKT - 1; b >= 0 && bmax < 0; --b)
+            if (bkt[b] > 0) bmax = b;
+        const int bh = bmax - SPH_HEAVY_CLASSES + 1;
         int acc = 0;
         for (int b = NBKT - 1; b >= 0; --b) {
             bkt[NBKT + b] = acc;
-            acc += bkt[b];
+            if (b >= bh) acc += bkt[b];
         }
-        *n_items = acc;
+        bkt[2 * NBKT] = bh;
+        bkt[2 * NBKT + 1] = acc;
     }
 }
 
-// Work items in decreasing cost class, so that the persistent kernels take
-// the longest items first and finish on short ones.  The order of items
-// inside a class does not affect any result (every item owns its outputs).
-__global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count, int chunk,
-                           int split_nj, const int *j_cnt, int *cursor, WorkItem *items, long long *pairs) {
+// Number of light items (class below the heavy ones) of each walk.
+__global__ void light_counts(int n, const int *n_walks, const int *i_count, const int *j_cnt, int chunk,
+                             int split_nj, const int *bkt, int *lc) {
     const int nw = *n_walks;
+    const int bh = bkt[2 * NBKT];
+    GRID_STRIDE(k, n + 1) {
+        int c = 0;
+        if (k < nw) {
+            const int ni = i_count[k], nj = j_cnt[k];
+            const int ch = item_chunk(nj, chunk, split_nj);
+            for (int c0 = 0; c0 < ni; c0 += ch) c += cost_bucket(nj, min(ch, ni - c0)) < bh ? 1 : 0;
+        }
+        lc[k] = c;
+    }
+}
+
+__global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count, int chunk,
+                           int split_nj, const int *j_cnt, int *bkt, const int *light_off, WorkItem *items,
+                           int *n_items, long long *pairs) {
+    const int nw = *n_walks;
+    const int bh = bkt[2 * NBKT];
+    const int n_heavy = bkt[2 * NBKT + 1];
     long long local = 0;
     GRID_STRIDE(k, n) {
         if (k < nw) {
             const int ni = i_count[k];
             const int nj = j_cnt[k];
             const int ch = item_chunk(nj, chunk, split_nj);
+            int lpos = n_heavy + light_off[k];
             for (int c0 = 0; c0 < ni; c0 += ch) {
                 const int sz = min(ch, ni - c0);
-                const int pos = atomicAdd(&cursor[cost_bucket(nj, sz)], 1);
+                const int b = cost_bucket(nj, sz);
+                const int pos = (b >= bh) ? atomicAdd(&bkt[NBKT + b], 1) : lpos++;
                 items[pos] = make_int4(k, i_first[k] + c0, sz, nj * sz);
             }
             local += (long long)ni * nj;
         }
+        if (k == 0) *n_items = n_heavy + light_off[nw];
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0 && local) atomicAdd((unsigned long long *)pairs, (unsigned long long)local);
@@ -995,11 +1029,17 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // drop most of the list); gravity lists are uniform and kept whole
     const int split_nj = (kind == 2) ? (1 << 30) : ITEM_SPLIT_NJ;
     int *bkt = s->scal.p + S_BKT;
-    CUDA_TRY(cudaMemsetAsync(bkt, 0, sizeof(int) * 2 * NBKT, st));
+    CUDA_TRY(cudaMemsetAsync(bkt, 0, sizeof(int) * (2 * NBKT + 2), st));
     item_buckets<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj, bkt);
-    bucket_offsets<<<1, 32, 0, st>>>(bkt, s->scal.p + S_NITEMS);
+    bucket_offsets<<<1, 32, 0, st>>>(bkt);
+    // light items in walk order: per-walk counts (the task arrays are free
+    // again once the lists are built) and their scan
+    light_counts<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj,
+                                                  bkt, s->tcnt.p);
+    r = exclusive_scan(s, s->tcnt.p, s->toff.p, n + 1);
+    if (r) return r;
     fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], ifirst, icount, chunk, split_nj, s->lcnt[kind].p,
-                                            bkt + NBKT, s->items.p, pairs);
+                                            bkt, s->toff.p, s->items.p, s->scal.p + S_NITEMS, pairs);
     return SPH_OK;
 }
 
