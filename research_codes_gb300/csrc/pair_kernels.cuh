@@ -25,9 +25,13 @@
 #include "sph_device.cuh"
 
 // Minimum resident blocks per SM requested from the compiler for the FP32C
-// density and hydro kernels (register budget 65536 / (128 threads x blocks)).
+// density, gravity and hydro kernels (register budget 65536 / (128 threads x
+// blocks)).
 #ifndef SPH_DENSITY_MIN_BLOCKS
 #define SPH_DENSITY_MIN_BLOCKS 5
+#endif
+#ifndef SPH_GRAVITY_MIN_BLOCKS
+#define SPH_GRAVITY_MIN_BLOCKS 4
 #endif
 #ifndef SPH_HYDRO_MIN_BLOCKS
 #define SPH_HYDRO_MIN_BLOCKS 4
@@ -802,12 +806,16 @@ struct GravityArgs {
 };
 
 template <bool F64, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_GRAVITY_MIN_BLOCKS)
 gravity_kernel(const GravityArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
-    __shared__ R4 s_p[WARPS][32];   // dx, dy, dz, mass
-    __shared__ R s_e[WARPS][32];    // eps2
+    // FP64: one record per entry; FP32C: structure of arrays, so that two
+    // consecutive entries load as one f32x2 operand
+    __shared__ R4 s_p[F64 ? WARPS : 1][32];   // dx, dy, dz, mass
+    __shared__ R s_e[F64 ? WARPS : 1][32];    // eps2
+    __shared__ __align__(16) float s_x[F64 ? 1 : WARPS][32], s_y[F64 ? 1 : WARPS][32], s_z[F64 ? 1 : WARPS][32],
+        s_m[F64 ? 1 : WARPS][32], s_q[F64 ? 1 : WARPS][32];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
@@ -834,46 +842,70 @@ gravity_kernel(const GravityArgs a) {
             e2i = l.w;
         }
         Acc<F64> ax, ay, az, pt, et;
+        // j records are loaded one tile ahead of their use, list indices
+        // two tiles ahead, so that their latency overlaps the pair loop
+        auto jlist = [&](int k) -> int { return a.j_idx ? a.j_idx[jb + k] : jb + k; };
+        float4 nh = make_float4(0, 0, 0, 0), nl = nh;   // next tile (FP32C)
+        dbl4 np64 = make_dbl4(0, 0, 0, 0);              // next tile (FP64)
+        double ne64 = 0.0;
+        auto load = [&](int j) {
+            if constexpr (F64) {
+                if (j < a.n_split) {
+                    np64 = a.j_pm[j];
+                    ne64 = a.j_eps2[j];
+                } else {
+                    np64 = a.s_pm[j - a.n_split];
+                    ne64 = a.s_eps2[j - a.n_split];
+                }
+            } else {
+                if (j < a.n_split) {
+                    nh = a.f_phi[j];
+                    nl = a.f_plo[j];
+                } else {
+                    nh = a.f_shi[j - a.n_split];
+                    nl = a.f_slo[j - a.n_split];
+                }
+            }
+        };
+        int jn = 0;
+        if (lane < nj) load(jlist(lane));
+        if (32 + lane < nj) jn = jlist(32 + lane);
         for (int t = 0; t < nj; t += 32) {
             const int jk = t + lane;
+            const float4 h = nh, l = nl;
+            const dbl4 p64 = np64;
+            const double e64 = ne64;
+            if (t + 32 + lane < nj) load(jn);
+            if (t + 64 + lane < nj) jn = jlist(t + 64 + lane);
             if (jk < nj) {
-                const int j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
                 if (F64) {
-                    dbl4 p;
-                    double e2;
-                    if (j < a.n_split) {
-                        p = a.j_pm[j];
-                        e2 = a.j_eps2[j];
-                    } else {
-                        p = a.s_pm[j - a.n_split];
-                        e2 = a.s_eps2[j - a.n_split];
-                    }
-                    s_p[wid][lane] = Real<F64>::make4(p.x, p.y, p.z, p.w);
-                    s_e[wid][lane] = e2;
+                    s_p[wid][lane] = Real<F64>::make4(p64.x, p64.y, p64.z, p64.w);
+                    s_e[wid][lane] = e64;
                 } else {
-                    float4 h, l;
-                    if (j < a.n_split) {
-                        h = a.f_phi[j];
-                        l = a.f_plo[j];
-                    } else {
-                        h = a.f_shi[j - a.n_split];
-                        l = a.f_slo[j - a.n_split];
-                    }
-                    s_p[wid][lane] = Real<F64>::make4((R)df_diff(h.x, l.x, ch.x, cl.x),
-                                                      (R)df_diff(h.y, l.y, ch.y, cl.y),
-                                                      (R)df_diff(h.z, l.z, ch.z, cl.z), (R)h.w);
-                    s_e[wid][lane] = (R)l.w;
+                    s_x[wid][lane] = df_diff(h.x, l.x, ch.x, cl.x);
+                    s_y[wid][lane] = df_diff(h.y, l.y, ch.y, cl.y);
+                    s_z[wid][lane] = df_diff(h.z, l.z, ch.z, cl.z);
+                    s_m[wid][lane] = h.w;
+                    s_q[wid][lane] = l.w;
                 }
             }
             __syncwarp();
             const int n = min(32, nj - t);
             R pax = 0, pay = 0, paz = 0, ppt = 0, pet = 0;
             auto pair = [&](int k) {
-                const R4 pj = s_p[wid][k];
+                R4 pj;
+                R ej;
+                if constexpr (F64) {
+                    pj = s_p[wid][k];
+                    ej = s_e[wid][k];
+                } else {
+                    pj = Real<F64>::make4(s_x[wid][k], s_y[wid][k], s_z[wid][k], s_m[wid][k]);
+                    ej = s_q[wid][k];
+                }
                 const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
                 const R r2 = dx * dx + dy * dy + dz * dz;
                 const R rei = rsqrt_r(r2 + e2i);
-                const R rej = rsqrt_r(r2 + s_e[wid][k]);
+                const R rej = rsqrt_r(r2 + ej);
                 const R rei3 = rei * rei * rei;
                 const R rej3 = rej * rej * rej;
                 const R g = pj.w * (rei3 + rej3);
@@ -883,7 +915,42 @@ gravity_kernel(const GravityArgs a) {
                 paz -= dz * g;
                 pet += pj.w * rei3;
             };
-            if (tpi == 1 && n == 32) {
+            if (!F64 && tpi == 1 && n == 32) {
+                // full tile, FP32C: two entries per instruction (f32x2); the
+                // even and odd entries are summed separately and combined
+                // at the end of the tile.  Sums of -x are kept as sums of x
+                // and negated once (exact).
+                const f2 XI = f2_make((float)xi, (float)xi), YI = f2_make((float)yi, (float)yi);
+                const f2 ZI = f2_make((float)zi, (float)zi), EI = f2_make((float)e2i, (float)e2i);
+                const f2 NEG = f2_make(-1.0f, -1.0f);
+                f2 AX = f2_make(0.0f, 0.0f), AY = AX, AZ = AX, PT = AX, ET = AX;
+#pragma unroll 4
+                for (int k = 0; k < 32; k += 2) {
+                    const f2 DX = f2_fma(f2_lds(&s_x[wid][k]), NEG, XI);
+                    const f2 DY = f2_fma(f2_lds(&s_y[wid][k]), NEG, YI);
+                    const f2 DZ = f2_fma(f2_lds(&s_z[wid][k]), NEG, ZI);
+                    const f2 M = f2_lds(&s_m[wid][k]);
+                    const f2 R2 = f2_fma(DZ, DZ, f2_fma(DY, DY, f2_mul(DX, DX)));
+                    const float2 ai = f2_get(f2_add(R2, EI));
+                    const float2 aj = f2_get(f2_add(R2, f2_lds(&s_q[wid][k])));
+                    const f2 REI = f2_make(rsqrt_r(ai.x), rsqrt_r(ai.y));
+                    const f2 REJ = f2_make(rsqrt_r(aj.x), rsqrt_r(aj.y));
+                    const f2 REI3 = f2_mul(f2_mul(REI, REI), REI);
+                    const f2 REJ3 = f2_mul(f2_mul(REJ, REJ), REJ);
+                    const f2 G = f2_mul(M, f2_add(REI3, REJ3));
+                    PT = f2_fma(M, f2_add(REI, REJ), PT);
+                    AX = f2_fma(DX, G, AX);
+                    AY = f2_fma(DY, G, AY);
+                    AZ = f2_fma(DZ, G, AZ);
+                    ET = f2_fma(M, REI3, ET);
+                }
+                const float2 ax2 = f2_get(AX), ay2 = f2_get(AY), az2 = f2_get(AZ), pt2 = f2_get(PT), et2 = f2_get(ET);
+                pax = -(R)(ax2.x + ax2.y);
+                pay = -(R)(ay2.x + ay2.y);
+                paz = -(R)(az2.x + az2.y);
+                ppt = -(R)(pt2.x + pt2.y);
+                pet = (R)(et2.x + et2.y);
+            } else if (tpi == 1 && n == 32) {
 #pragma unroll 8
                 for (int k = 0; k < 32; ++k) pair(k);
             } else {

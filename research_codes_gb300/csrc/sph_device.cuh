@@ -144,6 +144,45 @@ __device__ __forceinline__ int lanes_per_i(int n_i) {
 
 __device__ __forceinline__ int ilog2_pow2(int x) { return __ffs(x) - 1; }
 
+// Two FP32 values in one 64-bit register pair, for the packed f32x2
+// arithmetic of sm_100 and later: one instruction applies the operation to
+// both halves, each rounded exactly as the scalar instruction would.
+struct f2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ f2 f2_make(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 f2_get(f2 x) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(x.v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+// a * b + c
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+// two consecutive floats of shared memory (8-byte aligned address)
+__device__ __forceinline__ f2 f2_lds(const float *p) {
+    f2 r;
+    r.v = *reinterpret_cast<const unsigned long long *>(p);
+    return r;
+}
+
 // Minimum / maximum over the 32 lanes of a warp (NaN lanes are ignored).
 __device__ __forceinline__ float warp_min(float v) {
     for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(FULL, v, o));

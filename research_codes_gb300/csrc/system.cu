@@ -344,20 +344,21 @@ __global__ void item_buckets(int n, const int *n_walks, const int *i_count, cons
 // cost classes go first, most expensive class first, so that the persistent
 // kernels start the longest items early; all other items follow in walk
 // order, so that warps running at the same time work on neighbouring walks
-// and share their j records in L2.  The order of items does not affect any
-// result (every item owns its outputs).
+// and share their j records in L2.  Gravity lists are of nearly uniform
+// length, so their items all stay in walk order (heavy = 0).  The order of
+// items does not affect any result (every item owns its outputs).
 #ifndef SPH_HEAVY_CLASSES
 #define SPH_HEAVY_CLASSES 2
 #endif
 
 // bkt[0..NBKT): class counts (in); bkt[NBKT + b]: cursor of heavy class b;
 // bkt[2 NBKT]: lowest heavy class; bkt[2 NBKT + 1]: number of heavy items.
-__global__ void bucket_offsets(int *bkt) {
+__global__ void bucket_offsets(int *bkt, int heavy) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int bmax = -1;
         for (int b = NBKT - 1; b >= 0 && bmax < 0; --b)
             if (bkt[b] > 0) bmax = b;
-        const int bh = bmax - SPH_HEAVY_CLASSES + 1;
+        const int bh = bmax - heavy + 1;
         int acc = 0;
         for (int b = NBKT - 1; b >= 0; --b) {
             bkt[NBKT + b] = acc;
@@ -1031,7 +1032,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     int *bkt = s->scal.p + S_BKT;
     CUDA_TRY(cudaMemsetAsync(bkt, 0, sizeof(int) * (2 * NBKT + 2), st));
     item_buckets<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj, bkt);
-    bucket_offsets<<<1, 32, 0, st>>>(bkt);
+    bucket_offsets<<<1, 32, 0, st>>>(bkt, kind == 2 ? 0 : SPH_HEAVY_CLASSES);
     // light items in walk order: per-walk counts (the task arrays are free
     // again once the lists are built) and their scan
     light_counts<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj,
