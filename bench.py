@@ -257,7 +257,7 @@ def run_ours(args):
     if os.path.exists(PROFILE_TRAFFIC):
         tr = json.load(open(PROFILE_TRAFFIC))
         if dom in tr:
-            traffic = tr[dom].get("bytes_per_launch_scaled")
+            traffic = tr[dom].get("bytes_per_launch")
 
     line = {"metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
             "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps,
@@ -499,7 +499,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-frac", type=float, default=0.03)
+    ap.add_argument("--cpu-frac", type=float, default=1.0)
     ap.add_argument("--ref-frac", type=float, default=0.03)
     args = ap.parse_args()
     if args.warmup < 3:
