@@ -405,6 +405,21 @@ int sph_system_download_sorted(sph_system *sys, int32_t field, double *out);
 
 int sph_system_get_stats(sph_system *sys, sph_system_stats *out);
 
+/* Host -> device copy of one per-particle field in upload order, for
+ * restarting from a checkpoint (the reference's readHexa restores the whole
+ * particle state, hdr_hgas.hpp:198-284, and continues without a new force
+ * evaluation, hdr_hgas.hpp:1383-1412).  Any field of sph_field except
+ * SPH_F_POS, SPH_F_VEL, SPH_F_MASS, SPH_F_NP, SPH_F_ID and SPH_F_ISTAR, which
+ * sph_system_upload sets. */
+int sph_system_set_field(sph_system *sys, int32_t field, const double *data);
+
+/* Run clock and the run parameters derived from the state: time, current
+ * time step, kernel-support-radius cap (ksrmax) and the internal-energy floor
+ * epsu (the reference keeps them in the checkpoint header,
+ * hdr_hgas.hpp:890-926).  set: a negative value leaves an entry unchanged. */
+int sph_system_get_clock(sph_system *sys, double *time, double *dt, double *ksr_max, double *eps_u);
+int sph_system_set_clock(sph_system *sys, double time, double dt, double ksr_max, double eps_u);
+
 /* Interaction lists of the last force evaluation (kind 0 density — the first
  * walk, which covers every group —, 1 hydro, 2 gravity), in Morton order:
  * walk w has i-particles [i_first[w], i_first[w] + i_count[w]) and list
@@ -433,6 +448,24 @@ int sph_system_graph_kernels(sph_system *sys, int32_t step, int64_t *kernels);
 
 /* Monopoles of the 2n-1 tree nodes: mom[4*k..] = (x, y, z, mass), eps2[k]. */
 int sph_system_get_nodes(sph_system *sys, double *mom, double *eps2);
+
+/* ------------------------------------------------------------------------ */
+/* Text encodings of the reference's particle files (host only, no device).
+ * Rows of n particles: "id istar" then ncol values of cols (row-major n x
+ * ncol).  Each returns the number of bytes the text needs (out may be null)
+ * and writes it when out holds cap >= that many bytes; minus a status code
+ * on bad arguments. */
+/* Checkpoint rows: values as the hexadecimal image of their FP64 bits
+ * ("%6lld %2lld %llx ..."), HelmholtzGas::writeHexa, hdr_hgas.hpp:286-316. */
+int64_t sph_format_hexa_rows(int64_t n, const int64_t *id, const int64_t *istar, int32_t ncol,
+                             const double *cols, char *out, int64_t cap);
+/* Parses n such rows from text[0..len); returns the rows read. */
+int64_t sph_parse_hexa_rows(const char *text, int64_t len, int64_t n, int32_t ncol, int64_t *id,
+                            int64_t *istar, double *cols);
+/* Snapshot rows (HelmholtzGas::writeAscii, hdr_hgas.hpp:136-180): kinds[k]
+ * is 'e' (" %+e"), 'c' (" %+.3e") or 'd' (" %6lld" of the value). */
+int64_t sph_format_ascii_rows(int64_t n, const int64_t *id, const int64_t *istar, int32_t ncol,
+                              const double *cols, const char *kinds, char *out, int64_t cap);
 
 /* ------------------------------------------------------------------------ */
 /* ABI self-description, used by the tests to check the struct layouts.

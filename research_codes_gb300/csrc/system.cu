@@ -631,6 +631,14 @@ __global__ void correct(int n, const double *dsc, dbl4 *vel, const dbl4 *vel2, c
 
 __global__ void advance_time(double *dsc) { dsc[D_TIME] += dsc[D_DT]; }
 
+// dst (current order) from src (upload order): dst[p] = src[orig[p]]
+__global__ void gather_field(int n, int width, const int *orig, const double *src, double *dst) {
+    GRID_STRIDE(p, n) {
+        const int q = orig[p];
+        for (int c = 0; c < width; ++c) dst[(size_t)p * width + c] = src[(size_t)q * width + c];
+    }
+}
+
 __global__ void scatter_field(int n, int width, const int *orig, const double *src, double *dst) {
     GRID_STRIDE(p, n) {
         const int q = orig[p];
@@ -1606,6 +1614,85 @@ extern "C" int sph_system_download(sph_system *s, int32_t field, double *out) {
     scatter_field<<<grid_for(n), 256, 0, s->st()>>>(n, w, s->orig[0].p, src, dst);
     CUDA_TRY(cudaMemcpyAsync(out, dst, sizeof(double) * w * (size_t)n, cudaMemcpyDeviceToHost, s->st()));
     CUDA_TRY(cudaStreamSynchronize(s->st()));
+    return SPH_OK;
+}
+
+namespace {
+// Writable device array of a field (restart), or null.
+double *field_target(sph_system *s, int field, int *width) {
+    *width = 1;
+    switch (field) {
+        case SPH_F_ACC: *width = 3; return s->acc.p;
+        case SPH_F_ACCH: *width = 3; return s->acch.p;
+        case SPH_F_ACCG1: *width = 3; return s->accg1.p;
+        case SPH_F_ACCG2: *width = 3; return s->accg2.p;
+        case SPH_F_DENS: return s->dens.p;
+        case SPH_F_PRES: return s->pres.p;
+        case SPH_F_VSND: return s->vsnd.p;
+        case SPH_F_KSR: return s->ksr[0].p;
+        case SPH_F_DIVV: return s->divv.p;
+        case SPH_F_ROTV: return s->rotv.p;
+        case SPH_F_BSWT: return s->bswt.p;
+        case SPH_F_GRDH: return s->grdh.p;
+        case SPH_F_UENE: return s->uene[0].p;
+        case SPH_F_UDOT: return s->udot.p;
+        case SPH_F_ALPH: return s->alph[0].p;
+        case SPH_F_ALPHU: return s->alphu[0].p;
+        case SPH_F_POT: return s->pot.p;
+        case SPH_F_ETA: return s->eta.p;
+        case SPH_F_VSMX: return s->vsmx.p;
+        case SPH_F_DIFFU: return s->diffu.p;
+        case SPH_F_ADOT: return s->adot.p;
+        case SPH_F_ADOTU: return s->adotu.p;
+        default: return nullptr;
+    }
+}
+}  // namespace
+
+extern "C" int sph_system_set_field(sph_system *s, int32_t field, const double *data) {
+    if (!s || !data) return SPH_ERR_INVALID_ARGUMENT;
+    int w = 1;
+    double *dst = field_target(s, field, &w);
+    if (!dst) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    // staging (3n doubles) receives the upload-order copy
+    CUDA_TRY(cudaMemcpyAsync(s->staging.p, data, sizeof(double) * w * (size_t)n, cudaMemcpyHostToDevice, st));
+    gather_field<<<grid_for(n), 256, 0, st>>>(n, w, s->orig[0].p, s->staging.p, dst);
+    if (field == SPH_F_UENE)
+        CUDA_TRY(cudaMemcpyAsync(s->uene2[0].p, dst, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    if (field == SPH_F_ALPH)
+        CUDA_TRY(cudaMemcpyAsync(s->alph2[0].p, dst, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    if (field == SPH_F_ALPHU)
+        CUDA_TRY(cudaMemcpyAsync(s->alphu2[0].p, dst, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+extern "C" int sph_system_get_clock(sph_system *s, double *time, double *dt, double *ksr_max, double *eps_u) {
+    if (!s) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    double dc[D_NI];
+    CUDA_TRY(cudaMemcpyAsync(dc, s->dscal.p, sizeof(dc), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    if (time) *time = dc[D_TIME];
+    if (dt) *dt = dc[D_DT];
+    if (ksr_max) *ksr_max = dc[D_KSRMAX];
+    if (eps_u) *eps_u = dc[D_EPSU];
+    return SPH_OK;
+}
+
+extern "C" int sph_system_set_clock(sph_system *s, double time, double dt, double ksr_max, double eps_u) {
+    if (!s) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    cudaStream_t st = s->st();
+    const int slot[4] = {D_TIME, D_DT, D_KSRMAX, D_EPSU};
+    const double val[4] = {time, dt, ksr_max, eps_u};
+    for (int k = 0; k < 4; ++k)
+        if (val[k] >= 0.0)
+            CUDA_TRY(cudaMemcpyAsync(s->dscal.p + slot[k], &val[k], sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
     return SPH_OK;
 }
 

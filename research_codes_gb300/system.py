@@ -66,6 +66,10 @@ def _declare(lib):
         "sph_system_phase_times": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float), _I32]),
         "sph_system_set_graph": (ctypes.c_int, [_P, _I32]),
         "sph_system_graph_kernels": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_int64)]),
+        "sph_system_set_field": (ctypes.c_int, [_P, _I32, _P]),
+        "sph_system_get_clock": (ctypes.c_int, [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
+                                                ctypes.POINTER(_D)]),
+        "sph_system_set_clock": (ctypes.c_int, [_P, _D, _D, _D, _D]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -132,6 +136,23 @@ class ParticleSystem:
 
     def set_graph(self, on):
         check(self.lib.sph_system_set_graph(self.handle, 1 if on else 0), self.ctx.handle, "set_graph")
+
+    def set_field(self, field, data):
+        """Host -> device copy of one field in upload order (restart)."""
+        code, w = FIELDS[field]
+        arr = np.ascontiguousarray(data, dtype=np.float64)
+        if arr.size != self.n * w:
+            raise ValueError(f"{field}: expected {self.n * w} values, got {arr.size}")
+        check(self.lib.sph_system_set_field(self.handle, code, _ptr(arr)), self.ctx.handle, f"set_field {field}")
+
+    def clock(self):
+        """(time, dt, ksr_max, eps_u) of the run."""
+        v = [_D() for _ in range(4)]
+        check(self.lib.sph_system_get_clock(self.handle, *[ctypes.byref(x) for x in v]), self.ctx.handle, "clock")
+        return tuple(x.value for x in v)
+
+    def set_clock(self, time=-1.0, dt=-1.0, ksr_max=-1.0, eps_u=-1.0):
+        check(self.lib.sph_system_set_clock(self.handle, time, dt, ksr_max, eps_u), self.ctx.handle, "set_clock")
 
     def graph_kernels(self, step=True):
         """Kernel launches per replay of the captured step (or force) graph."""

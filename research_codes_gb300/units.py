@@ -13,6 +13,7 @@ UNIT_VELOCITY = UNIT_LENGTH / UNIT_TIME
 UNIT_DENSITY = UNIT_MASS / UNIT_LENGTH ** 3
 UNIT_ENERGY = UNIT_VELOCITY ** 2      # specific energy
 UNIT_PRESSURE = UNIT_MASS / (UNIT_LENGTH * UNIT_TIME ** 2)
+UNIT_ACCELERATION = UNIT_VELOCITY / UNIT_TIME
 
 # GravityConstantInThisUnit, hdr_heos.hpp:102-104
 G = GRAVITY_CGS / (UNIT_LENGTH ** 3 / UNIT_MASS / UNIT_TIME ** 2)
