@@ -446,6 +446,23 @@ int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);
  * graph has not been captured. */
 int sph_system_graph_kernels(sph_system *sys, int32_t step, int64_t *kernels);
 
+/* ---- analysis of the current state on the device (the reference's
+ * post-processing scripts).  star < 0: all particles, else those with
+ * istar == star. */
+/* Density-weighted centre and velocity, analysis/common.py:71-90:
+ * out = (x, y, z, vx, vy, vz, sum of densities). */
+int sph_system_center_of_gravity(sph_system *sys, int32_t star, double *out);
+/* Bound and unbound mass (out[0], out[1]): unbound when
+ * |v - vel_ref|^2 / 2 + pot + u > 0, analysis/unbound_mass/unbound_mass.py:10-27. */
+int sph_system_bound_mass(sph_system *sys, int32_t star, const double *vel_ref, double *out);
+/* Mass within `radius` of `center`, energy_check/energy_check.py:50-68. */
+int sph_system_mass_within(sph_system *sys, int32_t star, const double *center, double radius, double *out);
+/* Distances of the particles of the set from `center`, sorted ascending on
+ * the device, with their masses (arrays of n; the first *count are set), the
+ * input of Lagrange radii, analysis/lagrange_radius/lagrange_radius.py:25-47. */
+int sph_system_radii_sorted(sph_system *sys, int32_t star, const double *center, double *r, double *m,
+                            int64_t *count);
+
 /* Monopoles of the 2n-1 tree nodes: mom[4*k..] = (x, y, z, mass), eps2[k]. */
 int sph_system_get_nodes(sph_system *sys, double *mom, double *eps2);
 

@@ -157,6 +157,63 @@ struct UeneMin : MinOp {
     __device__ void operator()(int p, double *a) const { a[0] = fmin(a[0], uene[p]); }
 };
 
+// Analysis of the state (the reference's post-processing scripts, run here
+// on the device): particle set = all particles (star < 0) or those of one
+// star (istar == star).
+// density-weighted centre and velocity, analysis/common.py:71-90
+struct DensCentre : SumOp {
+    static constexpr int K = 7;
+    const dbl4 *pos, *vel;
+    const double *dens;
+    const int *istar;
+    int star;
+    __device__ void operator()(int p, double *a) const {
+        if (star >= 0 && istar[p] != star) return;
+        const dbl4 x = pos[p], v = vel[p];
+        const double d = dens[p];
+        a[0] += d * x.x;
+        a[1] += d * x.y;
+        a[2] += d * x.z;
+        a[3] += d * v.x;
+        a[4] += d * v.y;
+        a[5] += d * v.z;
+        a[6] += d;
+    }
+};
+
+// bound / unbound mass: e = |v - v_ref|^2 / 2 + pot + u > 0 is unbound,
+// analysis/unbound_mass/unbound_mass.py:10-27
+struct BoundMass : SumOp {
+    static constexpr int K = 2;
+    const dbl4 *pos, *vel;
+    const double *pot, *uene;
+    const int *istar;
+    int star;
+    double vx, vy, vz;
+    __device__ void operator()(int p, double *a) const {
+        if (star >= 0 && istar[p] != star) return;
+        const dbl4 v = vel[p];
+        const double dx = v.x - vx, dy = v.y - vy, dz = v.z - vz;
+        const double e = 0.5 * (dx * dx + dy * dy + dz * dz) + pot[p] + uene[p];
+        a[e > 0.0 ? 1 : 0] += pos[p].w;
+    }
+};
+
+// mass within a radius of a point, energy_check/energy_check.py:50-68
+struct MassWithin : SumOp {
+    static constexpr int K = 1;
+    const dbl4 *pos;
+    const int *istar;
+    int star;
+    double cx, cy, cz, r;
+    __device__ void operator()(int p, double *a) const {
+        if (star >= 0 && istar[p] != star) return;
+        const dbl4 x = pos[p];
+        const double dx = x.x - cx, dy = x.y - cy, dz = x.z - cz;
+        if (sqrt(dx * dx + dy * dy + dz * dz) < r) a[0] += x.w;
+    }
+};
+
 struct StarComs : SumOp {    // both stars' centres (calcSystemSize, hdr_util.hpp:95-113)
     static constexpr int K = 8;
     const dbl4 *pos;
@@ -746,6 +803,7 @@ struct sph_system {
     HostBuf<double> h_dscal;
     HostBuf<long long> h_lscal;
     DevBuf<double> staging;
+    DevBuf<double> an_buf;   // analysis scratch (4 n), allocated on first use
     DevBuf<char> cub_tmp;
     size_t cub_bytes = 0;
     // graph
@@ -818,7 +876,7 @@ int alloc_all(sph_system *s) {
     e |= s->tasks.ensure(s->task_cap) | s->tlcnt.ensure(s->task_cap + 1) | s->tloff.ensure(s->task_cap + 1);
     e |= s->items.ensure(n);
     e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
-    e |= s->partial.ensure(RED_BLOCKS * MAX_RED) | s->box.ensure(8);
+    e |= s->partial.ensure(RED_BLOCKS * MAX_RED + MAX_RED) | s->box.ensure(8);
     e |= s->h_scal.ensure(S_NI) | s->h_dscal.ensure(D_NI) | s->h_lscal.ensure(L_NI);
     // CUB scratch: radix sort of (uint64, int) pairs and exclusive sums over n ints
     size_t b1 = 0, b2 = 0;
@@ -1378,7 +1436,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
             s->roots.release();
         }
     }
-    s->items.release(); s->lscal.release(); s->cub_tmp.release();
+    s->items.release(); s->lscal.release(); s->cub_tmp.release(); s->an_buf.release();
     s->h_scal.release(); s->h_dscal.release(); s->h_lscal.release();
     delete s;
     return SPH_OK;
@@ -1799,5 +1857,96 @@ extern "C" int sph_system_get_nodes(sph_system *s, double *mom, double *eps2) {
     CUDA_TRY(cudaMemcpyAsync(mom, s->mom.p, sizeof(dbl4) * nn, cudaMemcpyDeviceToHost, s->st()));
     CUDA_TRY(cudaMemcpyAsync(eps2, s->neps2.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, s->st()));
     CUDA_TRY(cudaStreamSynchronize(s->st()));
+    return SPH_OK;
+}
+
+// ============================================================== analysis
+namespace {
+// distance of every particle of the set from (cx, cy, cz) (+inf outside the
+// set) and its mass
+__global__ void radii_from(int n, const dbl4 *pos, const int *istar, int star, double cx, double cy, double cz,
+                           double *r, double *m) {
+    GRID_STRIDE(p, n) {
+        const dbl4 x = pos[p];
+        const double dx = x.x - cx, dy = x.y - cy, dz = x.z - cz;
+        r[p] = (star < 0 || istar[p] == star) ? sqrt(dx * dx + dy * dy + dz * dz) : INFINITY;
+        m[p] = x.w;
+    }
+}
+
+template <class F>
+int reduce_to_host(sph_system *s, const F &f, double *out) {
+    reduce(s, f, s->partial.p + RED_BLOCKS * MAX_RED);   // result slots after the partials
+    CUDA_TRY(cudaMemcpyAsync(out, s->partial.p + RED_BLOCKS * MAX_RED, sizeof(double) * F::K,
+                             cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    return SPH_OK;
+}
+}  // namespace
+
+extern "C" int sph_system_center_of_gravity(sph_system *s, int32_t star, double *out) {
+    if (!s || !out) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    DensCentre f{};
+    f.pos = s->pos[0].p; f.vel = s->vel[0].p; f.dens = s->dens.p; f.istar = s->istar[0].p; f.star = star;
+    double a[7];
+    const int r = reduce_to_host(s, f, a);
+    if (r) return r;
+    for (int k = 0; k < 6; ++k) out[k] = a[6] > 0.0 ? a[k] / a[6] : 0.0;
+    out[6] = a[6];
+    return SPH_OK;
+}
+
+extern "C" int sph_system_bound_mass(sph_system *s, int32_t star, const double *vel_ref, double *out) {
+    if (!s || !vel_ref || !out) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    BoundMass f{};
+    f.pos = s->pos[0].p; f.vel = s->vel[0].p; f.pot = s->pot.p; f.uene = s->uene[0].p; f.istar = s->istar[0].p;
+    f.star = star; f.vx = vel_ref[0]; f.vy = vel_ref[1]; f.vz = vel_ref[2];
+    return reduce_to_host(s, f, out);
+}
+
+extern "C" int sph_system_mass_within(sph_system *s, int32_t star, const double *center, double radius,
+                                      double *out) {
+    if (!s || !center || !out) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    MassWithin f{};
+    f.pos = s->pos[0].p; f.istar = s->istar[0].p; f.star = star;
+    f.cx = center[0]; f.cy = center[1]; f.cz = center[2]; f.r = radius;
+    return reduce_to_host(s, f, out);
+}
+
+extern "C" int sph_system_radii_sorted(sph_system *s, int32_t star, const double *center, double *r_out,
+                                       double *m_out, int64_t *count) {
+    if (!s || !center || !count) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    if (s->an_buf.ensure(4 * (size_t)n))
+        return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "analysis buffer allocation failed");
+    double *r0 = s->an_buf.p, *m0 = r0 + n, *r1 = m0 + n, *m1 = r1 + n;
+    radii_from<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->istar[0].p, star, center[0], center[1], center[2],
+                                            r0, m0);
+    size_t bytes = 0;
+    CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, bytes, r0, r1, m0, m1, n, 0, 64, st));
+    if (bytes > s->cub_bytes) {
+        if (s->cub_tmp.ensure(bytes)) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "CUB scratch allocation failed");
+        s->cub_bytes = bytes;
+        s->graph_valid = false;
+        s->force_graph_valid = false;
+    }
+    bytes = s->cub_bytes;
+    CUDA_TRY(cub::DeviceRadixSort::SortPairs(s->cub_tmp.p, bytes, r0, r1, m0, m1, n, 0, 64, st));
+    std::vector<double> rh(n);
+    CUDA_TRY(cudaMemcpyAsync(rh.data(), r1, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    int64_t c = 0;
+    while (c < n && rh[c] != INFINITY) ++c;
+    *count = c;
+    if (r_out) std::memcpy(r_out, rh.data(), sizeof(double) * (size_t)c);
+    if (m_out) {
+        CUDA_TRY(cudaMemcpyAsync(m_out, m1, sizeof(double) * (size_t)c, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
     return SPH_OK;
 }
