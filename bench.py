@@ -179,7 +179,9 @@ def run_ours(args):
     log(f"[bench] rank {rank}: {args.config} n={n} ic {time.time() - t_ic:.1f}s")
 
     ctx = functors.Context(device=local, precision="fp32c", eta=ETA)
-    ps = ParticleSystem(ctx, n, n_group=args.n_group)
+    # the large collision (c4) runs its gravity with node quadrupoles
+    quad = 1 if args.config == "c4" else 0
+    ps = ParticleSystem(ctx, n, n_group=args.n_group, quadrupole=quad)
     ps.upload(s)
     ps.compute_forces()
     stream = torch.cuda.ExternalStream(ctx.stream())

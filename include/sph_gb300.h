@@ -333,6 +333,10 @@ typedef struct sph_system_params {
                             mass after every force evaluation (hdr_util.hpp:489-527)   */
     int32_t max_density_iterations; /* cap on search-radius expansions              */
     int32_t use_graph;   /* capture sph_system_step's body as a CUDA graph              */
+    int32_t quadrupole;  /* 1: tree nodes accepted by the gravity walk act with their
+                            mass and traceless quadrupole (no counterpart in the
+                            reference, whose SPJ is a monopole, hdr_gravity.hpp:6-91);
+                            0: monopole, as the reference                             */
 } sph_system_params;
 
 /* Fields for sph_system_download / sph_system_download_sorted. */

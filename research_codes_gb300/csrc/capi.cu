@@ -773,6 +773,7 @@ extern "C" int sph_dispatch_gravity(sph_context *ctx, int32_t tag, int32_t n_wal
         a.j_idx = nullptr;
         a.queue = ctx->d_queue + K_GRAV;
         a.o_acc = ks.o[0].p; a.o_pot = ks.o[1].p; a.o_eta = ks.o[2].p;
+        a.s_quad = nullptr; a.f_sq0 = nullptr; a.f_sq1 = nullptr;   // SPJ are monopoles
         launch_gravity(a, ctx->prm.precision, pair_grid(ctx, K_GRAV, ctx->prm.precision, a.n_items), ctx->stream);
     }
     if (ni > 0)

@@ -141,6 +141,7 @@ extern "C" int sph_calc_gravity_ep_noalloc(const sph_GravityEPI *epi, int32_t n_
     noalloc_prepare<<<pb < 1024 ? pb : 1024, 256, 0, s>>>(epi, n_i, epj, n_j, scr);
     sphk::GravityArgs a;
     a.i_pe = nullptr; a.j_pm = nullptr; a.j_eps2 = nullptr; a.s_pm = nullptr; a.s_eps2 = nullptr;
+    a.s_quad = nullptr; a.f_sq0 = nullptr; a.f_sq1 = nullptr;
     a.fi_phi = reinterpret_cast<const float4 *>(scr + OFF_FI_HI);
     a.fi_plo = reinterpret_cast<const float4 *>(scr + OFF_FI_LO);
     a.f_phi = reinterpret_cast<const float4 *>(scr + OFF_FJ_HI);

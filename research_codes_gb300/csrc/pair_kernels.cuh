@@ -803,6 +803,12 @@ struct GravityArgs {
     int *queue;
     double *o_acc;          // 3 per particle (assigned)
     double *o_pot, *o_eta;
+    // quadrupole of the sources k >= n_split (tree nodes), traceless, about
+    // their centre of mass; null: monopoles only (the reference's SPJ).
+    // FP64: 6 per node (xx, yy, zz, xy, xz, yz); FP32C: (xx, yy, zz, xy) and
+    // (xz, yz, -, -)
+    const double *s_quad;
+    const float4 *f_sq0, *f_sq1;
 };
 
 template <bool F64, int WARPS>
@@ -816,6 +822,13 @@ gravity_kernel(const GravityArgs a) {
     __shared__ R s_e[F64 ? WARPS : 1][32];    // eps2
     __shared__ __align__(16) float s_x[F64 ? 1 : WARPS][32], s_y[F64 ? 1 : WARPS][32], s_z[F64 ? 1 : WARPS][32],
         s_m[F64 ? 1 : WARPS][32], s_q[F64 ? 1 : WARPS][32];
+    // tree-node entries of the list with their quadrupoles, compacted into a
+    // 64-entry ring (position in the item frame + eps^2; Q xx yy zz xy; Q xz yz)
+    __shared__ R4 q_p[WARPS][64];
+    __shared__ R4 q_a[WARPS][64];
+    __shared__ typename Real<F64>::T2 q_b[WARPS][64];
+    const unsigned lt = lanemask_lt();
+    const bool quad = F64 ? (a.s_quad != nullptr) : (a.f_sq0 != nullptr);
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
@@ -867,16 +880,77 @@ gravity_kernel(const GravityArgs a) {
                 }
             }
         };
-        int jn = 0;
-        if (lane < nj) load(jlist(lane));
+        int jn = 0, jnx = 0;   // list index two tiles ahead, of the next tile
+        if (lane < nj) {
+            jnx = jlist(lane);
+            load(jnx);
+        }
         if (32 + lane < nj) jn = jlist(32 + lane);
+        int qhead = 0, qfill = 0;
+        // quadrupole terms of the node entries in the ring: the potential
+        // -(1/2) r.Q.r R^5 and acceleration Q r R^5 - (5/2)(r.Q.r) r R^7 with
+        // r = x_i - c and R = (r^2 + eps_node^2)^(-1/2), accumulated doubled
+        // like the monopole sums (halved once at the end)
+        auto run_quad = [&](int n_q) {
+            R qax = 0, qay = 0, qaz = 0, qpt = 0;
+            for (int k = sub; k < n_q; k += tpi) {
+                const R4 P = q_p[wid][qhead + k];
+                const R4 A = q_a[wid][qhead + k];
+                const typename Real<F64>::T2 B = q_b[wid][qhead + k];
+                const R dx = xi - P.x, dy = yi - P.y, dz = zi - P.z;
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                const R rr = rsqrt_r(r2 + P.w);
+                const R rr2 = rr * rr;
+                const R rr5 = rr2 * rr2 * rr;
+                const R rr7 = rr5 * rr2;
+                const R qx = A.x * dx + A.w * dy + B.x * dz;
+                const R qy = A.w * dx + A.y * dy + B.y * dz;
+                const R qz = B.x * dx + B.y * dy + A.z * dz;
+                const R rqr = dx * qx + dy * qy + dz * qz;
+                const R f = (R)5 * rqr * rr7;
+                qax += (R)2 * qx * rr5 - f * dx;
+                qay += (R)2 * qy * rr5 - f * dy;
+                qaz += (R)2 * qz * rr5 - f * dz;
+                qpt -= rqr * rr5;
+            }
+            ax.add(qax);
+            ay.add(qay);
+            az.add(qaz);
+            pt.add(qpt);
+            __syncwarp();
+        };
         for (int t = 0; t < nj; t += 32) {
             const int jk = t + lane;
             const float4 h = nh, l = nl;
             const dbl4 p64 = np64;
             const double e64 = ne64;
-            if (t + 32 + lane < nj) load(jn);
+            const int jcur = jnx;
+            if (t + 32 + lane < nj) {
+                jnx = jn;
+                load(jn);
+            }
             if (t + 64 + lane < nj) jn = jlist(t + 64 + lane);
+            if (quad) {
+                const bool node = jk < nj && jcur >= a.n_split;
+                const unsigned mq = __ballot_sync(FULL, node);
+                if (node) {
+                    const int slot = (qhead + qfill + __popc(mq & lt)) & 63;
+                    const int nd = jcur - a.n_split;
+                    if constexpr (F64) {
+                        const double *q = a.s_quad + 6 * (size_t)nd;
+                        q_p[wid][slot] = Real<F64>::make4(p64.x, p64.y, p64.z, e64);
+                        q_a[wid][slot] = Real<F64>::make4(q[0], q[1], q[2], q[3]);
+                        q_b[wid][slot] = Real<F64>::make2(q[4], q[5]);
+                    } else {
+                        const float4 q0 = a.f_sq0[nd], q1 = a.f_sq1[nd];
+                        q_p[wid][slot] = Real<F64>::make4(df_diff(h.x, l.x, ch.x, cl.x), df_diff(h.y, l.y, ch.y, cl.y),
+                                                          df_diff(h.z, l.z, ch.z, cl.z), l.w);
+                        q_a[wid][slot] = q0;
+                        q_b[wid][slot] = make_float2(q1.x, q1.y);
+                    }
+                }
+                qfill += __popc(mq);
+            }
             if (jk < nj) {
                 if (F64) {
                     s_p[wid][lane] = Real<F64>::make4(p64.x, p64.y, p64.z, p64.w);
@@ -962,7 +1036,13 @@ gravity_kernel(const GravityArgs a) {
             pt.add(ppt);
             et.add(pet);
             __syncwarp();
+            if (qfill >= 32) {
+                run_quad(32);
+                qhead ^= 32;
+                qfill -= 32;
+            }
         }
+        if (qfill > 0) run_quad(qfill);
         const double sax = seg_sum(ax.value(), tpi), say = seg_sum(ay.value(), tpi);
         const double saz = seg_sum(az.value(), tpi), spt = seg_sum(pt.value(), tpi);
         const double set = seg_sum(et.value(), tpi);

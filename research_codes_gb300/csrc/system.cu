@@ -767,6 +767,8 @@ struct sph_system {
     DevBuf<int2> child;
     DevBuf<int> parent, first, count, visit;
     DevBuf<dbl4> mom;
+    DevBuf<double> quad;          // 6 per node, quadrupole runs only
+    DevBuf<float4> fq0, fq1;
     DevBuf<double> neps2;
     DevBuf<float4> flo, fhi, fmom, ptest;
     // FP32C double-float records (particles, hydro fields, tree monopoles)
@@ -831,6 +833,7 @@ struct sph_system {
         sphtree::Nodes t;
         t.child = child.p; t.parent = parent.p; t.first = first.p; t.count = count.p;
         t.mom = mom.p; t.eps2 = neps2.p; t.visit = visit.p;
+        t.quad = quad.p; t.fq0 = fq0.p; t.fq1 = fq1.p;
         t.flo = flo.p; t.fhi = fhi.p; t.fmom = fmom.p; t.ptest = ptest.p;
         return t;
     }
@@ -860,6 +863,7 @@ int alloc_all(sph_system *s) {
     e |= s->pe.ensure(n) | s->h1.ensure(n) | s->h2.ensure(n) | s->h3.ensure(n);
     e |= s->child.ensure(n) | s->parent.ensure(nn) | s->first.ensure(nn) | s->count.ensure(nn);
     e |= s->visit.ensure(n) | s->mom.ensure(nn) | s->neps2.ensure(nn);
+    if (s->prm.quadrupole) e |= s->quad.ensure(6 * nn) | s->fq0.ensure(nn) | s->fq1.ensure(nn);
     e |= s->flo.ensure(nn) | s->fhi.ensure(nn) | s->fmom.ensure(nn) | s->ptest.ensure(n);
     DevBuf<float4> *f1[] = {&s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo, &s->f_g1, &s->f_g2, &s->f_g3};
     for (auto *b : f1) e |= b->ensure(n);
@@ -920,9 +924,15 @@ int refit_tree(sph_system *s) {
     cudaStream_t st = s->st();
     sphtree::Nodes t = s->nodes();
     CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
-    sphtree::refit_bottom<<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
-        s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
-    sphtree::refit_top<<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+    if (s->prm.quadrupole) {
+        sphtree::refit_bottom<true><<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
+            s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
+        sphtree::refit_top<true><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+    } else {
+        sphtree::refit_bottom<false><<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
+            s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
+        sphtree::refit_top<false><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+    }
     return SPH_OK;
 }
 
@@ -1225,6 +1235,11 @@ int gravity_phase(sph_system *s, bool eager) {
     a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
     a.j_off = s->loff[2].p; a.j_idx = s->jidx[2].p; a.queue = s->scal.p + S_QUEUE;
     a.o_acc = s->r_acc.p; a.o_pot = s->r_pot.p; a.o_eta = s->r_eta.p;
+    const bool q64 = s->prm.quadrupole && ctx->prm.precision == SPH_PREC_FP64;
+    const bool q32 = s->prm.quadrupole && ctx->prm.precision != SPH_PREC_FP64;
+    a.s_quad = q64 ? s->quad.p : nullptr;
+    a.f_sq0 = q32 ? s->fq0.p : nullptr;
+    a.f_sq1 = q32 ? s->fq1.p : nullptr;
     sphrt::launch_gravity(a, ctx->prm.precision, ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st);
     cudaEventRecord(s->ev[EV_GK_E], st);
     gravity_writeback<<<grid_for(n), 256, 0, st>>>(n, s->prm.G, s->r_acc.p, s->r_pot.p, s->r_eta.p, s->ksr[0].p,
@@ -1369,6 +1384,7 @@ extern "C" void sph_system_params_default(sph_system_params *p) {
     p->ksr_max_mode = 1;
     p->max_density_iterations = 8;
     p->use_graph = 1;
+    p->quadrupole = 0;
 }
 
 extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p, sph_system **out) {
@@ -1419,7 +1435,8 @@ extern "C" int sph_system_destroy(sph_system *s) {
     for (auto *b : d1) b->release();
     s->np.release(); s->t_np.release(); s->t_itr.release(); s->pe.release(); s->h1.release();
     s->h2.release(); s->h3.release(); s->child.release(); s->parent.release(); s->first.release();
-    s->count.release(); s->visit.release(); s->mom.release();
+    s->count.release(); s->visit.release(); s->mom.release(); s->quad.release(); s->fq0.release();
+    s->fq1.release();
     DevBuf<float4> *f1[] = {&s->flo, &s->fhi, &s->fmom, &s->ptest, &s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo,
                             &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
     for (auto *b : f1) b->release();

@@ -49,6 +49,12 @@ struct Nodes {
     float4 *fhi;      // hi (rounded up), w = largest box side (up)
     float4 *fmom;     // centre of mass, mass
     float4 *ptest;    // per particle: position (nearest), h (rounded up)
+    // quadrupole (when the system uses it, else null): traceless
+    // Q = sum m (3 d d^T - |d|^2 I) about the centre of mass, FP64 as
+    // (xx, yy, zz, xy, xz, yz) per node, and its FP32 copy
+    // fq0 = (xx, yy, zz, xy), fq1 = (xz, yz, 0, 0)
+    double *quad;
+    float4 *fq0, *fq1;
 };
 
 // ---- 1. keys ------------------------------------------------------------
@@ -193,6 +199,60 @@ __device__ __forceinline__ NodeData load_node_cg(const Nodes &t, int node) {
     return d;
 }
 
+// Traceless quadrupole of a parent from its children's, about the parent's
+// centre of mass c: Q = Q_a + Q_b + sum_k m_k (3 d_k d_k^T - |d_k|^2 I),
+// d_k = c_k - c (parallel-axis rule; linear in the moments, so the traceless
+// form combines directly).
+struct Quad {
+    double q[6];   // xx, yy, zz, xy, xz, yz
+};
+
+__device__ __forceinline__ void add_shifted(Quad &r, const Quad &a, double m, double dx, double dy, double dz) {
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    r.q[0] += a.q[0] + m * (3.0 * dx * dx - d2);
+    r.q[1] += a.q[1] + m * (3.0 * dy * dy - d2);
+    r.q[2] += a.q[2] + m * (3.0 * dz * dz - d2);
+    r.q[3] += a.q[3] + m * 3.0 * dx * dy;
+    r.q[4] += a.q[4] + m * 3.0 * dx * dz;
+    r.q[5] += a.q[5] + m * 3.0 * dy * dz;
+}
+
+__device__ __forceinline__ Quad combine_quad(const NodeData &a, const Quad &qa, const NodeData &b, const Quad &qb) {
+    Quad r;
+    for (int k = 0; k < 6; ++k) r.q[k] = 0.0;
+    const double m = a.sm.w + b.sm.w;
+    if (!(m > 0.0)) {
+        for (int k = 0; k < 6; ++k) r.q[k] = qa.q[k] + qb.q[k];
+        return r;
+    }
+    const double mi = 1.0 / m;
+    const double cx = (a.sm.x + b.sm.x) * mi, cy = (a.sm.y + b.sm.y) * mi, cz = (a.sm.z + b.sm.z) * mi;
+    const NodeData *c[2] = {&a, &b};
+    const Quad *q[2] = {&qa, &qb};
+    for (int k = 0; k < 2; ++k) {
+        const double mk = c[k]->sm.w;
+        if (mk > 0.0) {
+            const double ik = 1.0 / mk;
+            add_shifted(r, *q[k], mk, c[k]->sm.x * ik - cx, c[k]->sm.y * ik - cy, c[k]->sm.z * ik - cz);
+        } else {
+            for (int j = 0; j < 6; ++j) r.q[j] += q[k]->q[j];
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ void store_quad(const Nodes &t, int node, const Quad &q) {
+    for (int k = 0; k < 6; ++k) t.quad[6 * (size_t)node + k] = q.q[k];
+    t.fq0[node] = make_float4((float)q.q[0], (float)q.q[1], (float)q.q[2], (float)q.q[3]);
+    t.fq1[node] = make_float4((float)q.q[4], (float)q.q[5], 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ Quad load_quad_cg(const Nodes &t, int node) {
+    Quad q;
+    for (int k = 0; k < 6; ++k) q.q[k] = __ldcg(&t.quad[6 * (size_t)node + k]);
+    return q;
+}
+
 // The refit runs in two parts.  Bottom: every maximal subtree of at most
 // REFIT_B particles is refitted by one block in shared memory (one thread per
 // leaf climbing while it is the second arrival at a node, block-scope
@@ -209,11 +269,13 @@ __global__ void mark_subtrees(Nodes t, int n, int *roots, int *n_roots) {
     }
 }
 
+template <bool QUAD>
 __global__ void __launch_bounds__(REFIT_B)
 refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes t, const int *roots,
              const int *n_roots) {
     // slots 0..B-1: internal node (index - first), B..2B-1: leaf (particle - first)
     __shared__ NodeData sd[2 * REFIT_B];
+    __shared__ Quad sq[QUAD ? 2 * REFIT_B : 1];
     __shared__ int visit[REFIT_B];
     const int nr = *n_roots;
     for (int r = blockIdx.x; r < nr; r += gridDim.x) {
@@ -239,6 +301,12 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
             t.fmom[node] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)x.w);
             t.ptest[p] = make_float4((float)x.x, (float)x.y, (float)x.z, __double2float_ru(hp));
             sd[REFIT_B + threadIdx.x] = d;
+            if (QUAD) {
+                Quad z;
+                for (int k = 0; k < 6; ++k) z.q[k] = 0.0;
+                sq[REFIT_B + threadIdx.x] = z;
+                store_quad(t, node, z);
+            }
             while (node != root) {
                 node = t.parent[node];
                 // internal nodes of the subtree have indices in [a, a + c)
@@ -250,6 +318,11 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
                 const int sa = (ch.x >= n - 1) ? REFIT_B + (ch.x - (n - 1) - a) : ch.x - a;
                 const int sb = (ch.y >= n - 1) ? REFIT_B + (ch.y - (n - 1) - a) : ch.y - a;
                 if (sa < 0 || sa >= 2 * REFIT_B || sb < 0 || sb >= 2 * REFIT_B) break;
+                if (QUAD) {
+                    const Quad q = combine_quad(sd[sa], sq[sa], sd[sb], sq[sb]);
+                    sq[node - a] = q;
+                    store_quad(t, node, q);
+                }
                 d = combine(sd[sa], sd[sb]);
                 sd[node - a] = d;
                 store_node(t, node, d);
@@ -260,6 +333,7 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
 }
 
 // visit[] (internal nodes) is zero on entry.
+template <bool QUAD>
 __global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots) {
     const int nr = *n_roots;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
@@ -272,7 +346,9 @@ __global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots) 
                          : "=r"(arrived) : "l"(&t.visit[node]) : "memory");
             if (arrived == 0) break;   // sibling not finished yet
             const int2 ch = t.child[node];
-            store_node(t, node, combine(load_node_cg(t, ch.x), load_node_cg(t, ch.y)));
+            const NodeData da = load_node_cg(t, ch.x), db = load_node_cg(t, ch.y);
+            if (QUAD) store_quad(t, node, combine_quad(da, load_quad_cg(t, ch.x), db, load_quad_cg(t, ch.y)));
+            store_node(t, node, combine(da, db));
             node = t.parent[node];
         }
     }

@@ -34,7 +34,7 @@ class SystemParams(ctypes.Structure):
     _fields_ = [("n_group", _I32), ("n_leaf", _I32), ("theta", _D), ("G", _D), ("c_dt", _D),
                 ("dt_max", _D), ("dt_min", _D), ("alpha_max", _D), ("alpha_min", _D),
                 ("alphu_max", _D), ("alphu_min", _D), ("ksr_max_mode", _I32),
-                ("max_density_iterations", _I32), ("use_graph", _I32)]
+                ("max_density_iterations", _I32), ("use_graph", _I32), ("quadrupole", _I32)]
 
 
 class SystemStats(ctypes.Structure):

@@ -315,3 +315,36 @@ def test_checkpoint_restart_continues_bit_for_bit(tmp_path):
         assert snap["pos"].shape == (n, 3) and np.all(snap["np"] > 0)
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32c", "fp64"])
+def test_quadrupole_tree_gravity_vs_direct_sum(prec):
+    """theta = 0.5 tree gravity with node quadrupoles against direct FP64
+    summation (the oracle of the quadrupole option, which has no counterpart
+    in the reference): the force error falls well below the monopole tree's
+    on the same state."""
+    s = _two_stars(n=6000)
+    n = len(s["mass"])
+    err = {}
+    for quad in (0, 1):
+        with functors.Context(precision=prec, eta=1.18) as ctx:
+            sys = ParticleSystem(ctx, n, n_group=64, use_graph=0, quadrupole=quad)
+            sys.upload(s)
+            sys.compute_forces()
+            f = _sorted(sys, "pos", "mass", "ksr", "accg2", "pot")
+            eps2 = (f["ksr"] / units.KSRH) ** 2
+            sel = np.random.default_rng(1).choice(n, 300, replace=False)
+            epi = np.zeros(len(sel), abi.GravityEPI)
+            epi["pos"], epi["eps2"] = f["pos"][sel], eps2[sel]
+            epj = np.zeros(n, abi.GravityEPJ)
+            epj["mass"], epj["pos"], epj["eps2"] = f["mass"], f["pos"], eps2
+            ref = orc.gravity(epi, epj)
+            G = sys.params.G
+            a_err = np.linalg.norm(f["accg2"][sel] - G * ref["acc"], axis=1) / np.linalg.norm(G * ref["acc"], axis=1)
+            p_err = np.abs(f["pot"][sel] - G * ref["pot"]) / np.abs(G * ref["pot"])
+            err[quad] = (np.median(a_err), np.quantile(a_err, 0.99), np.median(p_err))
+            sys.close()
+    assert err[1][0] < 0.35 * err[0][0], err
+    assert err[1][1] < 0.5 * err[0][1], err
+    assert err[1][2] < 0.5 * err[0][2], err
+    assert err[1][0] < 1e-3, err
