@@ -184,6 +184,16 @@ def run_ours(args):
     ps = ParticleSystem(ctx, n, n_group=args.n_group, quadrupole=quad)
     ps.upload(s)
     ps.compute_forces()
+    tuned = None
+    if not args.no_autotune:
+        # work shaping only: n_group stays the reference's (it defines the
+        # listed pairs of the metric)
+        from research_codes_gb300 import autotune
+        ps.compute_forces()
+        best, table = autotune.autotune(ps, candidates={k: v for k, v in autotune.CANDIDATES.items()
+                                                        if k != "n_group"})
+        tuned = {"chosen": best, "force_ms": [{"params": p, "ms": round(ms, 3)} for p, ms in table[:6]]}
+        log(f"[bench] autotune: {best}")
     stream = torch.cuda.ExternalStream(ctx.stream())
     for _ in range(args.warmup):
         ps.step(1)
@@ -282,7 +292,7 @@ def run_ours(args):
                                  "pairs beyond the kernel support, per_kernel gives the evaluated work",
                          "frac_evaluated": per_kernel[dom]["achieved_evaluated_tflops"] / peak,
                          "per_kernel": per_kernel},
-            "gpu_launches": None, "clocks": clk}
+            "gpu_launches": None, "clocks": clk, "autotune": tuned}
 
     # kernel launches in the timed region: the kernel nodes of the captured
     # step graph (CUB sort/scan kernels compiled into the library included)
@@ -501,6 +511,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-frac", type=float, default=1.0)
     ap.add_argument("--ref-frac", type=float, default=0.03)
     args = ap.parse_args()

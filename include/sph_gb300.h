@@ -337,6 +337,10 @@ typedef struct sph_system_params {
                             mass and traceless quadrupole (no counterpart in the
                             reference, whose SPJ is a monopole, hdr_gravity.hpp:6-91);
                             0: monopole, as the reference                             */
+    int32_t item_split_nj; /* density / hydro walks whose list is longer than this are
+                            cut into work items of 16, 8 or 4 i-particles (<= 0: 4096) */
+    int32_t heavy_classes; /* work items of this many most expensive cost classes run
+                            first, the rest in walk order (< 0: 2)                      */
 } sph_system_params;
 
 /* Fields for sph_system_download / sph_system_download_sorted. */
@@ -376,6 +380,12 @@ typedef struct sph_system_stats {
 } sph_system_stats;
 
 void sph_system_params_default(sph_system_params *p);
+
+/* Changes the run parameters of an existing system (the next evaluation
+ * re-captures its graphs): n_group, n_leaf, theta, the time-step and
+ * viscosity parameters, item_split_nj and heavy_classes; quadrupole may only
+ * be switched on if the system was created with it. */
+int sph_system_set_params(sph_system *sys, const sph_system_params *p);
 
 /* Allocates a system of n particles on the context's device. */
 int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p,

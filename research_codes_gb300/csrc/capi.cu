@@ -320,6 +320,9 @@ extern "C" int sph_context_create(const sph_params *p, sph_context **out) {
 
 extern "C" int sph_context_destroy(sph_context *ctx) {
     if (!ctx) return SPH_ERR_INVALID_ARGUMENT;
+    // systems hold the context's stream: they must go first
+    if (ctx->n_systems > 0)
+        return set_error(ctx, SPH_ERR_STATE, "%d system(s) still use this context", ctx->n_systems);
     cudaSetDevice(ctx->prm.device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (int k = 0; k < 3; ++k) ctx->kind[k].release();

@@ -146,6 +146,7 @@ struct sph_context {
     int *h_flags = nullptr;   // pinned copies of the flags
     int grid[3][2] = {{0}};   // persistent grid per kind and precision
     sphrt::KindState kind[3];
+    int n_systems = 0;        // live sph_system objects using this context
     char err[512] = {0};
 };
 

@@ -27,7 +27,7 @@ using sphrt::HostBuf;
 namespace {
 
 constexpr double KSRH = sphk::KSRH;
-constexpr int ITEM_SPLIT_NJ = 4096;   // list length above which a walk's items are halved (down to 4 i)
+constexpr int ITEM_SPLIT_NJ = 4096;   // default list length above which a walk's items are halved (down to 4 i)
 constexpr int RED_BLOCKS = 296;   // 2 x 148..152 SMs; fixed for deterministic sums
 constexpr int RED_THREADS = 256;
 constexpr int MAX_RED = 8;
@@ -1059,7 +1059,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
         int nt = 0;
         CUDA_TRY(cudaMemcpyAsync(&nt, s->toff.p + n, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
-        if (nt > s->task_cap) {
+        if (nt + nt / 4 > s->task_cap) {
             r = grow_tasks(s, nt + nt / 2 + 1024);
             if (r) return r;
         }
@@ -1083,7 +1083,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
         long long tot = 0;
         CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
-        if (tot + 1 > s->lcap[kind]) {
+        if (tot + tot / 4 + 1 > s->lcap[kind]) {   // keep a quarter of headroom for graph replays
             long long want = tot + tot / 2 + 1024;
             if (kind == 3) want = std::max(want, s->lcap[0]);   // re-walks may cover many walks
             if (s->jidx[kind].ensure((size_t)want))
@@ -1104,11 +1104,12 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     const int *icount = item_count ? item_count : s->walk_count[kind];
     // density and hydro walks with long lists are split (their pair loops
     // drop most of the list); gravity lists are uniform and kept whole
-    const int split_nj = (kind == 2) ? (1 << 30) : ITEM_SPLIT_NJ;
+    const int split_nj = (kind == 2) ? (1 << 30) : (s->prm.item_split_nj > 0 ? s->prm.item_split_nj : ITEM_SPLIT_NJ);
     int *bkt = s->scal.p + S_BKT;
     CUDA_TRY(cudaMemsetAsync(bkt, 0, sizeof(int) * (2 * NBKT + 2), st));
     item_buckets<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj, bkt);
-    bucket_offsets<<<1, 32, 0, st>>>(bkt, kind == 2 ? 0 : SPH_HEAVY_CLASSES);
+    bucket_offsets<<<1, 32, 0, st>>>(bkt, kind == 2 ? 0 : (s->prm.heavy_classes >= 0 ? s->prm.heavy_classes
+                                                                                   : SPH_HEAVY_CLASSES));
     // light items in walk order: per-walk counts (the task arrays are free
     // again once the lists are built) and their scan
     light_counts<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj,
@@ -1294,7 +1295,6 @@ int force_body(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     CUDA_TRY(cudaMemsetAsync(s->lscal.p, 0, sizeof(long long) * L_NI, st));
-    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_ERROR, 0, sizeof(int), st));
     int r = build_tree(s);
     if (r) return r;
     r = density_phase(s, eager);
@@ -1365,6 +1365,30 @@ int check_errors(sph_system *s) {
     return SPH_OK;
 }
 
+// Before a call: the error bits collect every problem of the call's steps.
+int clear_errors(sph_system *s) {
+    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_ERROR, 0, sizeof(int), s->st()));
+    return SPH_OK;
+}
+
+// After a graph replay: lists that filled more than 80% of their capacity
+// send the next call through an eager evaluation, which grows them (graph
+// replays cannot allocate).
+int check_headroom(sph_system *s) {
+    long long lc[L_NI];
+    CUDA_TRY(cudaMemcpyAsync(lc, s->lscal.p, sizeof(lc), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    const int slot[4] = {L_LIST_D, L_LIST_H, L_LIST_G, L_LIST_R};
+    for (int k = 0; k < 4; ++k)
+        if (lc[slot[k]] * 5 > s->lcap[k] * 4) {
+            s->graph_valid = false;
+            s->force_graph_valid = false;
+        }
+    return SPH_OK;
+}
+
+bool capacity_error(int r) { return r == SPH_ERR_CAPACITY; }
+
 }  // namespace
 
 // ============================================================== C ABI
@@ -1385,6 +1409,8 @@ extern "C" void sph_system_params_default(sph_system_params *p) {
     p->max_density_iterations = 8;
     p->use_graph = 1;
     p->quadrupole = 0;
+    p->item_split_nj = ITEM_SPLIT_NJ;
+    p->heavy_classes = SPH_HEAVY_CLASSES;
 }
 
 extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p, sph_system **out) {
@@ -1400,6 +1426,7 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
         return SPH_ERR_INVALID_ARGUMENT;
     }
     cudaSetDevice(ctx->prm.device);
+    ctx->n_systems++;   // released by sph_system_destroy
     if (alloc_all(s)) {
         sph_system_destroy(s);
         return sphrt::set_error(ctx, SPH_ERR_CUDA, "system allocation for %lld particles failed", (long long)n);
@@ -1455,6 +1482,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
     }
     s->items.release(); s->lscal.release(); s->cub_tmp.release(); s->an_buf.release();
     s->h_scal.release(); s->h_dscal.release(); s->h_lscal.release();
+    s->ctx->n_systems--;
     delete s;
     return SPH_OK;
 }
@@ -1572,23 +1600,36 @@ int capture(sph_system *s, bool step, cudaGraphExec_t *exec) {
 extern "C" int sph_system_compute_forces(sph_system *s) {
     if (!s) return SPH_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->ctx->prm.device);
-    int r = SPH_OK;
+    int r = clear_errors(s);
+    if (r) return r;
     if (s->force_graph_precision != s->ctx->prm.precision) s->force_graph_valid = false;
-    if (!s->prm.use_graph || !s->force_graph_valid) {
-        // eager evaluation (sizes the lists); the graph is captured afterwards
-        r = force_body(s, true);
-        if (!r) r = check_errors(s);
-        if (!r && s->prm.use_graph) {
-            r = capture(s, false, &s->force_exec);
-            if (!r) {
-                s->force_graph_valid = true;
-                s->force_graph_precision = s->ctx->prm.precision;
-            }
-        }
-    } else {
+    if (s->prm.use_graph && s->force_graph_valid) {
         const cudaError_t e = cudaGraphLaunch(s->force_exec, s->st());
         if (e != cudaSuccess) return sphrt::cuda_error(s->ctx, e, "cudaGraphLaunch");
         r = check_errors(s);
+        if (!r) r = check_headroom(s);
+        if (capacity_error(r)) {
+            // a list outgrew its buffer during the replay: the evaluation
+            // only changes derived fields and h (which the density iteration
+            // re-converges), so it is repeated eagerly with grown buffers
+            s->graph_valid = false;
+            s->force_graph_valid = false;
+            r = clear_errors(s);
+            if (r) return r;
+        } else {
+            s->last_status = r;
+            return r;
+        }
+    }
+    // eager evaluation (sizes the lists); the graph is captured afterwards
+    r = force_body(s, true);
+    if (!r) r = check_errors(s);
+    if (!r && s->prm.use_graph) {
+        r = capture(s, false, &s->force_exec);
+        if (!r) {
+            s->force_graph_valid = true;
+            s->force_graph_precision = s->ctx->prm.precision;
+        }
     }
     s->last_status = r;
     return r;
@@ -1603,6 +1644,22 @@ extern "C" int sph_system_graph_kernels(sph_system *s, int32_t step, int64_t *ke
     return SPH_OK;
 }
 
+extern "C" int sph_system_set_params(sph_system *s, const sph_system_params *p) {
+    if (!s || !p) return SPH_ERR_INVALID_ARGUMENT;
+    if (p->n_group < 1 || p->n_leaf < 1 || p->n_leaf > sphtree::MAX_LEAF || !(p->theta > 0.0))
+        return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "n_group, n_leaf (1..%d) or theta out of range",
+                                sphtree::MAX_LEAF);
+    if (p->quadrupole && !s->prm.quadrupole)
+        return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT,
+                                "quadrupole needs a system created with it (node moment buffers)");
+    const int use_graph = s->prm.use_graph;
+    s->prm = *p;
+    s->prm.use_graph = use_graph;
+    s->graph_valid = false;
+    s->force_graph_valid = false;
+    return SPH_OK;
+}
+
 extern "C" int sph_system_set_graph(sph_system *s, int32_t use_graph) {
     if (!s) return SPH_ERR_INVALID_ARGUMENT;
     s->prm.use_graph = use_graph ? 1 : 0;
@@ -1613,8 +1670,9 @@ extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
     if (!s || n_steps < 0) return SPH_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->ctx->prm.device);
     cudaStream_t st = s->st();
+    int r = clear_errors(s);
+    if (r) return r;
     for (int k = 0; k < n_steps; ++k) {
-        int r = SPH_OK;
         if (s->graph_precision != s->ctx->prm.precision) s->graph_valid = false;
         if (!s->prm.use_graph || !s->graph_valid) {
             // eager step (sizes lists, then the graph is captured for the next steps)
@@ -1628,11 +1686,24 @@ extern "C" int sph_system_step(sph_system *s, int32_t n_steps) {
             }
         } else {
             CUDA_TRY(cudaGraphLaunch(s->step_exec, st));
-            if (k == n_steps - 1) r = check_errors(s);
+            // errors of replayed steps accumulate; they are read at the end
+            // of the call, or when the lists near their capacity
+            if (k == n_steps - 1 || (k & 15) == 15) {
+                r = check_errors(s);
+                if (!r) r = check_headroom(s);
+            }
         }
         s->steps++;
         s->last_status = r;
-        if (r) return r;
+        if (r) {
+            if (capacity_error(r)) {
+                // the step ran on truncated lists: its state is not valid;
+                // the next call is eager and grows the buffers
+                s->graph_valid = false;
+                s->force_graph_valid = false;
+            }
+            return r;
+        }
     }
     return SPH_OK;
 }

@@ -14,6 +14,7 @@ Differences from the reference, by design:
   * failures raise abi.SPHError instead of assert()/silent corruption.
 """
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -53,9 +54,13 @@ class Context:
         check(lib.sph_context_create(ctypes.byref(p), ctypes.byref(h)), what="sph_context_create")
         self.handle = h
         self.lib = lib
+        self._systems = weakref.WeakSet()
 
     def close(self):
         if getattr(self, "handle", None):
+            # systems on this context go first (they use its stream)
+            for sys_ in list(getattr(self, "_systems", ())):
+                sys_.close()
             self.lib.sph_context_destroy(self.handle)
             self.handle = None
 

@@ -34,7 +34,8 @@ class SystemParams(ctypes.Structure):
     _fields_ = [("n_group", _I32), ("n_leaf", _I32), ("theta", _D), ("G", _D), ("c_dt", _D),
                 ("dt_max", _D), ("dt_min", _D), ("alpha_max", _D), ("alpha_min", _D),
                 ("alphu_max", _D), ("alphu_min", _D), ("ksr_max_mode", _I32),
-                ("max_density_iterations", _I32), ("use_graph", _I32), ("quadrupole", _I32)]
+                ("max_density_iterations", _I32), ("use_graph", _I32), ("quadrupole", _I32),
+                ("item_split_nj", _I32), ("heavy_classes", _I32)]
 
 
 class SystemStats(ctypes.Structure):
@@ -67,6 +68,7 @@ def _declare(lib):
         "sph_system_set_graph": (ctypes.c_int, [_P, _I32]),
         "sph_system_graph_kernels": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_int64)]),
         "sph_system_set_field": (ctypes.c_int, [_P, _I32, _P]),
+        "sph_system_set_params": (ctypes.c_int, [_P, ctypes.POINTER(SystemParams)]),
         "sph_system_get_clock": (ctypes.c_int, [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
                                                 ctypes.POINTER(_D)]),
         "sph_system_set_clock": (ctypes.c_int, [_P, _D, _D, _D, _D]),
@@ -101,6 +103,8 @@ class ParticleSystem:
         check(self.lib.sph_system_create(ctx.handle, self.n, ctypes.byref(self.params), ctypes.byref(h)),
               ctx.handle, "sph_system_create")
         self.handle = h
+        if hasattr(ctx, "_systems"):
+            ctx._systems.add(self)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -136,6 +140,14 @@ class ParticleSystem:
 
     def set_graph(self, on):
         check(self.lib.sph_system_set_graph(self.handle, 1 if on else 0), self.ctx.handle, "set_graph")
+
+    def set_params(self, **params):
+        """Changes run parameters (n_group, theta, item_split_nj, ...)."""
+        for k, v in params.items():
+            if k not in dict(SystemParams._fields_):
+                raise KeyError(k)
+            setattr(self.params, k, v)
+        check(self.lib.sph_system_set_params(self.handle, ctypes.byref(self.params)), self.ctx.handle, "set_params")
 
     def set_field(self, field, data):
         """Host -> device copy of one field in upload order (restart)."""

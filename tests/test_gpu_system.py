@@ -348,3 +348,55 @@ def test_quadrupole_tree_gravity_vs_direct_sum(prec):
     assert err[1][1] < 0.5 * err[0][1], err
     assert err[1][2] < 0.5 * err[0][2], err
     assert err[1][0] < 1e-3, err
+
+
+def test_autotune_and_set_params():
+    """The autotuner only reshapes the GPU work: densities after tuning match
+    the default parameters' within FP32 summation-order rounding, and it
+    never returns a configuration slower than the one it started from."""
+    from research_codes_gb300 import autotune
+    s = _two_stars(n=6000)
+    n = len(s["mass"])
+    with functors.Context(eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, n, n_group=64)
+        sys.upload(s)
+        for _ in range(3):
+            sys.compute_forces()
+        h0 = sys.download("ksr")
+        sys.compute_forces()
+        d0 = sys.download("dens")
+        best, table = autotune.autotune(sys, candidates={"n_group": (32, 64, 128), "item_split_nj": (256, 4096),
+                                                         "heavy_classes": (0, 2)}, reps=2)
+        start = [ms for p, ms in table if p == {"n_group": 64, "item_split_nj": 4096, "heavy_classes": 2}]
+        assert start and min(ms for _, ms in table) <= start[0]
+        assert all(getattr(sys.params, k) == v for k, v in best.items())
+        # the same evaluation (same first guess of h) under the tuned parameters
+        sys.set_field("ksr", h0)
+        sys.compute_forces()
+        rel = np.abs(sys.download("dens") - d0) / d0
+        assert np.median(rel) < 1e-6 and np.quantile(rel, 0.999) < 1e-4, (np.median(rel), rel.max())
+        with pytest.raises(abi.SPHError):
+            sys.set_params(n_leaf=99)
+        sys.close()
+
+
+def test_graph_replay_recovers_from_list_overflow():
+    """A captured force evaluation whose lists outgrow their buffers (search
+    radii tripled behind the graph's back) is repeated eagerly with grown
+    buffers instead of returning truncated results."""
+    s = _star(n=4000, seed=3)
+    n = len(s["mass"])
+    with functors.Context(eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, n, n_group=64)
+        sys.upload(s)
+        sys.compute_forces()
+        sys.compute_forces()            # captured, replays from now on
+        before = sys.stats()["list_density"]
+        sys.set_field("ksr", sys.download("ksr") * 3.0)
+        sys.compute_forces()            # overflows during the replay, then recovers
+        st = sys.stats()
+        assert st["last_status"] == 0 and st["list_density"] > before
+        assert np.all(np.isfinite(sys.download("dens"))) and np.all(sys.download("np") > 0)
+        sys.compute_forces()
+        assert sys.stats()["last_status"] == 0
+        sys.close()
