@@ -163,17 +163,14 @@ def run_ours(args):
     from research_codes_gb300 import functors, ic
     from research_codes_gb300.system import ParticleSystem, state_from_ic
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from research_codes_gb300 import replicas
+    world, rank, local = replicas.rank_info()
     torch.cuda.set_device(local)
+    replicas.init("nccl", torch.device("cuda", local))
 
     global ETA
     t_ic = time.time()
-    s, ETA = ic.config_system(args.config, scale=args.scale, seed=args.seed + rank)
+    s, ETA = ic.config_system(args.config, scale=args.scale, seed=replicas.replica_seed(args.seed, rank))
     s = state_from_ic(s)
     n = len(s["mass"])
     log(f"[bench] rank {rank}: {args.config} n={n} ic {time.time() - t_ic:.1f}s")
@@ -203,8 +200,7 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -213,19 +209,15 @@ def run_ours(args):
     e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     st = ps.stats()
     pairs = {"density": st["pairs_density"], "hydro": st["pairs_hydro"], "gravity": st["pairs_gravity"]}
     inter = sum(pairs.values())
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    # every rank evolves its own replica: the job's pairs over the slowest rank
+    value, ms = replicas.aggregate_rate(inter, ms, args.steps, device="cuda")
     ms_step = ms / args.steps
-    value = world * inter * args.steps / (ms * 1e-3)
     log(f"[bench] {ms_step:.2f} ms/step, {inter:.3e} pairs/step, iters {st['density_iterations']}")
 
     # ---- per-kernel durations: CUDA events on the engine's stream around each
@@ -402,8 +394,7 @@ def run_ours(args):
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finalize()
 
 
 # ------------------------------------------------------------------ reference arm
