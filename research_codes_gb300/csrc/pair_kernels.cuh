@@ -131,6 +131,10 @@ density_kernel(const DensityArgs a) {
     __shared__ R4 s_v[WARPS][64];
     __shared__ float2 s_vl[WARPS][64];
     __shared__ long long s_id[WARPS][64];
+    // FP32C density passes: the same ring as a structure of arrays, so that
+    // two consecutive entries load as one f32x2 operand
+    __shared__ __align__(16) float s_rx[F64 ? 1 : WARPS][64], s_ry[F64 ? 1 : WARPS][64],
+        s_rz[F64 ? 1 : WARPS][64], s_rm[F64 ? 1 : WARPS][64];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
@@ -232,7 +236,14 @@ density_kernel(const DensityArgs a) {
                 const unsigned m = __ballot_sync(FULL, keep);
                 if (keep) {
                     const int slot = (head + fill + __popc(m & lt)) & 63;
-                    s_p[wid][slot] = p4;
+                    if (!F64 && !with_v) {
+                        s_rx[wid][slot] = (float)p4.x;
+                        s_ry[wid][slot] = (float)p4.y;
+                        s_rz[wid][slot] = (float)p4.z;
+                        s_rm[wid][slot] = (float)p4.w;
+                    } else {
+                        s_p[wid][slot] = p4;
+                    }
                     if (with_v) {
                         if constexpr (F64) {
                             s_v[wid][slot] = Real<F64>::make4((R)cur.v.x, (R)cur.v.y, (R)cur.v.z, (R)0);
@@ -265,8 +276,13 @@ density_kernel(const DensityArgs a) {
             R part = 0;
             // rho pair term m_j W0(q)/c0; neighbour count only in the last
             // pass (the only np the reference stores, :297)
-            auto pair = [&](const R4 *tile, int k, bool count) {
-                const R4 pj = tile[k];
+            auto pair = [&](int k, bool count) {
+                R4 pj;
+                if constexpr (F64) {
+                    pj = s_p[wid][k];
+                } else {
+                    pj = Real<F64>::make4(s_rx[wid][k], s_ry[wid][k], s_rz[wid][k], s_rm[wid][k]);
+                }
                 const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
                 const R r2 = dx * dx + dy * dy + dz * dz;
                 const R q = sqrt_q(r2, hinv2);
@@ -275,19 +291,48 @@ density_kernel(const DensityArgs a) {
                 part += pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
                 if (count) cnt += (q < (R)1) ? 1 : 0;
             };
+            // full FP32C tile: two entries per instruction (f32x2); even and
+            // odd entries summed apart and combined at the end of the tile
+            auto run_packed = [&](int head, bool count) {
+                const f2 XI = f2_make((float)xi, (float)xi), YI = f2_make((float)yi, (float)yi);
+                const f2 ZI = f2_make((float)zi, (float)zi), H2 = f2_make((float)hinv2, (float)hinv2);
+                const f2 NEG = f2_make(-1.0f, -1.0f), ONE = f2_make(1.0f, 1.0f), FOUR = f2_make(4.0f, 4.0f);
+                f2 PART = f2_make(0.0f, 0.0f);
+                int c2 = 0;
+#pragma unroll 4
+                for (int k = 0; k < 32; k += 2) {
+                    const f2 DX = f2_fma(f2_lds(&s_rx[wid][head + k]), NEG, XI);
+                    const f2 DY = f2_fma(f2_lds(&s_ry[wid][head + k]), NEG, YI);
+                    const f2 DZ = f2_fma(f2_lds(&s_rz[wid][head + k]), NEG, ZI);
+                    const float2 x2 = f2_get(f2_mul(f2_fma(DZ, DZ, f2_fma(DY, DY, f2_mul(DX, DX))), H2));
+                    float q0, q1;
+                    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(q0) : "f"(x2.x));
+                    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(q1) : "f"(x2.y));
+                    const f2 Q = f2_make(q0, q1);
+                    const float2 u = f2_get(f2_fma(Q, NEG, ONE));
+                    const f2 U = f2_make(max0(u.x), max0(u.y));
+                    const f2 U2 = f2_mul(U, U);
+                    PART = f2_fma(f2_lds(&s_rm[wid][head + k]), f2_mul(f2_mul(U2, U2), f2_fma(Q, FOUR, ONE)), PART);
+                    if (count) c2 += (q0 < 1.0f ? 1 : 0) + (q1 < 1.0f ? 1 : 0);
+                }
+                const float2 ps = f2_get(PART);
+                part = (R)(ps.x + ps.y);
+                cnt += c2;
+            };
             auto run = [&](int head, int n) {
-                const R4 *tile = &s_p[wid][head];
                 part = 0;
-                if (tpi == 1 && n == 32) {
+                if (!F64 && tpi == 1 && n == 32) {
+                    run_packed(head, pass == 2);
+                } else if (tpi == 1 && n == 32) {
                     if (pass == 2) {
 #pragma unroll 8
-                        for (int k = 0; k < 32; ++k) pair(tile, k, true);
+                        for (int k = 0; k < 32; ++k) pair(head + k, true);
                     } else {
 #pragma unroll 8
-                        for (int k = 0; k < 32; ++k) pair(tile, k, false);
+                        for (int k = 0; k < 32; ++k) pair(head + k, false);
                     }
                 } else {
-                    for (int k = sub; k < n; k += tpi) pair(tile, k, pass == 2);
+                    for (int k = sub; k < n; k += tpi) pair(head + k, pass == 2);
                 }
                 acc.add(part);
                 __syncwarp();
