@@ -246,10 +246,10 @@ int sph_calc_gravity_sp(sph_context *ctx,
                         sph_Gravity *force);
 
 /* Allocation-free variant of sph_calc_gravity_ep for callers that cannot
- * allocate device memory: code recording a CUDA graph (cudaMalloc cannot be
- * captured), host callbacks and library hooks that may not synchronise the
- * device, runtimes that own all device memory through a fixed arena.  No
- * counterpart in the reference.
+ * allocate device memory: host callbacks and library hooks that may not
+ * synchronise the device (an allocation can), runtimes that own all device
+ * memory through a fixed arena, loops that cannot afford an allocation's
+ * latency or failure in mid-run.  No counterpart in the reference.
  *
  * epi, epj and force are DEVICE pointers owned by the caller; the work is
  * queued on `stream` (a cudaStream_t, NULL = default stream) and the call

@@ -1,11 +1,11 @@
 // noalloc.cu — sph_calc_gravity_ep_noalloc: the gravity functor for callers
 // that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code running while a stream is being
-// captured into a CUDA graph (allocation is not a capturable operation),
-// code inside a host callback or a library hook that may not synchronise the
-// device, and embedded runtimes that own all device memory through a fixed
-// arena.  Such a caller still has its input and output buffers in device
+// Some callers cannot call cudaMalloc: code inside a host callback or a
+// library hook that may not synchronise the device (an allocation can
+// synchronise it), embedded runtimes that own all device memory through a
+// fixed arena, and loops that cannot afford an allocation's latency or its
+// failure in mid-run.  Such a caller still has its input and output buffers in device
 // memory.  This entry point works on those buffers and keeps its own scratch
 // (the FP32 double-float records, the per-particle results before they are
 // added to the caller's forces, the work items and the work-queue counter) in

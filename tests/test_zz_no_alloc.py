@@ -1,7 +1,8 @@
 """The allocation-free gravity entry point (sph_calc_gravity_ep_noalloc).
 
-Callers that cannot allocate device memory (graph capture, host callbacks,
-fixed-arena runtimes) pass device buffers they already own; the entry point
+Callers that cannot allocate device memory (host callbacks that may not
+synchronise the device, fixed-arena runtimes) pass device buffers they
+already own; the entry point
 keeps its scratch in a static device array of the library.  This test calls it
 through the C ABI with device buffers made by torch (the test may allocate;
 the entry point does not), twice in a row with different inputs, and compares
