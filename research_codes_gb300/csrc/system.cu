@@ -74,13 +74,22 @@ __global__ void __launch_bounds__(RED_THREADS) reduce_stage1(int n, F f, double 
     if (threadIdx.x < F::K) partial[blockIdx.x * MAX_RED + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// One warp per value: lane l combines partials l, l+32, ... in order, then a
+// fixed shuffle tree combines the lanes (the same order on every run).
+template <class Op>
+__device__ __forceinline__ double warp_combine(const double *partial, int nb, int k, int lane) {
+    double a = Op::identity();
+    for (int b = lane; b < nb; b += 32) a = Op::op(a, partial[b * MAX_RED + k]);
+    for (int o = 16; o > 0; o >>= 1) a = Op::op(a, __shfl_xor_sync(0xffffffffu, a, o));
+    return a;
+}
+
 template <class F>
 __global__ void reduce_stage2(const double *partial, int nb, double *out) {
-    const int k = threadIdx.x;
+    const int k = threadIdx.x >> 5;
     if (k >= F::K) return;
-    double a = F::identity();
-    for (int b = 0; b < nb; ++b) a = F::op(a, partial[b * MAX_RED + k]);
-    out[k] = a;
+    const double a = warp_combine<F>(partial, nb, k, threadIdx.x & 31);
+    if ((threadIdx.x & 31) == 0) out[k] = a;
 }
 
 struct SumOp {
@@ -250,12 +259,17 @@ __global__ void bbox_stage1(const dbl4 *pos, int n, double *partial) {
     if (threadIdx.x < 6) partial[blockIdx.x * MAX_RED + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+struct MaxOp {
+    __device__ static double identity() { return -1.0e300; }
+    __device__ static double op(double a, double b) { return fmax(a, b); }
+};
+
 __global__ void bbox_stage2(const double *partial, int nb, double *box) {
-    const int k = threadIdx.x;
+    const int k = threadIdx.x >> 5;
     if (k >= 6) return;
-    double a = (k < 3) ? 1e300 : -1e300;
-    for (int b = 0; b < nb; ++b) a = (k < 3) ? fmin(a, partial[b * MAX_RED + k]) : fmax(a, partial[b * MAX_RED + k]);
-    box[k] = a;
+    const double a = (k < 3) ? warp_combine<MinOp>(partial, nb, k, threadIdx.x & 31)
+                             : warp_combine<MaxOp>(partial, nb, k, threadIdx.x & 31);
+    if ((threadIdx.x & 31) == 0) box[k] = a;
 }
 
 struct Persist {          // state carried across steps (permuted on each re-sort)
@@ -913,7 +927,7 @@ int exclusive_scan(sph_system *s, const int *in, int *out, int count = -1) {
 template <class F>
 void reduce(sph_system *s, F f, double *out) {
     reduce_stage1<F><<<RED_BLOCKS, RED_THREADS, 0, s->st()>>>(s->n, f, s->partial.p);
-    reduce_stage2<F><<<1, 32, 0, s->st()>>>(s->partial.p, RED_BLOCKS, out);
+    reduce_stage2<F><<<1, 32 * F::K, 0, s->st()>>>(s->partial.p, RED_BLOCKS, out);
 }
 
 // Morton sort + permutation + radix tree + refit + groups.
@@ -933,6 +947,7 @@ int refit_tree(sph_system *s) {
             s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
         sphtree::refit_top<false><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
     }
+    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t);
     return SPH_OK;
 }
 
@@ -942,7 +957,7 @@ int build_tree(sph_system *s) {
     cudaStream_t st = s->st();
     cudaEventRecord(s->ev[EV_TREE_B], st);
     bbox_stage1<<<RED_BLOCKS, RED_THREADS, 0, st>>>(s->pos[0].p, n, s->partial.p);
-    bbox_stage2<<<1, 32, 0, st>>>(s->partial.p, RED_BLOCKS, s->box.p);
+    bbox_stage2<<<1, 32 * 6, 0, st>>>(s->partial.p, RED_BLOCKS, s->box.p);
     sphtree::morton_keys<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, n, s->box.p, s->keys[0].p, s->perm[0].p);
     cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
     cub::DoubleBuffer<int> vb(s->perm[0].p, s->perm[1].p);

@@ -164,36 +164,55 @@ __device__ __forceinline__ NodeData leaf_data(const dbl4 &x, double h, double ep
     return d;
 }
 
-// Writes a node: FP32 boxes with the side length (rounded up), the monopole
-// (centre of mass, mass; mass-weighted eps^2) in FP64 and its FP32 copy.
+// Writes an internal node during the climb: FP32 boxes with the side length
+// (rounded up) and the monopole still as unnormalised sums (sum m x, sum m;
+// sum m eps^2), so that no division sits on the climb's critical path;
+// normalise_nodes turns them into centre of mass and mean eps^2 afterwards.
 __device__ __forceinline__ void store_node(const Nodes &t, int node, const NodeData &d) {
     const float size = fmaxf(fmaxf(__fsub_ru(d.fhi.x, d.flo.x), __fsub_ru(d.fhi.y, d.flo.y)),
                              __fsub_ru(d.fhi.z, d.flo.z));
     t.flo[node] = d.flo;
     t.fhi[node] = make_float4(d.fhi.x, d.fhi.y, d.fhi.z, size);
-    dbl4 m;
-    double e2;
-    if (d.sm.w > 0.0) {
-        const double mi = 1.0 / d.sm.w;
-        m = make_dbl4(d.sm.x * mi, d.sm.y * mi, d.sm.z * mi, d.sm.w);
-        e2 = d.se * mi;
-    } else {
-        m = make_dbl4(0.5 * ((double)d.flo.x + d.fhi.x), 0.5 * ((double)d.flo.y + d.fhi.y),
-                      0.5 * ((double)d.flo.z + d.fhi.z), 0.0);
-        e2 = 0.0;
-    }
-    t.mom[node] = m;
-    t.eps2[node] = e2;
-    t.fmom[node] = make_float4((float)m.x, (float)m.y, (float)m.z, (float)m.w);
+    t.mom[node] = d.sm;
+    t.eps2[node] = d.se;
 }
 
-// A node written by another SM, back as refit data (L1 bypassed).
-__device__ __forceinline__ NodeData load_node_cg(const Nodes &t, int node) {
+// Centre of mass, mass-weighted eps^2 and the FP32 copy of the internal
+// nodes from their sums (leaves hold the particle's own values).
+__global__ void normalise_nodes(int n, Nodes t) {
+    for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < n - 1; node += gridDim.x * blockDim.x) {
+        const dbl4 s = t.mom[node];
+        dbl4 m;
+        double e2;
+        if (s.w > 0.0) {
+            const double mi = 1.0 / s.w;
+            m = make_dbl4(s.x * mi, s.y * mi, s.z * mi, s.w);
+            e2 = t.eps2[node] * mi;
+        } else {
+            const float4 lo = t.flo[node], hi = t.fhi[node];
+            m = make_dbl4(0.5 * ((double)lo.x + hi.x), 0.5 * ((double)lo.y + hi.y), 0.5 * ((double)lo.z + hi.z),
+                          0.0);
+            e2 = 0.0;
+        }
+        t.mom[node] = m;
+        t.eps2[node] = e2;
+        t.fmom[node] = make_float4((float)m.x, (float)m.y, (float)m.z, (float)m.w);
+    }
+}
+
+// A node written by another SM, back as refit data (L1 bypassed): leaves
+// hold (x, m) and eps^2, internal nodes the sums of the climb.
+__device__ __forceinline__ NodeData load_node_cg(const Nodes &t, int node, int n) {
     NodeData d;
     const double2 *q = reinterpret_cast<const double2 *>(&t.mom[node]);
     const double2 a = __ldcg(q), b = __ldcg(q + 1);
-    d.sm = make_dbl4(b.y * a.x, b.y * a.y, b.y * b.x, b.y);
-    d.se = b.y * __ldcg(&t.eps2[node]);
+    if (node >= n - 1) {
+        d.sm = make_dbl4(b.y * a.x, b.y * a.y, b.y * b.x, b.y);
+        d.se = b.y * __ldcg(&t.eps2[node]);
+    } else {
+        d.sm = make_dbl4(a.x, a.y, b.x, b.y);
+        d.se = __ldcg(&t.eps2[node]);
+    }
     d.flo = __ldcg(&t.flo[node]);
     d.fhi = __ldcg(&t.fhi[node]);
     return d;
@@ -346,7 +365,7 @@ __global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots) 
                          : "=r"(arrived) : "l"(&t.visit[node]) : "memory");
             if (arrived == 0) break;   // sibling not finished yet
             const int2 ch = t.child[node];
-            const NodeData da = load_node_cg(t, ch.x), db = load_node_cg(t, ch.y);
+            const NodeData da = load_node_cg(t, ch.x, n), db = load_node_cg(t, ch.y, n);
             if (QUAD) store_quad(t, node, combine_quad(da, load_quad_cg(t, ch.x), db, load_quad_cg(t, ch.y)));
             store_node(t, node, combine(da, db));
             node = t.parent[node];
