@@ -341,6 +341,12 @@ typedef struct sph_system_params {
                             cut into work items of 16, 8 or 4 i-particles (<= 0: 4096) */
     int32_t heavy_classes; /* work items of this many most expensive cost classes run
                             first, the rest in walk order (< 0: 2)                      */
+    float   density_list_slack; /* radius of the density kernel's per-lane neighbour
+                            lists over each particle's first-pass h (default 1.03): the
+                            first pass writes them, the later passes and the gradient
+                            pass read them while h stays within it; <= 0 or NaN: no
+                            lists, every pass streams the walk's j-list; above 2 the
+                            create / set_params calls fail with INVALID_ARGUMENT       */
 } sph_system_params;
 
 /* Fields for sph_system_download / sph_system_download_sorted. */
@@ -376,6 +382,10 @@ typedef struct sph_system_stats {
     int64_t evals_hydro_near;             /* hydro pairs evaluated in full        */
     int64_t evals_hydro_far;              /* hydro pairs beyond both supports,
                                              signal velocity only                */
+    int64_t density_list_passes;          /* first walk: work-item passes after
+                                             the first (second, third, gradient)
+                                             served from neighbour lists         */
+    int64_t density_sweep_passes;         /* ... that swept the walk's j-list     */
     int32_t last_status;
 } sph_system_stats;
 

@@ -575,7 +575,7 @@ extern "C" int sph_dispatch_density(sph_context *ctx, int32_t tag, int32_t n_wal
         sphk::make_density_records<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(nj, ks.a4[2].p, ks.a4[3].p, ks.f4[4].p,
                                                                              ks.f4[5].p, ks.f4[6].p, ks.f4[7].p);
     if (!ks.items.empty()) {
-        sphk::DensityArgs a;
+        sphk::DensityArgs a{};
         a.n_eval = nullptr;
         a.i_pm = ks.a4[0].p; a.i_vel = ks.a4[1].p; a.i_id = ks.id[0].p; a.i_ksr = ks.d1[0].p; a.i_rs = ks.d1[1].p;
         a.j_pm = ks.a4[2].p; a.j_vel = ks.a4[3].p; a.j_id = ks.id[1].p;
@@ -680,7 +680,7 @@ extern "C" int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
             nj, ks.a4[2].p, ks.a4[3].p, ks.a4[6].p, ks.a4[7].p, ks.a2[1].p, ks.f4[4].p, ks.f4[5].p, ks.f4[6].p,
             ks.f4[7].p, ks.f4[11].p, ks.f4[12].p, ks.f4[13].p);
     if (!ks.items.empty()) {
-        sphk::HydroArgs a;
+        sphk::HydroArgs a{};
         a.n_eval_near = nullptr;
         a.n_eval_far = nullptr;
         a.i_pm = ks.a4[0].p; a.i_vel = ks.a4[1].p; a.i_id = ks.id[0].p;
@@ -761,7 +761,7 @@ extern "C" int sph_dispatch_gravity(sph_context *ctx, int32_t tag, int32_t n_wal
         sphk::make_gravity_records<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(nj, ks.a4[2].p, ks.d1[0].p, ks.f4[4].p,
                                                                              ks.f4[5].p);
     if (!ks.items.empty()) {
-        sphk::GravityArgs a;
+        sphk::GravityArgs a{};
         a.i_pe = ks.a4[0].p;
         a.j_pm = ks.a4[2].p; a.j_eps2 = ks.d1[0].p;
         a.s_pm = ks.a4[2].p; a.s_eps2 = ks.d1[0].p;

@@ -28,7 +28,7 @@
 // density, gravity and hydro kernels (register budget 65536 / (128 threads x
 // blocks)).
 #ifndef SPH_DENSITY_MIN_BLOCKS
-#define SPH_DENSITY_MIN_BLOCKS 5
+#define SPH_DENSITY_MIN_BLOCKS 4
 #endif
 #ifndef SPH_GRAVITY_MIN_BLOCKS
 #define SPH_GRAVITY_MIN_BLOCKS 4
@@ -115,11 +115,45 @@ struct DensityArgs {
     int *amb_w;             // its walk
     int amb_cap;
     float amb_tol;
-    // when set: pair evaluations performed (j-entries kept by the support
-    // test x i-particles): [0] the three density passes, [1] the gradient pass
-    unsigned long long *n_eval;
+    // Per-warp neighbour lists; null: every pass sweeps the walk's j-list.
+    // Warp w of the grid (blockIdx.x * WARPS + warp) owns the int array
+    // nbr[w * nbr_cap * 32, (w + 1) * nbr_cap * 32), entry c of lane l at
+    // [c * 32 + l]; warps w >= nbr_warps sweep.  nbr_slack (> 1) is the list
+    // radius in units of each i-particle's first-pass h.
+    int *nbr = nullptr;
+    int nbr_cap = 0;
+    int nbr_warps = 0;
+    float nbr_slack = 1.0f;
+    // when set: pair evaluations performed, [0] the three density passes
+    // ((j-entries kept by the support test x i-particles) of the swept passes
+    // plus the list entries of the listed ones), [1] the gradient pass
+    unsigned long long *n_eval = nullptr;
+    // when set: [0] item passes (second, third, gradient) served from the
+    // neighbour lists, [1] item passes that swept the walk's j-list
+    unsigned long long *n_pass = nullptr;
 };
 
+template <bool B>
+struct BTag {
+    static constexpr bool value = B;
+};
+
+// The density functor of hdr_density.hpp:252-350 for one work item per warp:
+// three fixed-point passes rho(h) -> h = eta ksrh (m / rho)^(1/3) from the
+// first guess, then the gradient pass (grdh, divv, rotv) with the final h.
+//
+// Every pass can stream the walk's j-list through a shared ring (kept entries
+// of each 32-entry chunk compacted by the item-box support test), which
+// evaluates every kept entry for every i-particle of the item: ~10x more
+// pairs than the kernel support holds.  With neighbour lists the first pass
+// streams the list once with the support widened by nbr_slack and also writes,
+// per lane, the j indices within nbr_slack * (first-pass h) of its
+// i-particle; the second and third passes and the gradient pass then loop over
+// each lane's own list (gathering the j records) whenever every h of the item
+// has stayed within that radius and no lane's list overflowed nbr_cap;
+// otherwise the pass sweeps.  Entries beyond a particle's support add exactly
+// zero in both forms, so the two differ only in the grouping of the FP32
+// partial sums.
 template <bool F64, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_DENSITY_MIN_BLOCKS)
 density_kernel(const DensityArgs a) {
@@ -135,11 +169,22 @@ density_kernel(const DensityArgs a) {
     // two consecutive entries load as one f32x2 operand
     __shared__ __align__(16) float s_rx[F64 ? 1 : WARPS][64], s_ry[F64 ? 1 : WARPS][64],
         s_rz[F64 ? 1 : WARPS][64], s_rm[F64 ? 1 : WARPS][64];
+    __shared__ int s_j[WARPS][64];   // j index of each ring entry (list-building pass)
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
     const int n_items = a.n_items_dev ? *a.n_items_dev : a.n_items;
     const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
+    const int gw = blockIdx.x * WARPS + wid;
+    // this lane's neighbour list: entry c at a.nbr[nlb + c * 32]
+    const bool has_nl = a.nbr != nullptr && gw < a.nbr_warps;
+    const int nlb = has_nl ? gw * a.nbr_cap * 32 + lane : 0;
+    // list radius^2 over (first-pass h)^2, and the largest h (over the
+    // first-pass h) a listed pass accepts: every pair with q < 1 then has r^2
+    // below the list radius with a margin of 2e-5 over the rounding of both
+    // tests
+    const R nl_lim = (R)a.nbr_slack * (R)a.nbr_slack;
+    const double nl_hmax = (double)a.nbr_slack * 0.99998;
 
     for (;;) {
         int item = 0;
@@ -149,37 +194,31 @@ density_kernel(const DensityArgs a) {
         const ItemRef r = decode(a.items[item], a.j_off, a.i_list, lane);
         const int tpi = r.tpi, sub = r.sub, ii = r.ii, nj = r.nj, jb = r.jb;
 
-        // i-particle relative to the centre particle c
-        R xi, yi, zi, vxi, vyi, vzi;
-        float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
+        // i-particle relative to the centre particle c (velocity, id, mass
+        // and search radius are read where they are used, keeping the
+        // registers of the passes free)
+        R xi, yi, zi;
         float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
         if (F64) {
-            const dbl4 p = a.i_pm[ii], v = a.i_vel[ii];
+            const dbl4 p = a.i_pm[ii];
             xi = (R)p.x; yi = (R)p.y; zi = (R)p.z;
-            vxi = (R)v.x; vyi = (R)v.y; vzi = (R)v.z;
         } else {
             cph = a.fi.phi[r.ic]; cpl = a.fi.plo[r.ic];
-            const float4 ph = a.fi.phi[ii], pl = a.fi.plo[ii], vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
+            const float4 ph = a.fi.phi[ii], pl = a.fi.plo[ii];
             xi = (R)df_diff(ph.x, pl.x, cph.x, cpl.x);
             yi = (R)df_diff(ph.y, pl.y, cph.y, cpl.y);
             zi = (R)df_diff(ph.z, pl.z, cph.z, cpl.z);
-            // velocities stay absolute hi/lo pairs and are differenced per
-            // pair: an item may straddle two colliding streams
-            vxi = vh.x; vyi = vh.y; vzi = vh.z;
-            lxi = vl.x; lyi = vl.y; lzi = vl.z;
         }
         // The kernel is zero for r >= h, so a j-particle farther than the
         // largest h of the item from the item's box adds nothing to any sum
         // or count of this item: staging drops it before the pair loop.
         IBox<R> box;
         box.from_lanes(xi, yi, zi);
-        const long long idi = a.i_id[ii];
-        const double rs_i = a.i_rs[ii];
-        const double mi = a.i_pm[ii].w;
         double h = a.i_ksr[ii];
-        double rho = 0.0;
-        long long np = 0;
-        bool itr = false;
+        // largest h a listed pass accepts for this lane
+        const float nl_h = (float)(h * nl_hmax);
+        R rho = 0;
+        int np = 0;
 
         // One j record as loaded from memory (FP32C double-float or FP64).
         struct JRec {
@@ -202,24 +241,43 @@ density_kernel(const DensityArgs a) {
             }
             if (with_v) q.id = a.j_id[j];
         };
+        // position of particle j in the frame of the pair loops (FP32C:
+        // relative to the centre particle; FP64: absolute) and its mass
+        auto jpos = [&](int j) -> R4 {
+            if constexpr (F64) {
+                const dbl4 p = a.j_pm[j];
+                return Real<F64>::make4((R)p.x, (R)p.y, (R)p.z, (R)p.w);
+            } else {
+                const float4 ph = __ldg(&a.fj.phi[j]), pl = __ldg(&a.fj.plo[j]);
+                return Real<F64>::make4(df_diff(ph.x, pl.x, cph.x, cpl.x), df_diff(ph.y, pl.y, cph.y, cpl.y),
+                                        df_diff(ph.z, pl.z, cph.z, cpl.z), ph.w);
+            }
+        };
         // Streams the walk's list through the ring: lane k takes entry t+k,
         // entries that can lie within sqrt(rf2) of the item box are
         // compacted into the ring, and consume(base, n) runs whenever 32 are
         // ready (and once more for the rest).  Loads run one 32-entry chunk
         // ahead of their use (the list index two chunks ahead) so that their
         // latency overlaps the box test and the pair loops.  with_v also
-        // stages velocities and ids (gradient pass).
-        long long kept = 0;   // j-entries kept by the support test, all passes
-        auto sweep = [&](const R rf2, const bool with_v, auto &&consume) {
+        // stages velocities and ids (gradient pass), with_j the j indices.
+        unsigned kept = 0;   // j-entries kept by the support test, all sweeps
+        auto sweep = [&](const R rf2, const bool with_v, const bool with_j, auto &&consume) {
             int head = 0, fill = 0;
             JRec cur, nxt;
-            int jn = 0;
-            if (lane < nj) load(jlist(lane), with_v, nxt);
+            int jn = 0, jnx = 0;
+            if (lane < nj) {
+                jnx = jlist(lane);
+                load(jnx, with_v, nxt);
+            }
             if (32 + lane < nj) jn = jlist(32 + lane);
             for (int t = 0; t < nj; t += 32) {
                 cur = nxt;
+                const int jc = jnx;
                 const bool valid = t + lane < nj;
-                if (t + 32 + lane < nj) load(jn, with_v, nxt);
+                if (t + 32 + lane < nj) {
+                    jnx = jn;
+                    load(jn, with_v, nxt);
+                }
                 if (t + 64 + lane < nj) jn = jlist(t + 64 + lane);
                 bool keep = false;
                 R4 p4;
@@ -253,6 +311,7 @@ density_kernel(const DensityArgs a) {
                         }
                         s_id[wid][slot] = cur.id;
                     }
+                    if (with_j) s_j[wid][slot] = jc;
                 }
                 fill += __popc(m);
                 kept += __popc(m);
@@ -266,45 +325,76 @@ density_kernel(const DensityArgs a) {
             if (fill > 0) consume(head, fill);
         };
 
+        // neighbour list of this lane: its length (above nbr_cap the list is
+        // unusable), appended by the first pass from the ring
+        int ncnt = 0;
+        bool nl_ok = false;
+        unsigned ev_list = 0, ev_list_g = 0;   // list entries evaluated (this lane)
+        int n_listed = 0;                      // of the 3 item passes after the first
+        auto nl_push = [&](int head, unsigned msk) {
+            while (msk) {
+                const int k = __ffs(msk) - 1;
+                msk &= msk - 1;
+                if (ncnt < a.nbr_cap) a.nbr[nlb + ncnt * 32] = s_j[wid][head + k];
+                ++ncnt;
+            }
+        };
+
         // three fixed-point passes, hdr_density.hpp:264-302
         for (int pass = 0; pass < 3; ++pass) {
             const R hinv = (R)1 / (R)h;
             const R hinv2 = hinv * hinv;
-            const R rf2 = support2<R>(h);
+            const bool build = has_nl && pass == 0;
+            const bool listed = pass > 0 && nl_ok && __all_sync(FULL, (float)h <= nl_h);
             Acc<F64> acc;
             int cnt = 0;
             R part = 0;
             // rho pair term m_j W0(q)/c0; neighbour count only in the last
             // pass (the only np the reference stores, :297)
-            auto pair = [&](int k, bool count) {
+            auto term = [&](const R4 pj, bool count) -> R {
+                const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                const R q = sqrt_q(r2, hinv2);
+                const R u = max0((R)1 - q);
+                const R u2 = u * u;
+                if (count) cnt += (q < (R)1) ? 1 : 0;
+                return pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
+            };
+            // ring entry k; with mark set, bit k of *mark flags an entry
+            // within the list radius
+            auto pair = [&](int k, bool count, unsigned *mark) {
                 R4 pj;
                 if constexpr (F64) {
                     pj = s_p[wid][k];
                 } else {
                     pj = Real<F64>::make4(s_rx[wid][k], s_ry[wid][k], s_rz[wid][k], s_rm[wid][k]);
                 }
-                const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                const R r2 = dx * dx + dy * dy + dz * dz;
-                const R q = sqrt_q(r2, hinv2);
-                const R u = max0((R)1 - q);
-                const R u2 = u * u;
-                part += pj.w * (u2 * u2 * ((R)1 + (R)4 * q));
-                if (count) cnt += (q < (R)1) ? 1 : 0;
+                part += term(pj, count);
+                if (mark) {
+                    const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+                    if ((dx * dx + dy * dy + dz * dz) * hinv2 < nl_lim) *mark |= 1u << (k & 31);
+                }
             };
             // full FP32C tile: two entries per instruction (f32x2); even and
-            // odd entries summed apart and combined at the end of the tile
-            auto run_packed = [&](int head, bool count) {
+            // odd entries summed apart and combined at the end of the tile;
+            // the list-building form also flags the entries within the list
+            // radius
+            auto run_packed = [&](int head, bool count, auto build_tag) {
+                constexpr bool B = decltype(build_tag)::value;
                 const f2 XI = f2_make((float)xi, (float)xi), YI = f2_make((float)yi, (float)yi);
                 const f2 ZI = f2_make((float)zi, (float)zi), H2 = f2_make((float)hinv2, (float)hinv2);
                 const f2 NEG = f2_make(-1.0f, -1.0f), ONE = f2_make(1.0f, 1.0f), FOUR = f2_make(4.0f, 4.0f);
+                const float lim = (float)nl_lim;
                 f2 PART = f2_make(0.0f, 0.0f);
                 int c2 = 0;
+                unsigned msk = 0;
 #pragma unroll 4
                 for (int k = 0; k < 32; k += 2) {
                     const f2 DX = f2_fma(f2_lds(&s_rx[wid][head + k]), NEG, XI);
                     const f2 DY = f2_fma(f2_lds(&s_ry[wid][head + k]), NEG, YI);
                     const f2 DZ = f2_fma(f2_lds(&s_rz[wid][head + k]), NEG, ZI);
                     const float2 x2 = f2_get(f2_mul(f2_fma(DZ, DZ, f2_fma(DY, DY, f2_mul(DX, DX))), H2));
+                    if constexpr (B) msk |= (x2.x < lim ? 1u << k : 0u) | (x2.y < lim ? 2u << k : 0u);
                     float q0, q1;
                     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(q0) : "f"(x2.x));
                     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(q1) : "f"(x2.y));
@@ -318,46 +408,81 @@ density_kernel(const DensityArgs a) {
                 const float2 ps = f2_get(PART);
                 part = (R)(ps.x + ps.y);
                 cnt += c2;
+                if constexpr (B) nl_push(head, msk);
             };
             auto run = [&](int head, int n) {
                 part = 0;
                 if (!F64 && tpi == 1 && n == 32) {
-                    run_packed(head, pass == 2);
-                } else if (tpi == 1 && n == 32) {
-                    if (pass == 2) {
-#pragma unroll 8
-                        for (int k = 0; k < 32; ++k) pair(head + k, true);
-                    } else {
-#pragma unroll 8
-                        for (int k = 0; k < 32; ++k) pair(head + k, false);
-                    }
+                    if (build)
+                        run_packed(head, false, BTag<true>());
+                    else
+                        run_packed(head, pass == 2, BTag<false>());
                 } else {
-                    for (int k = sub; k < n; k += tpi) pair(head + k, pass == 2);
+                    unsigned msk = 0;
+                    unsigned *mark = build ? &msk : nullptr;
+                    if (tpi == 1 && n == 32) {
+                        if (pass == 2) {
+#pragma unroll 8
+                            for (int k = 0; k < 32; ++k) pair(head + k, true, nullptr);
+                        } else {
+#pragma unroll 8
+                            for (int k = 0; k < 32; ++k) pair(head + k, false, mark);
+                        }
+                    } else {
+                        for (int k = sub; k < n; k += tpi) pair(head + k, pass == 2, mark);
+                    }
+                    if (build) nl_push(head, msk);
                 }
                 acc.add(part);
                 __syncwarp();
             };
-            sweep(rf2, false, run);
+            if (listed) {
+                // this lane's list, four entries per round (gathers first)
+                const int cmax = (int)__reduce_max_sync(FULL, (unsigned)ncnt);
+                for (int c0 = 0; c0 < cmax; c0 += 4) {
+                    int jj[4];
+                    R4 pj[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) jj[u] = (c0 + u < ncnt) ? a.nbr[nlb + (c0 + u) * 32] : -1;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (jj[u] >= 0) pj[u] = jpos(jj[u]);
+                    part = 0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (jj[u] >= 0) part += term(pj[u], pass == 2);
+                    acc.add(part);
+                }
+                if (r.act) ev_list += (unsigned)ncnt;
+                ++n_listed;
+            } else {
+                const R rf2 = support2<R>(build ? h * (double)a.nbr_slack : h);
+                sweep(rf2, false, build, run);
+            }
+            if (build) nl_ok = __all_sync(FULL, ncnt <= a.nbr_cap);
             const double sum = seg_sum(acc.value(), tpi);
-            const long long c = seg_sum((long long)cnt, tpi);
+            const int c = (int)seg_sum((long long)cnt, tpi);
+            const double mi = a.i_pm[ii].w;
             double hn;
             if (F64) {
                 const double hinv_d = 1.0 / h;
-                rho = CEFF0 * hinv_d * hinv_d * hinv_d * sum;
-                hn = a.eta_ksrh * cbrt(mi / rho);
+                rho = (R)(CEFF0 * hinv_d * hinv_d * hinv_d * sum);
+                hn = a.eta_ksrh * cbrt(mi / (double)rho);
             } else {
                 // FP32 per-particle update (relative error ~1e-7, far inside
                 // the 1e-5 budget) keeps the FP64 pipe out of the loop
                 const float hinv_f = (float)hinv;
                 const float rho_f = (float)CEFF0 * hinv_f * hinv_f * hinv_f * (float)sum;
-                rho = (double)rho_f;
+                rho = (R)rho_f;
                 hn = (double)((float)a.eta_ksrh * cbrtf((float)mi / rho_f));
             }
             hn = (hn < ksr_max) ? hn : ksr_max;
             np = c;
-            itr = hn > rs_i;
             h = hn;
         }
+        // the search-radius decision of the last pass (hdr_density.hpp:299)
+        const double rs_i = a.i_rs[ii];
+        const bool itr = h > rs_i;
         if (!F64 && a.amb_count && r.act && sub == 0 && fabs(h - rs_i) <= (double)a.amb_tol * rs_i) {
             const int k = atomicAdd(a.amb_count, 1);
             if (k < a.amb_cap) {
@@ -366,26 +491,37 @@ density_kernel(const DensityArgs a) {
             }
         }
 
-        const long long kept_rho = kept;
+        const unsigned kept_rho = kept;
         // gradient pass with the final h, hdr_density.hpp:304-349
         {
+            const long long idi = a.i_id[ii];
+            R vxi, vyi, vzi;
+            float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
+            if (F64) {
+                const dbl4 v = a.i_vel[ii];
+                vxi = (R)v.x; vyi = (R)v.y; vzi = (R)v.z;
+            } else {
+                // velocities stay absolute hi/lo pairs and are differenced
+                // per pair: an item may straddle two colliding streams
+                const float4 vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
+                vxi = vh.x; vyi = vh.y; vzi = vh.z;
+                lxi = vl.x; lyi = vl.y; lzi = vl.z;
+            }
             const R hinv = (R)1 / (R)h;
-            const R rf2 = support2<R>(h);
             Acc<F64> g_acc, d_acc, rx_acc, ry_acc, rz_acc;
             R pg = 0, pd = 0, prx = 0, pry = 0, prz = 0;
-            auto pair = [&](int k) {
-                const R4 pj = s_p[wid][k];
-                const R4 vj = s_v[wid][k];
+            // pair terms; (vx, vy, vz) the j velocity (FP32C: hi parts, with
+            // the lo parts (lx, ly, lz) differenced apart)
+            auto gpair = [&](const R4 pj, R vx, R vy, R vz, float lx, float ly, float lz, long long idj) {
                 const R dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-                R ux = vxi - vj.x, uy = vyi - vj.y, uz = vzi - vj.z;
+                R ux = vxi - vx, uy = vyi - vy, uz = vzi - vz;
                 if (!F64) {
-                    const float2 vl = s_vl[wid][k];
-                    ux += (R)(lxi - (float)vj.w);
-                    uy += (R)(lyi - vl.x);
-                    uz += (R)(lzi - vl.y);
+                    ux += (R)(lxi - lx);
+                    uy += (R)(lyi - ly);
+                    uz += (R)(lzi - lz);
                 }
                 const R r2 = dx * dx + dy * dy + dz * dz;
-                const R ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
+                const R ri = (idi != idj) ? rsqrt_r(r2) : (R)0;
                 const R q = r2 * ri * hinv;
                 const R u = max0((R)1 - q);
                 const R u2 = u * u;
@@ -400,6 +536,19 @@ density_kernel(const DensityArgs a) {
                 pry += (uz * dx - ux * dz) * dw;
                 prz += (ux * dy - uy * dx) * dw;
             };
+            auto pair = [&](int k) {
+                const R4 vj = s_v[wid][k];
+                const float2 vl = s_vl[wid][k];
+                gpair(s_p[wid][k], vj.x, vj.y, vj.z, (float)vj.w, vl.x, vl.y, s_id[wid][k]);
+            };
+            auto fold = [&]() {
+                g_acc.add(pg);
+                d_acc.add(pd);
+                rx_acc.add(prx);
+                ry_acc.add(pry);
+                rz_acc.add(prz);
+                pg = 0; pd = 0; prx = 0; pry = 0; prz = 0;
+            };
             // Each lane first marks the tile entries inside its own support
             // (r^2/h^2 below 1 + 2e-5, so every pair with q < 1 is marked),
             // then evaluates the gradient terms of the marked entries only, in
@@ -412,7 +561,6 @@ density_kernel(const DensityArgs a) {
                 if (!(r2 * lim >= (R)1)) msk |= 1u << (k & 31);
             };
             auto run = [&](int head, int n) {
-                pg = 0; pd = 0; prx = 0; pry = 0; prz = 0;
                 unsigned msk = 0;
                 if (tpi == 1 && n == 32) {
 #pragma unroll 8
@@ -425,14 +573,46 @@ density_kernel(const DensityArgs a) {
                     msk &= msk - 1;
                     pair(head + k);
                 }
-                g_acc.add(pg);
-                d_acc.add(pd);
-                rx_acc.add(prx);
-                ry_acc.add(pry);
-                rz_acc.add(prz);
+                fold();
                 __syncwarp();
             };
-            sweep(rf2, true, run);
+            if (nl_ok && __all_sync(FULL, (float)h <= nl_h)) {
+                // this lane's list, two entries per round (gathers first)
+                const int cmax = (int)__reduce_max_sync(FULL, (unsigned)ncnt);
+                for (int c0 = 0; c0 < cmax; c0 += 2) {
+                    int jj[2];
+                    R4 pj[2];
+                    R4 vh[2];
+                    float4 vl[2];
+                    long long idj[2];
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) jj[u] = (c0 + u < ncnt) ? a.nbr[nlb + (c0 + u) * 32] : -1;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        if (jj[u] >= 0) {
+                            pj[u] = jpos(jj[u]);
+                            if constexpr (F64) {
+                                const dbl4 v = a.j_vel[jj[u]];
+                                vh[u] = Real<F64>::make4((R)v.x, (R)v.y, (R)v.z, (R)0);
+                                vl[u] = make_float4(0, 0, 0, 0);
+                            } else {
+                                vh[u] = __ldg(&a.fj.vhi[jj[u]]);
+                                vl[u] = __ldg(&a.fj.vlo[jj[u]]);
+                            }
+                            idj[u] = __ldg(&a.j_id[jj[u]]);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        if (jj[u] >= 0) gpair(pj[u], vh[u].x, vh[u].y, vh[u].z, vl[u].x, vl[u].y, vl[u].z, idj[u]);
+                    if ((c0 & 7) == 6) fold();
+                }
+                fold();
+                if (r.act) ev_list_g += (unsigned)ncnt;
+                ++n_listed;
+            } else {
+                sweep(support2<R>(h), true, false, run);
+            }
             const double sg = seg_sum(g_acc.value(), tpi);
             const double sd = seg_sum(d_acc.value(), tpi);
             const double sx = seg_sum(rx_acc.value(), tpi);
@@ -445,7 +625,7 @@ density_kernel(const DensityArgs a) {
                     const double hinv4 = hinv_d * hinv_d * hinv_d * hinv_d;
                     const double grdh = -hinv4 * sg;
                     const double rx = CEFF1 * hinv4 * sx, ry = CEFF1 * hinv4 * sy, rz = CEFF1 * hinv4 * sz;
-                    const double rhoinv = 1.0 / rho;
+                    const double rhoinv = 1.0 / (double)rho;
                     omega = 1.0 / (1.0 + h * rhoinv * grdh / 3.0);
                     const double rot2 = rx * rx + ry * ry + rz * rz;
                     const double rot = (rot2 != 0.0) ? sqrt(rot2) : 0.0;
@@ -465,18 +645,26 @@ density_kernel(const DensityArgs a) {
                     divv = -(float)CEFF1 * hinv4 * (float)sd * rinv * om;
                     rotv = ((rot2 != 0.0f) ? sqrtf(rot2) : 0.0f) * rinv * om;
                 }
-                a.o_dens[ii] = rho;
+                a.o_dens[ii] = (double)rho;
                 a.o_divv[ii] = divv;
                 a.o_rotv[ii] = rotv;
                 a.o_grdh[ii] = omega;
                 a.o_ksr[ii] = h;
-                a.o_np[ii] = np;
+                a.o_np[ii] = (long long)np;
                 a.o_itr[ii] = itr ? 1 : 0;
             }
         }
-        if (a.n_eval && lane == 0) {
-            atomicAdd(a.n_eval, (unsigned long long)kept_rho * (unsigned long long)r.ni);
-            atomicAdd(a.n_eval + 1, (unsigned long long)(kept - kept_rho) * (unsigned long long)r.ni);
+        if (a.n_eval) {
+            const unsigned long long l0 = __reduce_add_sync(FULL, ev_list);
+            const unsigned long long l1 = __reduce_add_sync(FULL, ev_list_g);
+            if (lane == 0) {
+                atomicAdd(a.n_eval, (unsigned long long)kept_rho * (unsigned long long)r.ni + l0);
+                atomicAdd(a.n_eval + 1, (unsigned long long)(kept - kept_rho) * (unsigned long long)r.ni + l1);
+            }
+        }
+        if (a.n_pass && lane == 0) {
+            atomicAdd(a.n_pass, (unsigned long long)n_listed);
+            atomicAdd(a.n_pass + 1, (unsigned long long)(3 - n_listed));
         }
     }
 }

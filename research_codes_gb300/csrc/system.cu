@@ -28,6 +28,12 @@ namespace {
 
 constexpr double KSRH = sphk::KSRH;
 constexpr int ITEM_SPLIT_NJ = 4096;   // default list length above which a walk's items are halved (down to 4 i)
+// density neighbour lists: entries per lane (a lane with more sweeps) and
+// the default list radius over the first-pass h (later passes whose h grew
+// beyond it sweep)
+constexpr int NBR_CAP = 96;
+constexpr float NBR_SLACK = 1.03f;
+constexpr float MAX_NBR_SLACK = 2.0f;
 constexpr int RED_BLOCKS = 296;   // 2 x 148..152 SMs; fixed for deterministic sums
 constexpr int RED_THREADS = 256;
 constexpr int MAX_RED = 8;
@@ -41,7 +47,7 @@ enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN
        D_R2, D_DN, D_NI };
 // 64-bit counters
 enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_EVAL_D1,
-       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_NI };
+       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_DLISTED, L_DSWEPT, L_NI };
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
@@ -793,6 +799,9 @@ struct sph_system {
     DevBuf<int> amb_i, amb_w;
     DevBuf<WorkItem> fitems;
     int amb_cap = 0;
+    // per-warp neighbour lists of the density kernel (scratch)
+    DevBuf<int> nbr;
+    int nbr_warps = 0;
     // groups and walks
     DevBuf<int> gflag, groot, gscan, group_node, group_first, group_count;
     DevBuf<int> aflag, ascan, a_node, a_first, a_count;
@@ -885,6 +894,8 @@ int alloc_all(sph_system *s) {
     e |= s->uflag.ensure(n) | s->uscan.ensure(n) | s->ulist.ensure(n) | s->a_sfirst.ensure(n) | s->a_scount.ensure(n);
     s->amb_cap = std::max<int>(1024, s->n / 16);
     e |= s->amb_i.ensure(s->amb_cap) | s->amb_w.ensure(s->amb_cap) | s->fitems.ensure(s->amb_cap);
+    s->nbr_warps = std::max(s->ctx->grid[0][0], s->ctx->grid[0][1]) * PAIR_WARPS;
+    e |= s->nbr.ensure((size_t)s->nbr_warps * NBR_CAP * 32);
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count};
     for (auto *b : i1) e |= b->ensure(n);
@@ -1052,7 +1063,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
                           int chunk = 32) {
     const int n = s->n;
     cudaStream_t st = s->st();
-    sphtree::ListArgs a;
+    sphtree::ListArgs a{};
     a.t = s->nodes();
     a.n = n;
     a.root = 0;
@@ -1173,8 +1184,14 @@ int density_phase(sph_system *s, bool eager) {
                                   s->a_sfirst.p, s->a_scount.p, it == 0 ? 32 : 8);
         if (r) return r;
         CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
-        sphk::DensityArgs a;
+        sphk::DensityArgs a{};
         a.n_eval = (it == 0) ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_D1) : nullptr;
+        a.n_pass = (it == 0) ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_DLISTED) : nullptr;
+        const bool lists = s->prm.density_list_slack > 0.0f;
+        a.nbr = lists ? s->nbr.p : nullptr;
+        a.nbr_cap = NBR_CAP;
+        a.nbr_warps = s->nbr_warps;
+        a.nbr_slack = lists ? s->prm.density_list_slack : 1.0f;
         a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p; a.i_ksr = s->ksr[0].p;
         a.i_rs = s->rs.p;
         a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
@@ -1205,6 +1222,8 @@ int density_phase(sph_system *s, bool eager) {
             CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
             sphk::DensityArgs f = a;
             f.n_eval = nullptr;
+            f.n_pass = nullptr;
+            f.nbr = nullptr;
             f.items = s->fitems.p;
             f.n_items_dev = s->scal.p + S_NFIX;
             f.i_list = s->amb_i.p;
@@ -1240,7 +1259,7 @@ int gravity_phase(sph_system *s, bool eager) {
     }
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_GK_B], st);
-    sphk::GravityArgs a;
+    sphk::GravityArgs a{};
     a.i_pe = s->pe.p;
     a.j_pm = s->pos[0].p; a.j_eps2 = s->eps2.p;
     a.s_pm = s->mom.p; a.s_eps2 = s->neps2.p;
@@ -1279,7 +1298,7 @@ int hydro_phase(sph_system *s, bool eager) {
     if (r) return r;
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_HK_B], st);
-    sphk::HydroArgs a;
+    sphk::HydroArgs a{};
     a.n_eval_near = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HN);
     a.n_eval_far = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HF);
     a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p;
@@ -1426,6 +1445,7 @@ extern "C" void sph_system_params_default(sph_system_params *p) {
     p->quadrupole = 0;
     p->item_split_nj = ITEM_SPLIT_NJ;
     p->heavy_classes = SPH_HEAVY_CLASSES;
+    p->density_list_slack = NBR_SLACK;
 }
 
 extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p, sph_system **out) {
@@ -1436,7 +1456,8 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
     s->ctx = ctx;
     s->n = (int)n;
     if (p) s->prm = *p; else sph_system_params_default(&s->prm);
-    if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || s->prm.n_leaf > sphtree::MAX_LEAF || !(s->prm.theta > 0.0)) {
+    if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || s->prm.n_leaf > sphtree::MAX_LEAF || !(s->prm.theta > 0.0) ||
+        s->prm.density_list_slack > MAX_NBR_SLACK) {
         delete s;
         return SPH_ERR_INVALID_ARGUMENT;
     }
@@ -1483,7 +1504,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
                             &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
     for (auto *b : f1) b->release();
     s->uflag.release(); s->uscan.release(); s->ulist.release(); s->a_sfirst.release(); s->a_scount.release();
-    s->amb_i.release(); s->amb_w.release(); s->fitems.release();
+    s->amb_i.release(); s->amb_w.release(); s->fitems.release(); s->nbr.release();
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count,
                          &s->scal};
@@ -1664,6 +1685,8 @@ extern "C" int sph_system_set_params(sph_system *s, const sph_system_params *p) 
     if (p->n_group < 1 || p->n_leaf < 1 || p->n_leaf > sphtree::MAX_LEAF || !(p->theta > 0.0))
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "n_group, n_leaf (1..%d) or theta out of range",
                                 sphtree::MAX_LEAF);
+    if (p->density_list_slack > MAX_NBR_SLACK)
+        return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "density_list_slack above %g", (double)MAX_NBR_SLACK);
     if (p->quadrupole && !s->prm.quadrupole)
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT,
                                 "quadrupole needs a system created with it (node moment buffers)");
@@ -1900,6 +1923,8 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->evals_density_grad = lc[L_EVAL_DG1];
     o->evals_hydro_near = lc[L_EVAL_HN];
     o->evals_hydro_far = lc[L_EVAL_HF];
+    o->density_list_passes = lc[L_DLISTED];
+    o->density_sweep_passes = lc[L_DSWEPT];
     o->last_status = s->last_status;
     return SPH_OK;
 }

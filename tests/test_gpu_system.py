@@ -380,6 +380,48 @@ def test_autotune_and_set_params():
         sys.close()
 
 
+@pytest.mark.parametrize("prec", ["fp32c", "fp64"])
+def test_density_neighbour_lists_match_sweeps(prec):
+    """The density kernel's per-lane neighbour lists (written by the first
+    pass, read by the later passes and the gradient pass) give the results of
+    streaming the walk's j-list in every pass, up to the grouping of the
+    partial sums: from a converged first guess of h, where the passes read
+    the lists, and from a guess 10% too small, where h outgrows the list
+    radius and the passes sweep."""
+    s = _two_stars(n=6000)
+    n = len(s["mass"])
+    fields = ("dens", "ksr", "grdh", "divv", "rotv", "np")
+    with functors.Context(precision=prec, eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, n, n_group=64, use_graph=0)
+        assert abs(sys.params.density_list_slack - 1.03) < 1e-6
+        sys.upload(s)
+        for _ in range(3):
+            sys.compute_forces()
+        h0 = sys.download("ksr")
+        for scale in (1.0, 0.9):
+            out = {}
+            for slack in (1.03, 0.0):
+                sys.set_params(density_list_slack=slack)
+                sys.set_field("ksr", h0 * scale)
+                sys.compute_forces()
+                out[slack] = ({f: sys.download(f) for f in fields}, sys.stats())
+            (a, sa), (b, sb) = out[1.03], out[0.0]
+            assert sb["density_list_passes"] == 0 and sb["density_sweep_passes"] > 0
+            total = sa["density_list_passes"] + sa["density_sweep_passes"]
+            if scale == 1.0:
+                assert sa["density_list_passes"] > 0.9 * total, sa
+                assert sa["evals_density_grad"] < 0.5 * sb["evals_density_grad"]
+            else:
+                assert sa["density_sweep_passes"] > 0.5 * total, sa
+            for f in fields[:5]:
+                e = err(a[f], b[f], FLOOR_DERIV if f in DERIV else FLOOR)
+                assert e < _tol(prec, f in DERIV), (scale, f, e)
+            assert np.mean(a["np"] != b["np"]) <= (0 if prec == "fp64" else 0.01)
+        with pytest.raises(abi.SPHError):
+            sys.set_params(density_list_slack=3.0)
+        sys.close()
+
+
 def test_graph_replay_recovers_from_list_overflow():
     """A captured force evaluation whose lists outgrow their buffers (search
     radii tripled behind the graph's back) is repeated eagerly with grown
