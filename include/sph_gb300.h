@@ -347,6 +347,10 @@ typedef struct sph_system_params {
                             pass read them while h stays within it; <= 0 or NaN: no
                             lists, every pass streams the walk's j-list; above 2 the
                             create / set_params calls fail with INVALID_ARGUMENT       */
+    int32_t hydro_signal_skip; /* 1 (default): hydro tiles of 32 j-entries whose
+                            signal-velocity terms provably cannot raise any i-particle's
+                            maximum skip those terms (results unchanged bit for bit);
+                            0: every term is evaluated                                 */
 } sph_system_params;
 
 /* Fields for sph_system_download / sph_system_download_sorted. */
@@ -386,6 +390,10 @@ typedef struct sph_system_stats {
                                              the first (second, third, gradient)
                                              served from neighbour lists         */
     int64_t density_sweep_passes;         /* ... that swept the walk's j-list     */
+    int64_t hydro_sv_tiles_skipped;       /* hydro 32-entry tiles whose signal-
+                                             velocity terms provably could not
+                                             raise any lane's maximum (skipped)  */
+    int64_t hydro_sv_tiles;               /* hydro tiles tested                   */
     int32_t last_status;
 } sph_system_stats;
 

@@ -703,6 +703,15 @@ struct HydroArgs {
     // when set: pair evaluations performed in full (near) and for the
     // signal velocity only (far), j-entries x i-particles
     unsigned long long *n_eval_near, *n_eval_far;
+    // when set: per walk, the largest sound speed of its j-list (the signal
+    // velocity of every i-particle of the walk is at least its own sound
+    // speed plus this), which lets tiles that cannot raise the maximum skip
+    // their signal-velocity terms
+    const double *walk_csmax = nullptr;
+    int sv_skip = 0;   // nonzero: tiles test the bound and skip (0: every term evaluated)
+    // when set: [0] 32-entry tiles whose signal-velocity terms were skipped,
+    // [1] tiles evaluated
+    unsigned long long *n_skip = nullptr;
 };
 
 template <bool F64, int WARPS>
@@ -726,7 +735,8 @@ hydro_kernel(const HydroArgs a) {
     __shared__ float2 s_f[WARPS][64]; // P lo, u lo
     __shared__ long long s_id[WARPS][64];
     __shared__ R4 s_fp[WARPS][64];    // far: centred position, vsnd
-    __shared__ R4 s_fv[WARPS][64];    // far: velocity (hi)
+    __shared__ R4 s_fv[WARPS][64];    // far: velocity (hi), signal-velocity bound b_j
+    __shared__ R s_nb[WARPS][64];     // near: signal-velocity bound b_j
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
@@ -764,6 +774,37 @@ hydro_kernel(const HydroArgs a) {
             eg_i = g3.x; elo_i = g3.y; et_i = g3.z;
         }
         const long long idi = a.i_id[ii];
+        // Signal-velocity bounds.  With v_c the velocity of the item's centre
+        // particle, |v_i - v_j| <= d_i + d_j (d = |v - v_c|, FP32C with the
+        // hi and lo differences added per component) and |w| <= |v_i - v_j|,
+        // so every pair term cs_i + cs_j - 3 min(w, 0) of a tile is at most
+        // cs_i + 3 d_i + max_j b_j with b_j = cs_j + 3 d_j.  The maximum over
+        // the list starts at cs_i + (largest cs_j of the walk), which no pair
+        // term undercuts; a tile whose bound (with a 1e-5 relative margin over
+        // the rounding of both) stays below every lane's running maximum adds
+        // nothing to it and skips those terms: the maximum is unchanged bit
+        // for bit.
+        R vcx, vcy, vcz;
+        float lcx = 0.0f, lcy = 0.0f, lcz = 0.0f;
+        if (F64) {
+            const dbl4 v = a.i_vel[r.ic];
+            vcx = v.x; vcy = v.y; vcz = v.z;
+        } else {
+            const float4 vh = a.fi.vhi[r.ic], vl = a.fi.vlo[r.ic];
+            vcx = vh.x; vcy = vh.y; vcz = vh.z;
+            lcx = vl.x; lcy = vl.y; lcz = vl.z;
+        }
+        auto dvel = [&](R hx, R hy, R hz, float lx, float ly, float lz) -> R {
+            const R ex = fabs(hx - vcx) + (R)fabsf(lx - lcx);
+            const R ey = fabs(hy - vcy) + (R)fabsf(ly - lcy);
+            const R ez = fabs(hz - vcz) + (R)fabsf(lz - lcz);
+            return sqrt(ex * ex + ey * ey + ez * ez);
+        };
+        auto sv_bound = [&](R cs, R d) -> R {
+            const R b = cs + (R)3 * d;
+            return (b < (R)0) ? (R)0 : b;   // NaN stays NaN (no skip)
+        };
+        const R ub_i = cs_i + (R)3 * dvel(vxi, vyi, vzi, lxi, lyi, lzi);
         // i position in the item frame as one number (box and far pairs)
         const R xc = xi + (R)xlo, yc = yi + (R)ylo, zc = zi + (R)zlo;
         IBox<R> box;
@@ -773,6 +814,34 @@ hydro_kernel(const HydroArgs a) {
 
         Acc<F64> ax, ay, az, ud, df, gx, gy, gz;
         R vsmx = 0;
+        if (a.walk_csmax) {
+            const R v0 = cs_i + (R)a.walk_csmax[r.walk];
+            vsmx = (v0 > (R)0) ? v0 : (R)0;
+        }
+        // true when no pair term of the n-entry tile at bound[] can exceed
+        // any lane's running maximum
+        unsigned n_skipped = 0, n_tiles = 0;
+        auto skip_tile = [&](const R *bound, int stride, int n) -> bool {
+            if (!a.sv_skip) return false;
+            R b = (lane < n) ? bound[lane * stride] : (R)0;
+            R t;
+            if constexpr (F64) {
+                t = b;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const R u = __shfl_xor_sync(FULL, t, o);
+                    t = (u > t || u != u) ? u : t;
+                }
+            } else {
+                // non-negative floats (or NaN) order like their bit patterns
+                t = __uint_as_float(__reduce_max_sync(FULL, __float_as_uint(b)));
+            }
+            const bool ok = (ub_i + t) * (R)1.00001 <= vsmx;
+            const bool all = __all_sync(FULL, ok);
+            ++n_tiles;
+            if (all) ++n_skipped;
+            return all;
+        };
         int nhead = 0, nfill = 0, fhead = 0, ffill = 0;
         long long kept_n = 0, kept_f = 0;
         R pax = 0, pay = 0, paz = 0, pud = 0, pdf = 0, pgx = 0, pgy = 0, pgz = 0;
@@ -807,6 +876,21 @@ hydro_kernel(const HydroArgs a) {
             const R vs = cs_i + s_p2[wid][k].w - (R)3 * wneg;
             vsmx = vs > vsmx ? vs : vsmx;
             const R hj = s_p1[wid][k].w;
+            const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
+            if (!(r2 * hmin2 * (R)1.00002 >= (R)1)) msk |= 1u << (k & 31);
+        };
+        // the mark alone (tiles whose signal-velocity terms are skipped)
+        auto mark_only = [&](int k, unsigned &msk) {
+            const R4 P1 = s_p1[wid][k];
+            R dx = xi - P1.x, dy = yi - P1.y, dz = zi - P1.z;
+            if (!F64) {
+                const R4 P2 = s_p2[wid][k];
+                dx += (R)(xlo - (float)P2.x);
+                dy += (R)(ylo - (float)P2.y);
+                dz += (R)(zlo - (float)P2.z);
+            }
+            const R r2 = dx * dx + dy * dy + dz * dz;
+            const R hj = P1.w;
             const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
             if (!(r2 * hmin2 * (R)1.00002 >= (R)1)) msk |= 1u << (k & 31);
         };
@@ -873,7 +957,14 @@ hydro_kernel(const HydroArgs a) {
         auto run_near = [&](int n) {
             pax = 0; pay = 0; paz = 0; pud = 0; pdf = 0; pgx = 0; pgy = 0; pgz = 0;
             unsigned msk = 0;
-            if (tpi == 1 && n == 32) {
+            if (skip_tile(&s_nb[wid][nhead], 1, n)) {
+                if (tpi == 1 && n == 32) {
+#pragma unroll 8
+                    for (int k = 0; k < 32; ++k) mark_only(nhead + k, msk);
+                } else {
+                    for (int k = sub; k < n; k += tpi) mark_only(nhead + k, msk);
+                }
+            } else if (tpi == 1 && n == 32) {
 #pragma unroll 4
                 for (int k = 0; k < 32; ++k) signal(nhead + k, msk);
             } else {
@@ -895,6 +986,10 @@ hydro_kernel(const HydroArgs a) {
             __syncwarp();
         };
         auto run_far = [&](int n) {
+            if (skip_tile(&s_fv[wid][fhead].w, 4, n)) {
+                __syncwarp();
+                return;
+            }
             if (tpi == 1 && n == 32) {
 #pragma unroll 8
                 for (int k = 0; k < 32; ++k) far_pair(fhead + k);
@@ -948,6 +1043,7 @@ hydro_kernel(const HydroArgs a) {
                     s_c[wid][k] = Real<F64>::make4(g1_64.y, g1_64.z, g1_64.w, g2_64.x);
                     s_d[wid][k] = Real<F64>::make4(g2_64.z, g2_64.w, g3.x, g3.y);
                     s_f[wid][k] = make_float2(0.0f, 0.0f);
+                    s_nb[wid][k] = sv_bound(g2_64.y, dvel(v64.x, v64.y, v64.z, 0.0f, 0.0f, 0.0f));
                 } else {
                     const float4 vl = a.fj.vlo[j], g1 = a.fj_g1[j], g3 = a.fj_g3[j];
                     s_p1[wid][k] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y), (R)(ph.z - cph.z),
@@ -959,6 +1055,7 @@ hydro_kernel(const HydroArgs a) {
                     s_c[wid][k] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
                     s_d[wid][k] = Real<F64>::make4((R)g2.z, (R)g2.w, (R)g3.x, (R)g3.z);
                     s_f[wid][k] = make_float2(g1.y, g3.y);
+                    s_nb[wid][k] = sv_bound((R)g2.y, dvel(vh.x, vh.y, vh.z, vl.x, vl.y, vl.z));
                 }
                 s_id[wid][k] = a.j_id[j];
             }
@@ -966,10 +1063,12 @@ hydro_kernel(const HydroArgs a) {
                 const int k = (fhead + ffill + __popc(mf & lt)) & 63;
                 if (F64) {
                     s_fp[wid][k] = Real<F64>::make4(px, py, pz, g2_64.y);
-                    s_fv[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z, 0.0);
+                    s_fv[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z,
+                                                    sv_bound(g2_64.y, dvel(v64.x, v64.y, v64.z, 0.0f, 0.0f, 0.0f)));
                 } else {
                     s_fp[wid][k] = Real<F64>::make4(px, py, pz, (R)g2.y);
-                    s_fv[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)0);
+                    s_fv[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z,
+                                                    sv_bound((R)g2.y, dvel(vh.x, vh.y, vh.z, lcx, lcy, lcz)));
                 }
             }
             nfill += __popc(mn);
@@ -1009,6 +1108,10 @@ hydro_kernel(const HydroArgs a) {
         if (a.n_eval_near && lane == 0) {
             atomicAdd(a.n_eval_near, (unsigned long long)kept_n * (unsigned long long)r.ni);
             atomicAdd(a.n_eval_far, (unsigned long long)kept_f * (unsigned long long)r.ni);
+        }
+        if (a.n_skip && lane == 0) {
+            atomicAdd(a.n_skip, (unsigned long long)n_skipped);
+            atomicAdd(a.n_skip + 1, (unsigned long long)n_tiles);
         }
     }
 }

@@ -47,7 +47,7 @@ enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN
        D_R2, D_DN, D_NI };
 // 64-bit counters
 enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_EVAL_D1,
-       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_DLISTED, L_DSWEPT, L_NI };
+       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_DLISTED, L_DSWEPT, L_HSKIP, L_HTILES, L_NI };
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
@@ -587,6 +587,25 @@ __global__ void gravity_writeback(int n, double G, const double *acc, const doub
 }
 
 // HydroEPI/EPJ::copyFromFP, hdr_hydro.hpp:45-62 / 95-113 (umin = 0)
+// Largest sound speed over each hydro walk's j-list (one warp per walk; -inf
+// for an empty list).  The signal velocity of every i-particle of the walk,
+// a maximum of cs_i + cs_j - 3 min(w, 0) over the list (hdr_hydro.hpp:368-372),
+// is at least its own sound speed plus this.
+__global__ void walk_csmax(const int *n_walks, const int *j_off, const int *j_idx, const float4 *f_g2,
+                           const dbl4 *h2, double *out) {
+    const int lane = threadIdx.x & 31;
+    const int nw = *n_walks;
+    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += (gridDim.x * blockDim.x) >> 5) {
+        double m = -INFINITY;
+        for (int k = j_off[w] + lane; k < j_off[w + 1]; k += 32) {
+            const int j = j_idx ? j_idx[k] : k;
+            m = fmax(m, f_g2 ? (double)f_g2[j].y : h2[j].y);   // a NaN never raises the maximum
+        }
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) out[w] = m;
+    }
+}
+
 __global__ void hydro_prep(int n, const double *ksr, const double *pres, const double *grdh,
                            const double *dens, const double *bswt, const double *vsnd, const double *alph,
                            const double *alphu, const double *uene, const double *eta, dbl4 *h1, dbl4 *h2,
@@ -802,6 +821,7 @@ struct sph_system {
     // per-warp neighbour lists of the density kernel (scratch)
     DevBuf<int> nbr;
     int nbr_warps = 0;
+    DevBuf<double> w_csmax;   // per hydro walk: largest sound speed of its list
     // groups and walks
     DevBuf<int> gflag, groot, gscan, group_node, group_first, group_count;
     DevBuf<int> aflag, ascan, a_node, a_first, a_count;
@@ -895,7 +915,7 @@ int alloc_all(sph_system *s) {
     s->amb_cap = std::max<int>(1024, s->n / 16);
     e |= s->amb_i.ensure(s->amb_cap) | s->amb_w.ensure(s->amb_cap) | s->fitems.ensure(s->amb_cap);
     s->nbr_warps = std::max(s->ctx->grid[0][0], s->ctx->grid[0][1]) * PAIR_WARPS;
-    e |= s->nbr.ensure((size_t)s->nbr_warps * NBR_CAP * 32);
+    e |= s->nbr.ensure((size_t)s->nbr_warps * NBR_CAP * 32) | s->w_csmax.ensure(n);
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count};
     for (auto *b : i1) e |= b->ensure(n);
@@ -1296,11 +1316,19 @@ int hydro_phase(sph_system *s, bool eager) {
                                                               s->f_vlo.p, s->f_g1.p, s->f_g2.p, s->f_g3.p);
     int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
     if (r) return r;
+    const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
+    const bool skip = s->prm.hydro_signal_skip != 0;
+    if (skip)
+        walk_csmax<<<ctx->sm_count * 8, 256, 0, st>>>(s->walk_num[1], s->loff[1].p, s->jidx[1].p,
+                                                     f32 ? s->f_g2.p : nullptr, s->h2.p, s->w_csmax.p);
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_HK_B], st);
     sphk::HydroArgs a{};
     a.n_eval_near = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HN);
     a.n_eval_far = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HF);
+    a.n_skip = reinterpret_cast<unsigned long long *>(s->lscal.p + L_HSKIP);
+    a.walk_csmax = skip ? s->w_csmax.p : nullptr;
+    a.sv_skip = skip ? 1 : 0;
     a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p;
     a.i_h1 = s->h1.p; a.i_h2 = s->h2.p; a.i_h3 = s->h3.p;
     a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
@@ -1446,6 +1474,7 @@ extern "C" void sph_system_params_default(sph_system_params *p) {
     p->item_split_nj = ITEM_SPLIT_NJ;
     p->heavy_classes = SPH_HEAVY_CLASSES;
     p->density_list_slack = NBR_SLACK;
+    p->hydro_signal_skip = 1;
 }
 
 extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p, sph_system **out) {
@@ -1504,7 +1533,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
                             &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
     for (auto *b : f1) b->release();
     s->uflag.release(); s->uscan.release(); s->ulist.release(); s->a_sfirst.release(); s->a_scount.release();
-    s->amb_i.release(); s->amb_w.release(); s->fitems.release(); s->nbr.release();
+    s->amb_i.release(); s->amb_w.release(); s->fitems.release(); s->nbr.release(); s->w_csmax.release();
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count,
                          &s->scal};
@@ -1925,6 +1954,8 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->evals_hydro_far = lc[L_EVAL_HF];
     o->density_list_passes = lc[L_DLISTED];
     o->density_sweep_passes = lc[L_DSWEPT];
+    o->hydro_sv_tiles_skipped = lc[L_HSKIP];
+    o->hydro_sv_tiles = lc[L_HTILES];
     o->last_status = s->last_status;
     return SPH_OK;
 }

@@ -35,7 +35,8 @@ class SystemParams(ctypes.Structure):
                 ("dt_max", _D), ("dt_min", _D), ("alpha_max", _D), ("alpha_min", _D),
                 ("alphu_max", _D), ("alphu_min", _D), ("ksr_max_mode", _I32),
                 ("max_density_iterations", _I32), ("use_graph", _I32), ("quadrupole", _I32),
-                ("item_split_nj", _I32), ("heavy_classes", _I32), ("density_list_slack", ctypes.c_float)]
+                ("item_split_nj", _I32), ("heavy_classes", _I32), ("density_list_slack", ctypes.c_float),
+                ("hydro_signal_skip", _I32)]
 
 
 class SystemStats(ctypes.Structure):
@@ -45,7 +46,8 @@ class SystemStats(ctypes.Structure):
                 ("list_hydro", _I64), ("list_gravity", _I64), ("steps", _I64), ("density_rechecked", _I64),
                 ("evals_density_first", _I64), ("evals_density_grad", _I64), ("evals_hydro_near", _I64),
                 ("evals_hydro_far", _I64), ("density_list_passes", _I64),
-                ("density_sweep_passes", _I64), ("last_status", _I32)]
+                ("density_sweep_passes", _I64), ("hydro_sv_tiles_skipped", _I64), ("hydro_sv_tiles", _I64),
+                ("last_status", _I32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -391,8 +391,9 @@ def test_density_neighbour_lists_match_sweeps(prec):
     s = _two_stars(n=6000)
     n = len(s["mass"])
     fields = ("dens", "ksr", "grdh", "divv", "rotv", "np")
-    with functors.Context(precision=prec, eta=1.18) as ctx:
-        sys = ParticleSystem(ctx, n, n_group=64, use_graph=0)
+    # fixed clamp of h: the reference rule moves it after every evaluation
+    with functors.Context(precision=prec, eta=1.18, ksr_max=0.0) as ctx:
+        sys = ParticleSystem(ctx, n, n_group=64, use_graph=0, ksr_max_mode=0)
         assert abs(sys.params.density_list_slack - 1.03) < 1e-6
         sys.upload(s)
         for _ in range(3):
@@ -420,6 +421,38 @@ def test_density_neighbour_lists_match_sweeps(prec):
         with pytest.raises(abi.SPHError):
             sys.set_params(density_list_slack=3.0)
         sys.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32c", "fp64"])
+def test_hydro_signal_skip_is_exact(prec):
+    """Hydro tiles that skip their signal-velocity terms (the bound shows
+    they cannot raise any i-particle's maximum) leave every hydro output bit
+    for bit as evaluating all terms does: a star at rest, where most tiles
+    skip, and one with random velocities of the order of the sound speed,
+    where the velocity part of the bound keeps most tiles evaluated."""
+    for spin in (True, False):
+        s = _star(n=4000, seed=7, spin=spin)
+        n = len(s["mass"])
+        # fixed clamp of h: the reference rule moves it after every evaluation
+        with functors.Context(precision=prec, eta=1.18, ksr_max=0.0) as ctx:
+            sys = ParticleSystem(ctx, n, n_group=64, use_graph=0, ksr_max_mode=0)
+            sys.upload(s)
+            sys.compute_forces()
+            h0 = sys.download("ksr")
+            out = {}
+            for skip in (1, 0):
+                sys.set_params(hydro_signal_skip=skip)
+                sys.set_field("ksr", h0)
+                sys.compute_forces()
+                out[skip] = ({f: sys.download(f) for f in ("acch", "accg1", "udot", "vsmx", "diffu")},
+                             sys.stats())
+            (a, sa), (b, sb) = out[1], out[0]
+            assert sb["hydro_sv_tiles_skipped"] == 0
+            if not spin:
+                assert sa["hydro_sv_tiles_skipped"] > 0.3 * sa["hydro_sv_tiles"], sa
+            for f in a:
+                assert np.array_equal(a[f].view(np.uint64), b[f].view(np.uint64)), (spin, f)
+            sys.close()
 
 
 def test_graph_replay_recovers_from_list_overflow():
