@@ -587,22 +587,39 @@ __global__ void gravity_writeback(int n, double G, const double *acc, const doub
 }
 
 // HydroEPI/EPJ::copyFromFP, hdr_hydro.hpp:45-62 / 95-113 (umin = 0)
-// Largest sound speed over each hydro walk's j-list (one warp per walk; -inf
+// Largest sound speed over each hydro walk's j-list (one block per walk, -inf
 // for an empty list).  The signal velocity of every i-particle of the walk,
 // a maximum of cs_i + cs_j - 3 min(w, 0) over the list (hdr_hydro.hpp:368-372),
 // is at least its own sound speed plus this.
-__global__ void walk_csmax(const int *n_walks, const int *j_off, const int *j_idx, const float4 *f_g2,
-                           const dbl4 *h2, double *out) {
-    const int lane = threadIdx.x & 31;
+constexpr int CSMAX_THREADS = 256;
+__global__ void __launch_bounds__(CSMAX_THREADS) walk_csmax(const int *n_walks, const int *j_off, const int *j_idx,
+                                                            const float4 *f_g2, const dbl4 *h2, double *out) {
+    __shared__ double red[CSMAX_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = *n_walks;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += (gridDim.x * blockDim.x) >> 5) {
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
         double m = -INFINITY;
-        for (int k = j_off[w] + lane; k < j_off[w + 1]; k += 32) {
-            const int j = j_idx ? j_idx[k] : k;
-            m = fmax(m, f_g2 ? (double)f_g2[j].y : h2[j].y);   // a NaN never raises the maximum
+        const int e = j_off[w + 1];
+        // four entries per thread and round: their loads are in flight together
+        for (int k = j_off[w] + threadIdx.x; k < e; k += 4 * CSMAX_THREADS) {
+            int j[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int kk = k + u * CSMAX_THREADS;
+                j[u] = kk < e ? (j_idx ? j_idx[kk] : kk) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j[u] >= 0) m = fmax(m, f_g2 ? (double)f_g2[j[u]].y : h2[j[u]].y);   // NaN never raises it
         }
         for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) out[w] = m;
+        if (lane == 0) red[warp] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < CSMAX_THREADS / 32; ++k) m = fmax(m, red[k]);
+            out[w] = m;
+        }
+        __syncthreads();
     }
 }
 
@@ -1319,7 +1336,7 @@ int hydro_phase(sph_system *s, bool eager) {
     const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
     const bool skip = s->prm.hydro_signal_skip != 0;
     if (skip)
-        walk_csmax<<<ctx->sm_count * 8, 256, 0, st>>>(s->walk_num[1], s->loff[1].p, s->jidx[1].p,
+        walk_csmax<<<ctx->sm_count * 8, CSMAX_THREADS, 0, st>>>(s->walk_num[1], s->loff[1].p, s->jidx[1].p,
                                                      f32 ? s->f_g2.p : nullptr, s->h2.p, s->w_csmax.p);
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_HK_B], st);
