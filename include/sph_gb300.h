@@ -452,6 +452,24 @@ int sph_system_set_field(sph_system *sys, int32_t field, const double *data);
 int sph_system_get_clock(sph_system *sys, double *time, double *dt, double *ksr_max, double *eps_u);
 int sph_system_set_clock(sph_system *sys, double time, double dt, double ksr_max, double eps_u);
 
+/* Derivative of the step (no counterpart in the reference, which has no
+ * gradients).  sph_system_predict runs the leapfrog predictor alone
+ * (hdr_hgas.hpp:646-657) with the clock's dt; followed by
+ * sph_system_compute_forces it repeats the force evaluation of a step from
+ * that step's starting state.  sph_system_adjoint_forces is the
+ * vector-Jacobian product of the last force evaluation, with the lists, tree
+ * and dt of that evaluation held fixed:
+ *   seed (upload order, 8n doubles): dL/d of the outputs acc (3n), udot (n),
+ *        adot (n), ksr (n, the final h), pot (n), dens (n)
+ *   grad (upload order, 9n doubles): dL/d of the inputs position (3n),
+ *        velocity (3n), uene (n), alph (n), and the first guess of h (n).
+ * It needs monopole gravity, alphu_max = alphu_min = 0, no clamp of h
+ * (context ksr_max 0 and ksr_max_mode 0) and an evaluation with a single
+ * density walk; otherwise SPH_ERR_STATE.  FP64 arithmetic, either precision
+ * of the forward evaluation. */
+int sph_system_predict(sph_system *sys);
+int sph_system_adjoint_forces(sph_system *sys, const double *seed, double *grad);
+
 /* Interaction lists of the last force evaluation (kind 0 density — the first
  * walk, which covers every group —, 1 hydro, 2 gravity), in Morton order:
  * walk w has i-particles [i_first[w], i_first[w] + i_count[w]) and list

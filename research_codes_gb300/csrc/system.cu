@@ -17,6 +17,7 @@
 
 #include "../../include/sph_gb300.h"
 #include "capi_internal.h"
+#include "adjoint.cuh"
 #include "pair_kernels.cuh"
 #include "tree.cuh"
 
@@ -866,6 +867,11 @@ struct sph_system {
     HostBuf<long long> h_lscal;
     DevBuf<double> staging;
     DevBuf<double> an_buf;   // analysis scratch (4 n), allocated on first use
+    DevBuf<double> h_guess;  // first guess of h of the last density evaluation
+    // adjoint scratch, allocated on first use: accumulators, seeds, items
+    DevBuf<double> adj_acc, adj_seed;
+    DevBuf<sphadj::AdjItem> adj_items;
+    DevBuf<int> adj_cnt, adj_off;
     DevBuf<char> cub_tmp;
     size_t cub_bytes = 0;
     // graph
@@ -944,6 +950,7 @@ int alloc_all(sph_system *s) {
     e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
     e |= s->partial.ensure(RED_BLOCKS * MAX_RED + MAX_RED) | s->box.ensure(8);
     e |= s->h_scal.ensure(S_NI) | s->h_dscal.ensure(D_NI) | s->h_lscal.ensure(L_NI);
+    e |= s->h_guess.ensure(n);
     // CUB scratch: radix sort of (uint64, int) pairs and exclusive sums over n ints
     size_t b1 = 0, b2 = 0;
     cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
@@ -1194,6 +1201,8 @@ int density_phase(sph_system *s, bool eager) {
         sphk::make_density_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->vel[0].p, s->f_phi.p,
                                                                 s->f_plo.p, s->f_vhi.p, s->f_vlo.p);
     init_rs<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->rs.p);
+    // the first guess, kept for the derivative of this evaluation
+    CUDA_TRY(cudaMemcpyAsync(s->h_guess.p, s->ksr[0].p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, st));
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_ITERS, 1);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_AMBTOT, 0);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_UNCONV, 0);
@@ -1564,6 +1573,8 @@ extern "C" int sph_system_destroy(sph_system *s) {
     }
     s->items.release(); s->lscal.release(); s->cub_tmp.release(); s->an_buf.release();
     s->h_scal.release(); s->h_dscal.release(); s->h_lscal.release();
+    s->h_guess.release(); s->adj_acc.release(); s->adj_seed.release(); s->adj_items.release();
+    s->adj_cnt.release(); s->adj_off.release();
     s->ctx->n_systems--;
     delete s;
     return SPH_OK;
@@ -2124,5 +2135,111 @@ extern "C" int sph_system_radii_sorted(sph_system *s, int32_t star, const double
         CUDA_TRY(cudaMemcpyAsync(m_out, m1, sizeof(double) * (size_t)c, cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
     }
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------- derivative
+// Leapfrog predictor alone (hdr_hgas.hpp:646-657) with the clock's current dt:
+// with sph_system_compute_forces afterwards it reproduces the force evaluation
+// of a step from that step's starting state, for sph_system_adjoint_forces.
+extern "C" int sph_system_predict(sph_system *s) {
+    if (!s) return SPH_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(s->ctx->prm.device);
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    predict<<<grid_for(n), 256, 0, st>>>(n, s->dscal.p, s->pos[0].p, s->vel[0].p, s->vel2[0].p, s->acc.p,
+                                         s->uene[0].p, s->uene2[0].p, s->udot.p, s->alph[0].p, s->alph2[0].p,
+                                         s->adot.p, s->alphu[0].p, s->alphu2[0].p, s->adotu.p);
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+// Vector-Jacobian product of the last force evaluation (adjoint.cuh).
+// seed (host, upload order, 8n doubles): dL/d acc (3n), udot, adot, ksr (the
+// final h), pot, dens.  grad (host, upload order, 9n doubles): dL/d position
+// (3n), velocity (3n), internal energy, alpha, first guess of h.
+extern "C" int sph_system_adjoint_forces(sph_system *s, const double *seed, double *grad) {
+    if (!s || !seed || !grad) return SPH_ERR_INVALID_ARGUMENT;
+    sph_context *ctx = s->ctx;
+    cudaSetDevice(ctx->prm.device);
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    if (s->prm.quadrupole || s->prm.alphu_max != 0.0 || s->prm.alphu_min != 0.0 ||
+        !(ctx->prm.ksr_max <= 0.0 && s->prm.ksr_max_mode == 0))
+        return sphrt::set_error(ctx, SPH_ERR_STATE,
+                                "the derivative covers monopole gravity, alpha_u fixed at 0 and no clamp of h "
+                                "(ksr_max 0, ksr_max_mode 0)");
+    int sc[S_NI];
+    CUDA_TRY(cudaMemcpyAsync(sc, s->scal.p, sizeof(sc), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (sc[S_ITERS] != 1)
+        return sphrt::set_error(ctx, SPH_ERR_STATE,
+                                "the derivative needs a force evaluation with one density walk (got %d)", sc[S_ITERS]);
+    const int ng = sc[S_NGROUPS];
+    // scratch
+    const int NA = 26;   // doubles per particle in the accumulators (+ 4 per node, 2n nodes)
+    int e = s->adj_acc.ensure((size_t)NA * n + 8 * (size_t)n) | s->adj_seed.ensure(8 * (size_t)n + 9 * (size_t)n);
+    e |= s->adj_cnt.ensure(n + 1) | s->adj_off.ensure(n + 1);
+    if (e) return sphrt::set_error(ctx, SPH_ERR_CUDA, "adjoint scratch allocation failed");
+    CUDA_TRY(cudaMemsetAsync(s->adj_acc.p, 0, sizeof(double) * ((size_t)NA * n + 8 * (size_t)n), st));
+    // items: one warp per 32 particles of a group
+    sphadj::adj_item_counts<<<grid_for(ng), 256, 0, st>>>(ng, s->group_count.p, s->adj_cnt.p);
+    int r = exclusive_scan(s, s->adj_cnt.p, s->adj_off.p, ng);
+    if (r) return r;
+    int last[2];
+    CUDA_TRY(cudaMemcpyAsync(&last[0], s->adj_off.p + ng - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&last[1], s->adj_cnt.p + ng - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const int n_items = last[0] + last[1];
+    if (s->adj_items.ensure(n_items)) return sphrt::set_error(ctx, SPH_ERR_CUDA, "adjoint item allocation failed");
+    sphadj::adj_fill_items<<<grid_for(ng), 256, 0, st>>>(ng, s->group_first.p, s->group_count.p, s->adj_off.p,
+                                                         s->adj_items.p);
+    // seeds: host (upload order) -> device (sorted order)
+    double *up = s->adj_seed.p, *sd = s->adj_seed.p + 8 * (size_t)n;
+    CUDA_TRY(cudaMemcpyAsync(up, seed, sizeof(double) * 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    gather_field<<<grid_for(n), 256, 0, st>>>(n, 3, s->orig[0].p, up, sd);
+    for (int k = 0; k < 5; ++k)
+        gather_field<<<grid_for(n), 256, 0, st>>>(n, 1, s->orig[0].p, up + (3 + k) * (size_t)n,
+                                                  sd + (3 + k) * (size_t)n);
+    sphadj::AdjSeed sed{sd, sd + 3 * (size_t)n, sd + 4 * (size_t)n, sd + 5 * (size_t)n, sd + 6 * (size_t)n,
+                        sd + 7 * (size_t)n};
+    double *A = s->adj_acc.p;
+    auto slot = [&](int k) { return A + (size_t)k * n; };
+    sphadj::AdjAcc acc;
+    acc.x = slot(0); acc.v = slot(3); acc.u = slot(6); acc.alph = slot(7); acc.h0 = slot(8);
+    acc.h = slot(9); acc.rho = slot(10); acc.omega = slot(11); acc.divv = slot(12); acc.rotv = slot(13);
+    acc.c = slot(14); acc.b = slot(15); acc.pc = slot(16); acc.eta = slot(17); acc.e2 = slot(18);
+    acc.hinv = slot(19); acc.etas = slot(20); acc.bswt = slot(21);
+    acc.node = slot(NA);   // 8n doubles: 4 per node
+    sphadj::AdjState as;
+    as.n = n;
+    as.pos = s->pos[0].p; as.vel = s->vel[0].p; as.uene = s->uene[0].p; as.alph = s->alph[0].p;
+    as.h0 = s->h_guess.p; as.h = s->ksr[0].p; as.dens = s->dens.p; as.grdh = s->grdh.p; as.divv = s->divv.p;
+    as.rotv = s->rotv.p; as.pres = s->pres.p; as.vsnd = s->vsnd.p; as.bswt = s->bswt.p; as.eps2 = s->eps2.p;
+    as.eta = s->eta.p; as.etas = s->r_eta.p;
+    as.mom = s->mom.p; as.neps2 = s->neps2.p; as.parent = s->parent.p;
+    as.d_off = s->loff[0].p; as.d_idx = s->jidx[0].p; as.h_off = s->loff[1].p; as.h_idx = s->jidx[1].p;
+    as.g_off = s->loff[2].p; as.g_idx = s->jidx[2].p;
+    as.G = s->prm.G; as.amax = s->prm.alpha_max; as.amin = s->prm.alpha_min; as.eta_ksrh = ctx->prm.eta * KSRH;
+    const int eg = grid_for(n), wg = ctx->sm_count * 8;
+    sphadj::adj_alpha<<<eg, 256, 0, st>>>(as, sed, acc);
+    sphadj::adj_hydro<<<wg, 128, 0, st>>>(as, sed, acc, s->adj_items.p, n_items);
+    sphadj::adj_hydro_prep<<<eg, 256, 0, st>>>(as, acc);
+    sphadj::adj_gravity<<<wg, 128, 0, st>>>(as, sed, acc, s->adj_items.p, n_items);
+    sphadj::adj_nodes<<<eg, 256, 0, st>>>(as, acc);
+    sphadj::adj_switch<<<eg, 256, 0, st>>>(as, acc);
+    sphadj::adj_density_grad<<<wg, 128, 0, st>>>(as, acc, s->adj_items.p, n_items);
+    sphadj::adj_density_passes<<<wg, 128, 0, st>>>(as, acc, s->adj_items.p, n_items);
+    // results: sorted -> upload order
+    double *out = s->adj_seed.p;   // 9n doubles (the seeds are consumed)
+    scatter_field<<<grid_for(n), 256, 0, st>>>(n, 3, s->orig[0].p, acc.x, out);
+    scatter_field<<<grid_for(n), 256, 0, st>>>(n, 3, s->orig[0].p, acc.v, out + 3 * (size_t)n);
+    scatter_field<<<grid_for(n), 256, 0, st>>>(n, 1, s->orig[0].p, acc.u, out + 6 * (size_t)n);
+    scatter_field<<<grid_for(n), 256, 0, st>>>(n, 1, s->orig[0].p, acc.alph, out + 7 * (size_t)n);
+    scatter_field<<<grid_for(n), 256, 0, st>>>(n, 1, s->orig[0].p, acc.h0, out + 8 * (size_t)n);
+    CUDA_TRY(cudaMemcpyAsync(grad, out, sizeof(double) * 9 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    const cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) return sphrt::cuda_error(ctx, ce, "adjoint kernels");
     return SPH_OK;
 }

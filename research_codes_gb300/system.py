@@ -75,6 +75,8 @@ def _declare(lib):
         "sph_system_get_clock": (ctypes.c_int, [_P, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
                                                 ctypes.POINTER(_D)]),
         "sph_system_set_clock": (ctypes.c_int, [_P, _D, _D, _D, _D]),
+        "sph_system_predict": (ctypes.c_int, [_P]),
+        "sph_system_adjoint_forces": (ctypes.c_int, [_P, _P, _P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -140,6 +142,34 @@ class ParticleSystem:
 
     def compute_forces(self):
         check(self.lib.sph_system_compute_forces(self.handle), self.ctx.handle, "compute_forces")
+
+    def predict(self):
+        """Leapfrog predictor alone, with the clock's dt."""
+        check(self.lib.sph_system_predict(self.handle), self.ctx.handle, "predict")
+
+    SEED = (("acc", 3), ("udot", 1), ("adot", 1), ("ksr", 1), ("pot", 1), ("dens", 1))
+    GRAD = (("pos", 3), ("vel", 3), ("uene", 1), ("alph", 1), ("ksr", 1))
+
+    def adjoint_forces(self, seed):
+        """Vector-Jacobian product of the last force evaluation: `seed` maps
+        output names (acc, udot, adot, ksr, pot, dens; missing ones are zero)
+        to dL/d output in upload order; returns dL/d input for pos, vel, uene,
+        alph and ksr (the evaluation's first guess of h)."""
+        n = self.n
+        buf = np.zeros(8 * n, np.float64)
+        o = 0
+        for k, w in self.SEED:
+            if k in seed:
+                buf[o:o + w * n] = np.asarray(seed[k], np.float64).reshape(-1)
+            o += w * n
+        out = np.empty(9 * n, np.float64)
+        check(self.lib.sph_system_adjoint_forces(self.handle, _ptr(buf), _ptr(out)), self.ctx.handle,
+              "adjoint_forces")
+        res, o = {}, 0
+        for k, w in self.GRAD:
+            res[k] = out[o:o + w * n].reshape((n, 3) if w == 3 else n).copy()
+            o += w * n
+        return res
 
     def set_graph(self, on):
         check(self.lib.sph_system_set_graph(self.handle, 1 if on else 0), self.ctx.handle, "set_graph")
