@@ -42,7 +42,7 @@ constexpr int MAX_RED = 8;
 // int scalars
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_NTASKS, S_NROOTS, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
+       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_POOLMAX, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -463,6 +463,13 @@ __global__ void light_counts(int n, const int *n_walks, const int *i_count, cons
     }
 }
 
+// A list build that overflowed its buffers (capacity or stack error set)
+// leaves offsets that run past the list arrays: no pair kernel may read
+// them, so the evaluation gets no work items (it is repeated, or reported).
+__global__ void drop_items_on_overflow(int *scal) {
+    if (scal[S_ERROR] & (E_LISTCAP | E_STACK)) scal[S_NITEMS] = 0;
+}
+
 __global__ void fill_items(int n, const int *n_walks, const int *i_first, const int *i_count, int chunk,
                            int split_nj, const int *j_cnt, int *bkt, const int *light_off, WorkItem *items,
                            int *n_items, long long *pairs) {
@@ -529,6 +536,9 @@ struct DensOut {
 // hdr_density.hpp:401-411: converged particles take the result and get rs = 0,
 // the others expand rs by 1.1 and stay in the iteration.
 __global__ void commit_density(int n, double *rs, DensOut tmp, DensOut st, int *scal) {
+    // after a list overflow no density item ran: the state stays as it was
+    // for the repeated evaluation
+    if (scal[S_ERROR] & (E_LISTCAP | E_STACK)) return;
     int local = 0;
     GRID_STRIDE(p, n) {
         if (rs[p] != 0.0) {
@@ -594,9 +604,11 @@ __global__ void gravity_writeback(int n, double G, const double *acc, const doub
 // is at least its own sound speed plus this.
 constexpr int CSMAX_THREADS = 256;
 __global__ void __launch_bounds__(CSMAX_THREADS) walk_csmax(const int *n_walks, const int *j_off, const int *j_idx,
-                                                            const float4 *f_g2, const dbl4 *h2, double *out) {
+                                                            const float4 *f_g2, const dbl4 *h2, double *out,
+                                                            const int *scal) {
     __shared__ double red[CSMAX_THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (scal[S_ERROR] & (E_LISTCAP | E_STACK)) return;   // the lists overflowed (no hydro items either)
     const int nw = *n_walks;
     for (int w = blockIdx.x; w < nw; w += gridDim.x) {
         double m = -INFINITY;
@@ -852,6 +864,10 @@ struct sph_system {
     DevBuf<int> tcnt, toff, tlcnt, tloff;
     DevBuf<int2> tasks;
     int task_cap = 0;
+    // list chunk pool and the chunk ids of each task (single-traversal lists)
+    DevBuf<int> lpool, lchain;
+    long long lpool_chunks = 0;
+    int lchain_max = 0;
     DevBuf<int> roots;   // roots of the refit's bottom subtrees
     long long lcap[4] = {0, 0, 0, 0};
     int *walk_first[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -946,6 +962,10 @@ int alloc_all(sph_system *s) {
     e |= s->tcnt.ensure(n + 1) | s->toff.ensure(n + 1) | s->roots.ensure(n);
     s->task_cap = n / 16 + 4096;
     e |= s->tasks.ensure(s->task_cap) | s->tlcnt.ensure(s->task_cap + 1) | s->tloff.ensure(s->task_cap + 1);
+    s->lchain_max = 64;
+    s->lpool_chunks = (long long)n * 24 / sphtree::LIST_CHUNK + s->task_cap + 1024;
+    e |= s->lpool.ensure((size_t)s->lpool_chunks * sphtree::LIST_CHUNK) |
+         s->lchain.ensure((size_t)s->task_cap * s->lchain_max);
     e |= s->items.ensure(n);
     e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
     e |= s->partial.ensure(RED_BLOCKS * MAX_RED + MAX_RED) | s->box.ensure(8);
@@ -1056,7 +1076,8 @@ int build_tree(sph_system *s) {
 // Grows the task buffers (eager evaluations only) and the CUB scratch that
 // scans them.
 int grow_tasks(sph_system *s, int cap) {
-    int e = s->tasks.ensure(cap) | s->tlcnt.ensure((size_t)cap + 1) | s->tloff.ensure((size_t)cap + 1);
+    int e = s->tasks.ensure(cap) | s->tlcnt.ensure((size_t)cap + 1) | s->tloff.ensure((size_t)cap + 1) |
+            s->lchain.ensure((size_t)cap * s->lchain_max);
     if (e) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "task allocation of %d entries failed", cap);
     s->task_cap = cap;
     size_t b = 0;
@@ -1085,18 +1106,19 @@ void launch_tasks(int mode, bool write, int grid, const sphtree::ListArgs &a, in
     }
 }
 
-void launch_lists(int mode, bool fill, int grid, const sphtree::ListArgs &a, cudaStream_t st) {
+// the chunk pass of the list traversal (sphtree::PASS_CHUNK)
+void launch_lists(int mode, int grid, const sphtree::ListArgs &a, cudaStream_t st) {
     const int th = sphtree::TRAV_WARPS * 32;
-    if (mode == sphtree::GATHER) {
-        if (fill) sphtree::build_lists<sphtree::GATHER, true><<<grid, th, 0, st>>>(a);
-        else sphtree::build_lists<sphtree::GATHER, false><<<grid, th, 0, st>>>(a);
-    } else if (mode == sphtree::SYMMETRIC) {
-        if (fill) sphtree::build_lists<sphtree::SYMMETRIC, true><<<grid, th, 0, st>>>(a);
-        else sphtree::build_lists<sphtree::SYMMETRIC, false><<<grid, th, 0, st>>>(a);
-    } else {
-        if (fill) sphtree::build_lists<sphtree::GRAVITY, true><<<grid, th, 0, st>>>(a);
-        else sphtree::build_lists<sphtree::GRAVITY, false><<<grid, th, 0, st>>>(a);
-    }
+    if (mode == sphtree::GATHER)
+        sphtree::build_lists<sphtree::GATHER, sphtree::PASS_CHUNK><<<grid, th, 0, st>>>(a);
+    else if (mode == sphtree::SYMMETRIC)
+        sphtree::build_lists<sphtree::SYMMETRIC, sphtree::PASS_CHUNK><<<grid, th, 0, st>>>(a);
+    else
+        sphtree::build_lists<sphtree::GRAVITY, sphtree::PASS_CHUNK><<<grid, th, 0, st>>>(a);
+}
+
+__global__ void pool_usage(int *scal) {
+    atomicMax(&scal[S_POOLMAX], scal[S_POOL]);
 }
 
 // Builds the lists of `kind` over the walks (group nodes + radii) and the
@@ -1141,8 +1163,42 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.n_tasks = s->scal.p + S_NTASKS;
     a.count_out = s->tlcnt.p;
     a.offset = s->tloff.p;
-    CUDA_TRY(cudaMemsetAsync(s->tlcnt.p, 0, sizeof(int) * (size_t)(s->task_cap + 1), st));
-    launch_lists(mode, false, tgrid, a, st);
+    a.pool_next = s->scal.p + S_POOL;
+    a.pool_error = s->scal.p + S_POOLERR;
+    // one traversal: counts per task and the entries into pool chunks; in
+    // eager mode the pool and the chains grow until they hold the lists with
+    // a quarter of headroom (graph replays cannot allocate)
+    for (;;) {
+        a.pool = s->lpool.p;
+        a.pool_chunks = s->lpool_chunks;
+        a.chain = s->lchain.p;
+        a.chain_max = s->lchain_max;
+        CUDA_TRY(cudaMemsetAsync(s->tlcnt.p, 0, sizeof(int) * (size_t)(s->task_cap + 1), st));
+        CUDA_TRY(cudaMemsetAsync(s->scal.p + S_POOL, 0, 2 * sizeof(int), st));
+        launch_lists(mode, tgrid, a, st);
+        pool_usage<<<1, 1, 0, st>>>(s->scal.p);
+        if (!eager) break;
+        int pu[2];
+        CUDA_TRY(cudaMemcpyAsync(pu, s->scal.p + S_POOL, sizeof(pu), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        const long long used = pu[0];
+        const bool redo = pu[1] != 0;
+        if (!redo && used + used / 4 <= s->lpool_chunks) break;
+        if (used + used / 4 > s->lpool_chunks) {
+            const long long want = used + used / 2 + 1024;
+            if (s->lpool.ensure((size_t)want * sphtree::LIST_CHUNK))
+                return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list pool allocation of %lld chunks failed", want);
+            s->lpool_chunks = (long long)(s->lpool.cap / sphtree::LIST_CHUNK);
+        }
+        if (pu[1] & 2) {
+            s->lchain_max *= 2;
+            if (s->lchain.ensure((size_t)s->task_cap * s->lchain_max))
+                return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list chain allocation failed");
+        }
+        s->graph_valid = false;
+        s->force_graph_valid = false;
+        if (!redo) break;   // grown for headroom only: this traversal is complete
+    }
     r = exclusive_scan(s, s->tlcnt.p, s->tloff.p, s->task_cap + 1);
     if (r) return r;
     sphtree::group_lists<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], s->toff.p, s->tloff.p,
@@ -1165,10 +1221,10 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
         }
     }
     list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, s->lcap[kind], s->scal.p, s->lscal.p, lslot);
-    // 3. fill
+    // 3. the chunks to their list offsets
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
-    launch_lists(mode, true, tgrid, a, st);
+    sphtree::copy_lists<<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
     const int *icount = item_count ? item_count : s->walk_count[kind];
@@ -1188,6 +1244,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     if (r) return r;
     fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], ifirst, icount, chunk, split_nj, s->lcnt[kind].p,
                                             bkt, s->toff.p, s->items.p, s->scal.p + S_NITEMS, pairs);
+    drop_items_on_overflow<<<1, 1, 0, st>>>(s->scal.p);
     return SPH_OK;
 }
 
@@ -1346,7 +1403,7 @@ int hydro_phase(sph_system *s, bool eager) {
     const bool skip = s->prm.hydro_signal_skip != 0;
     if (skip)
         walk_csmax<<<ctx->sm_count * 8, CSMAX_THREADS, 0, st>>>(s->walk_num[1], s->loff[1].p, s->jidx[1].p,
-                                                     f32 ? s->f_g2.p : nullptr, s->h2.p, s->w_csmax.p);
+                                                     f32 ? s->f_g2.p : nullptr, s->h2.p, s->w_csmax.p, s->scal.p);
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     cudaEventRecord(s->ev[EV_HK_B], st);
     sphk::HydroArgs a{};
@@ -1383,6 +1440,7 @@ int force_body(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     CUDA_TRY(cudaMemsetAsync(s->lscal.p, 0, sizeof(long long) * L_NI, st));
+    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_POOLMAX, 0, sizeof(int), st));
     int r = build_tree(s);
     if (r) return r;
     r = density_phase(s, eager);
@@ -1472,6 +1530,13 @@ int check_headroom(sph_system *s) {
             s->graph_valid = false;
             s->force_graph_valid = false;
         }
+    int pm = 0;
+    CUDA_TRY(cudaMemcpyAsync(&pm, s->scal.p + S_POOLMAX, sizeof(int), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    if ((long long)pm * 5 > s->lpool_chunks * 4) {
+        s->graph_valid = false;
+        s->force_graph_valid = false;
+    }
     return SPH_OK;
 }
 
@@ -1568,6 +1633,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
         s->lcnt[k].release(); s->loff[k].release(); s->jidx[k].release();
         if (k == 0) {
             s->tcnt.release(); s->toff.release(); s->tlcnt.release(); s->tloff.release(); s->tasks.release();
+            s->lpool.release(); s->lchain.release();
             s->roots.release();
         }
     }

@@ -413,7 +413,20 @@ struct ListArgs {
     int *j_idx;
     long long capacity;     // entries available in j_idx
     int *error;             // bit 1: stack overflow, bit 2: capacity exceeded
+    // chunk pass: each task appends its entries to LIST_CHUNK-entry chunks
+    // taken from a pool (pool_next counts the chunks handed out); chain
+    // holds the chunk ids of task t at [t * chain_max, ...).  pool_error:
+    // bit 1 pool exhausted, bit 2 a task needed more than chain_max chunks
+    int *pool;
+    long long pool_chunks;
+    int *pool_next;
+    int *chain;
+    int chain_max;
+    int *pool_error;
 };
+
+constexpr int LIST_CHUNK = 128;   // entries per pool chunk (a multiple of 32)
+enum { PASS_COUNT = 0, PASS_FILL = 1, PASS_CHUNK = 2 };
 
 __device__ __forceinline__ float box_box_d2f(const float4 &alo, const float4 &ahi, const float4 &blo,
                                              const float4 &bhi) {
@@ -585,8 +598,13 @@ __global__ void group_lists(int n, const int *n_groups, const int *task_off, con
     }
 }
 
-template <int MODE, bool FILL>
+// One traversal per task (one warp each).  PASS_COUNT counts the entries of
+// every task; PASS_FILL writes them at the scanned task offsets; PASS_CHUNK
+// counts them and writes them, in the same order, into pool chunks, which
+// copy_lists moves to the scanned offsets (one traversal instead of two).
+template <int MODE, int PASS>
 __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
+    constexpr bool FILL = PASS == PASS_FILL;
     __shared__ int stack[TRAV_WARPS][STACK];
     __shared__ int cand[TRAV_WARPS][CAND];
     __shared__ int cpre[TRAV_WARPS][CAND + 1];
@@ -606,6 +624,38 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
         const float rg = group_radius(a, MODE, g, glo);
         long long out = FILL ? (long long)a.offset[task] : 0;
         int total = 0;
+        // chunk pass: current chunk, its fill, chunks taken by this task
+        int cchunk = -1, cfill = LIST_CHUNK, nch = 0;
+        bool pool_bad = false;
+        // appends the lanes' accepted entries (ballot order) to the task's chunks
+        auto emit = [&](bool ok, int value) {
+            const unsigned m = __ballot_sync(FULL, ok);
+            if (m == 0u) return;
+            const int cnt = __popc(m);
+            int nchunk = -1;
+            if (cfill + cnt > LIST_CHUNK) {
+                if (lane == 0) nchunk = atomicAdd(a.pool_next, 1);
+                nchunk = __shfl_sync(FULL, nchunk, 0);
+                if (nchunk >= a.pool_chunks || nch >= a.chain_max) {
+                    if (lane == 0) atomicOr(a.pool_error, nchunk >= a.pool_chunks ? 1 : 2);
+                    pool_bad = true;
+                } else if (lane == 0) {
+                    a.chain[(size_t)task * a.chain_max + nch] = nchunk;
+                }
+                ++nch;
+            }
+            if (ok && !pool_bad) {
+                const int pos = cfill + __popc(m & lt_mask);
+                const int ch = pos < LIST_CHUNK ? cchunk : nchunk;
+                a.pool[(size_t)ch * LIST_CHUNK + (pos < LIST_CHUNK ? pos : pos - LIST_CHUNK)] = value;
+            }
+            if (nchunk >= 0) {
+                cchunk = nchunk;
+                cfill = cfill + cnt - LIST_CHUNK;
+            } else {
+                cfill += cnt;
+            }
+        };
         int sp = 1, nc = 0;
         if (lane == 0) stack[wid][0] = tk.y;
         __syncwarp();
@@ -639,6 +689,7 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
                 }
                 // accepted monopoles (gravity)
                 if (MODE == GRAVITY) {
+                    if (PASS == PASS_CHUNK) emit(accept, a.n + node);
                     const unsigned am = __ballot_sync(FULL, accept);
                     if (FILL && accept) {
                         const long long w = out + __popc(am & lt_mask);
@@ -702,6 +753,7 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
                             const float r = widen(MODE == SYMMETRIC ? fmaxf(rg, x[u].w) : rg, slack);
                             ok = point_box_d2f(x[u].x, x[u].y, x[u].z, glo, ghi) <= r * r;
                         }
+                        if (PASS == PASS_CHUNK) emit(ok, p[u]);
                         const unsigned om = __ballot_sync(FULL, ok);
                         if (FILL && ok) {
                             const long long w = out + __popc(om & lt_mask);
@@ -719,6 +771,34 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
         }
         if (overflow && lane == 0) atomicOr(a.error, 1);
         if (!FILL && lane == 0) a.count_out[task] = total;
+    }
+}
+
+// Moves each task's chunks (PASS_CHUNK) to its scanned list offset; one warp
+// per task, coalesced.  After a pool or chain overflow nothing is copied and
+// the list-capacity error is raised (the evaluation is then repeated with
+// larger buffers).
+__global__ void copy_lists(ListArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int n_tasks = *a.n_tasks;
+    if (*a.pool_error) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.error, 2);
+        return;
+    }
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < n_tasks; task += warps) {
+        const int total = a.count_out[task];
+        const long long off = a.offset[task];
+        const int *chain = a.chain + (size_t)task * a.chain_max;
+        for (int k0 = 0; k0 < total; k0 += 32) {
+            const int k = k0 + lane;
+            if (k < total) {
+                const int ch = chain[k0 / LIST_CHUNK];
+                const long long w = off + k;
+                if (w < a.capacity) a.j_idx[w] = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
+                else atomicOr(a.error, 2);
+            }
+        }
     }
 }
 
