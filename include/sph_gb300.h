@@ -490,9 +490,10 @@ int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t
 int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);
 
 /* Kernel launches per replay of the captured graph: step = 1 for the
- * sph_system_step graph, 0 for the sph_system_compute_forces graph (every
- * kernel node of the graph, including the predicated density iterations
- * that return at once when no particle iterates).  SPH_ERR_STATE when that
+ * sph_system_step graph, 0 for the sph_system_compute_forces graph: its
+ * kernel nodes plus, for the density re-walks (a conditional while-node of
+ * the graph that runs while particles still iterate), the loop body's kernel
+ * nodes times the re-walks of the last evaluation.  SPH_ERR_STATE when that
  * graph has not been captured. */
 int sph_system_graph_kernels(sph_system *sys, int32_t step, int64_t *kernels);
 

@@ -559,6 +559,25 @@ __global__ void commit_density(int n, double *rs, DensOut tmp, DensOut st, int *
     if (__any_sync(0xffffffffu, local) && (threadIdx.x & 31) == 0) atomicAdd(&scal[S_UNCONV], 1);
 }
 
+// end of a walk of the captured re-walk loop (its index on the device) and
+// the loop's condition: another walk while particles iterate and walks remain
+__global__ void iteration_end_loop(int *scal, int max_it, cudaGraphConditionalHandle h) {
+    const int it = scal[S_ITERS] - 1;
+    unsigned more = 0;
+    if (scal[S_UNCONV] > 0) {
+        scal[S_ITERS] = it + 2;
+        if (it + 1 >= max_it) atomicOr(&scal[S_ERROR], E_NOTCONV);
+        else more = 1;
+    }
+    scal[S_UNCONV] = 0;
+    cudaGraphSetConditional(h, more);
+}
+
+// entry condition of the re-walk loop: the first walk left particles iterating
+__global__ void rewalk_start(const int *scal, int max_it, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, (scal[S_ITERS] > 1 && max_it > 1) ? 1u : 0u);
+}
+
 __global__ void iteration_end(int *scal, int max_it, int it) {
     if (scal[S_UNCONV] > 0) {
         scal[S_ITERS] = it + 2;
@@ -903,7 +922,12 @@ struct sph_system {
     long long steps = 0;
     int last_status = 0;
 
-    cudaStream_t st() const { return ctx->stream; }
+    // capture of the re-walk loop body runs on body_stream (st_override)
+    cudaStream_t st_override = nullptr;
+    cudaStream_t body_stream = nullptr;
+    long long rewalk_kernels[2] = {0, 0};   // kernel nodes of the loop body (force / step graph)
+    int capturing = -1;                     // graph being captured: 0 force, 1 step
+    cudaStream_t st() const { return st_override ? st_override : ctx->stream; }
     Persist persist(int k) {
         Persist p;
         p.pos = pos[k].p; p.vel = vel[k].p; p.vel2 = vel2[k].p; p.id = id[k].p; p.istar = istar[k].p;
@@ -1248,6 +1272,147 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     return SPH_OK;
 }
 
+long long count_kernel_nodes(cudaGraph_t g);
+
+// Walk `it` of the density iteration (hdr_density.hpp:372-415): 0 walks every
+// particle on the kind-0 lists, >= 1 only the particles still iterating (rs
+// expanded by 1.1) on kind-3 lists.  it < 0: a walk of the captured re-walk
+// loop, whose index is kept on the device and which sets the loop's
+// condition (cond) for the next walk.
+int density_walk(sph_system *s, int it, bool eager, cudaGraphConditionalHandle cond = 0) {
+    const int n = s->n;
+    cudaStream_t st = s->st();
+    sph_context *ctx = s->ctx;
+    const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
+    const int max_it = std::max(1, s->prm.max_density_iterations);
+    const bool first = it == 0;
+    DensOut tmp{s->t_dens.p, s->t_divv.p, s->t_rotv.p, s->t_grdh.p, s->t_ksr.p, s->t_np.p, s->t_itr.p};
+    DensOut out{s->dens.p, s->divv.p, s->rotv.p, s->grdh.p, s->ksr[0].p, s->np.p, nullptr};
+    CUDA_TRY(cudaMemsetAsync(s->aflag.p, 0, sizeof(int) * (size_t)n, st));
+    group_rs_max<<<ctx->sm_count * 8, 256, 0, st>>>(s->scal.p, s->group_first.p, s->group_count.p, s->rs.p,
+                                                     s->g_r.p, s->aflag.p);
+    int r = exclusive_scan(s, s->aflag.p, s->ascan.p);
+    if (r) return r;
+    compact_active<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->aflag.p, s->ascan.p, s->group_node.p,
+                                                s->group_first.p, s->group_count.p, s->g_r.p, s->a_node.p,
+                                                s->a_first.p, s->a_count.p, s->a_r.p, s->scal.p);
+    // i-particles: only those still iterating (all of them in the first walk)
+    iterating_flags<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, s->uflag.p);
+    r = exclusive_scan(s, s->uflag.p, s->uscan.p);
+    if (r) return r;
+    scatter_list<<<grid_for(n), 256, 0, st>>>(n, s->uflag.p, s->uscan.p, s->ulist.p);
+    walk_segments<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->a_first.p, s->a_count.p, s->uflag.p,
+                                               s->uscan.p, s->a_sfirst.p, s->a_scount.p);
+    const int kind = first ? 0 : 3;
+    r = build_lists_and_items(s, kind, s->a_node.p, s->a_r.p, eager, s->lscal.p + (first ? L_PAIRS_D1 : L_PAIRS_D),
+                              s->a_sfirst.p, s->a_scount.p, first ? 32 : 8);
+    if (r) return r;
+    CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+    sphk::DensityArgs a{};
+    a.n_eval = first ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_D1) : nullptr;
+    a.n_pass = first ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_DLISTED) : nullptr;
+    const bool lists = s->prm.density_list_slack > 0.0f;
+    a.nbr = lists ? s->nbr.p : nullptr;
+    a.nbr_cap = NBR_CAP;
+    a.nbr_warps = s->nbr_warps;
+    a.nbr_slack = lists ? s->prm.density_list_slack : 1.0f;
+    a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p; a.i_ksr = s->ksr[0].p;
+    a.i_rs = s->rs.p;
+    a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
+    a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+    a.j_off = s->loff[kind].p; a.j_idx = s->jidx[kind].p; a.queue = s->scal.p + S_QUEUE;
+    a.i_list = s->ulist.p;
+    a.fi = sphk::F32Part{s->f_phi.p, s->f_plo.p, s->f_vhi.p, s->f_vlo.p};
+    a.fj = a.fi;
+    a.o_dens = tmp.dens; a.o_divv = tmp.divv; a.o_rotv = tmp.rotv; a.o_grdh = tmp.grdh; a.o_ksr = tmp.ksr;
+    a.o_np = tmp.np; a.o_itr = tmp.itr;
+    a.eta_ksrh = ctx->prm.eta * KSRH;
+    a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
+    a.ksr_max_dev = (s->prm.ksr_max_mode == 1) ? s->dscal.p + D_KSRMAX : nullptr;
+    a.amb_count = f32 ? s->scal.p + S_AMB : nullptr;
+    a.amb_i = s->amb_i.p;
+    a.amb_w = s->amb_w.p;
+    a.amb_cap = s->amb_cap;
+    a.amb_tol = sphrt::AMB_TOL;
+    if (f32) CUDA_TRY(cudaMemsetAsync(s->scal.p + S_AMB, 0, sizeof(int), st));
+    if (first) cudaEventRecord(s->ev[EV_DENSK_B], st);
+    sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
+    if (first) cudaEventRecord(s->ev[EV_DENSK_E], st);
+    if (f32) {
+        // FP64 recomputation of decision-ambiguous particles (same lists)
+        sphk::make_fixup_items<<<8, 256, 0, st>>>(s->scal.p + S_AMB, s->amb_w.p, s->amb_cap, s->fitems.p,
+                                                  s->scal.p + S_NFIX);
+        accumulate_int<<<1, 1, 0, st>>>(s->scal.p + S_AMB, s->scal.p + S_AMBTOT);
+        CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
+        sphk::DensityArgs f = a;
+        f.n_eval = nullptr;
+        f.n_pass = nullptr;
+        f.nbr = nullptr;
+        f.items = s->fitems.p;
+        f.n_items_dev = s->scal.p + S_NFIX;
+        f.i_list = s->amb_i.p;
+        f.amb_count = nullptr;
+        sphrt::launch_density(f, SPH_PREC_FP64, ctx->grid[0][1], st);
+    }
+    commit_density<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, tmp, out, s->scal.p);
+    if (it >= 0)
+        iteration_end<<<1, 1, 0, st>>>(s->scal.p, max_it, it);
+    else
+        iteration_end_loop<<<1, 1, 0, st>>>(s->scal.p, max_it, cond);
+    return SPH_OK;
+}
+
+// In a captured graph the re-walks (walks 1 .. max_it-1) form one
+// conditional while-node whose body is a re-walk: it runs only as often as
+// particles still iterate, instead of max_it - 1 captured walks that mostly
+// find nothing to do.  Returns 1 if the graph could not take the node (the
+// caller then captures the walks unrolled).
+int capture_rewalk_loop(sph_system *s, int max_it, int *r_out) {
+    cudaStream_t st = s->st();
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    if (!s->body_stream || cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+        return 1;
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, 0) != cudaSuccess) return 1;
+    rewalk_start<<<1, 1, 0, st>>>(s->scal.p, max_it, h);
+    *r_out = SPH_OK;
+    auto fail = [&](cudaError_t e, const char *what) {
+        *r_out = sphrt::cuda_error(s->ctx, e, what);
+        return 0;
+    };
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return fail(e, "cudaStreamGetCaptureInfo");
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p);
+    if (e != cudaSuccess) return fail(e, "cudaGraphAddNode (re-walk loop)");
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return fail(e, "cudaStreamUpdateCaptureDependencies");
+    e = cudaStreamBeginCaptureToGraph(s->body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return fail(e, "cudaStreamBeginCaptureToGraph");
+    s->st_override = s->body_stream;
+    const int r = density_walk(s, -1, false, h);
+    s->st_override = nullptr;
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(s->body_stream, &got);
+    if (r) {
+        *r_out = r;
+        return 0;
+    }
+    if (e != cudaSuccess) return fail(e, "cudaStreamEndCapture (re-walk loop)");
+    if (s->capturing >= 0) s->rewalk_kernels[s->capturing] = count_kernel_nodes(body);
+    return 0;
+}
+
 int density_phase(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
@@ -1263,85 +1428,31 @@ int density_phase(sph_system *s, bool eager) {
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_ITERS, 1);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_AMBTOT, 0);
     set_int<<<1, 1, 0, st>>>(s->scal.p + S_UNCONV, 0);
-    DensOut tmp{s->t_dens.p, s->t_divv.p, s->t_rotv.p, s->t_grdh.p, s->t_ksr.p, s->t_np.p, s->t_itr.p};
-    DensOut out{s->dens.p, s->divv.p, s->rotv.p, s->grdh.p, s->ksr[0].p, s->np.p, nullptr};
     const int max_it = std::max(1, s->prm.max_density_iterations);
-    for (int it = 0; it < max_it; ++it) {
-        CUDA_TRY(cudaMemsetAsync(s->aflag.p, 0, sizeof(int) * (size_t)n, st));
-        group_rs_max<<<ctx->sm_count * 8, 256, 0, st>>>(s->scal.p, s->group_first.p, s->group_count.p, s->rs.p,
-                                                         s->g_r.p, s->aflag.p);
-        int r = exclusive_scan(s, s->aflag.p, s->ascan.p);
-        if (r) return r;
-        compact_active<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->aflag.p, s->ascan.p, s->group_node.p,
-                                                    s->group_first.p, s->group_count.p, s->g_r.p, s->a_node.p,
-                                                    s->a_first.p, s->a_count.p, s->a_r.p, s->scal.p);
-        // i-particles: only those still iterating (all of them in the first walk)
-        iterating_flags<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, s->uflag.p);
-        r = exclusive_scan(s, s->uflag.p, s->uscan.p);
-        if (r) return r;
-        scatter_list<<<grid_for(n), 256, 0, st>>>(n, s->uflag.p, s->uscan.p, s->ulist.p);
-        walk_segments<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->a_first.p, s->a_count.p, s->uflag.p,
-                                                   s->uscan.p, s->a_sfirst.p, s->a_scount.p);
-        const int kind = it == 0 ? 0 : 3;
-        r = build_lists_and_items(s, kind, s->a_node.p, s->a_r.p, eager, s->lscal.p + (it == 0 ? L_PAIRS_D1 : L_PAIRS_D),
-                                  s->a_sfirst.p, s->a_scount.p, it == 0 ? 32 : 8);
-        if (r) return r;
-        CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
-        sphk::DensityArgs a{};
-        a.n_eval = (it == 0) ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_D1) : nullptr;
-        a.n_pass = (it == 0) ? reinterpret_cast<unsigned long long *>(s->lscal.p + L_DLISTED) : nullptr;
-        const bool lists = s->prm.density_list_slack > 0.0f;
-        a.nbr = lists ? s->nbr.p : nullptr;
-        a.nbr_cap = NBR_CAP;
-        a.nbr_warps = s->nbr_warps;
-        a.nbr_slack = lists ? s->prm.density_list_slack : 1.0f;
-        a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p; a.i_ksr = s->ksr[0].p;
-        a.i_rs = s->rs.p;
-        a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
-        a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
-        a.j_off = s->loff[kind].p; a.j_idx = s->jidx[kind].p; a.queue = s->scal.p + S_QUEUE;
-        a.i_list = s->ulist.p;
-        a.fi = sphk::F32Part{s->f_phi.p, s->f_plo.p, s->f_vhi.p, s->f_vlo.p};
-        a.fj = a.fi;
-        a.o_dens = tmp.dens; a.o_divv = tmp.divv; a.o_rotv = tmp.rotv; a.o_grdh = tmp.grdh; a.o_ksr = tmp.ksr;
-        a.o_np = tmp.np; a.o_itr = tmp.itr;
-        a.eta_ksrh = ctx->prm.eta * KSRH;
-        a.ksr_max = ctx->prm.ksr_max > 0.0 ? ctx->prm.ksr_max : std::numeric_limits<double>::infinity();
-        a.ksr_max_dev = (s->prm.ksr_max_mode == 1) ? s->dscal.p + D_KSRMAX : nullptr;
-        a.amb_count = f32 ? s->scal.p + S_AMB : nullptr;
-        a.amb_i = s->amb_i.p;
-        a.amb_w = s->amb_w.p;
-        a.amb_cap = s->amb_cap;
-        a.amb_tol = sphrt::AMB_TOL;
-        if (f32) CUDA_TRY(cudaMemsetAsync(s->scal.p + S_AMB, 0, sizeof(int), st));
-        if (it == 0) cudaEventRecord(s->ev[EV_DENSK_B], st);
-        sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
-        if (it == 0) cudaEventRecord(s->ev[EV_DENSK_E], st);
-        if (f32) {
-            // FP64 recomputation of decision-ambiguous particles (same lists)
-            sphk::make_fixup_items<<<8, 256, 0, st>>>(s->scal.p + S_AMB, s->amb_w.p, s->amb_cap, s->fitems.p,
-                                                      s->scal.p + S_NFIX);
-            accumulate_int<<<1, 1, 0, st>>>(s->scal.p + S_AMB, s->scal.p + S_AMBTOT);
-            CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
-            sphk::DensityArgs f = a;
-            f.n_eval = nullptr;
-            f.n_pass = nullptr;
-            f.nbr = nullptr;
-            f.items = s->fitems.p;
-            f.n_items_dev = s->scal.p + S_NFIX;
-            f.i_list = s->amb_i.p;
-            f.amb_count = nullptr;
-            sphrt::launch_density(f, SPH_PREC_FP64, ctx->grid[0][1], st);
-        }
-        commit_density<<<grid_for(n), 256, 0, st>>>(n, s->rs.p, tmp, out, s->scal.p);
-        iteration_end<<<1, 1, 0, st>>>(s->scal.p, max_it, it);
-        if (eager) {
-            // stop on the host once every particle has converged; a captured
-            // graph keeps all iterations, which then find no active walk
+    int r = density_walk(s, 0, eager);
+    if (r) return r;
+    if (eager) {
+        // walk again while particles iterate (the host reads the walk count)
+        for (int it = 1; it < max_it; ++it) {
             int walks = 0;
             CUDA_TRY(cudaMemcpyAsync(&walks, s->scal.p + S_ITERS, sizeof(int), cudaMemcpyDeviceToHost, st));
             CUDA_TRY(cudaStreamSynchronize(st));
-            if (walks <= it + 1) break;
+            if (walks <= it) break;
+            r = density_walk(s, it, true);
+            if (r) return r;
+        }
+    } else if (max_it > 1) {
+        if (s->capturing >= 0) s->rewalk_kernels[s->capturing] = 0;
+        int rr = SPH_OK;
+        if (capture_rewalk_loop(s, max_it, &rr)) {
+            // no conditional node: every re-walk captured (they return at
+            // once when no particle iterates)
+            for (int it = 1; it < max_it; ++it) {
+                r = density_walk(s, it, false);
+                if (r) return r;
+            }
+        } else if (rr) {
+            return rr;
         }
     }
     cudaEventRecord(s->ev[EV_DENS_E], st);
@@ -1588,6 +1699,7 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
         return sphrt::set_error(ctx, SPH_ERR_CUDA, "system allocation for %lld particles failed", (long long)n);
     }
     for (int k = 0; k < EV_N; ++k) cudaEventCreate(&s->ev[k]);
+    cudaStreamCreateWithFlags(&s->body_stream, cudaStreamNonBlocking);
     cudaMemset(s->scal.p, 0, sizeof(int) * S_NI);
     cudaMemset(s->dscal.p, 0, sizeof(double) * D_NI);
     cudaMemset(s->lscal.p, 0, sizeof(long long) * L_NI);
@@ -1603,6 +1715,7 @@ extern "C" int sph_system_destroy(sph_system *s) {
     if (s->force_exec) cudaGraphExecDestroy(s->force_exec);
     for (int k = 0; k < EV_N; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
+    if (s->body_stream) cudaStreamDestroy(s->body_stream);
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->vel[k].release(); s->vel2[k].release(); s->id[k].release();
         s->istar[k].release(); s->orig[k].release(); s->uene[k].release(); s->uene2[k].release();
@@ -1741,7 +1854,9 @@ int capture(sph_system *s, bool step, cudaGraphExec_t *exec) {
     }
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    s->capturing = step ? 1 : 0;
     const int rc = step ? step_body(s, false) : force_body(s, false);
+    s->capturing = -1;
     const cudaError_t ec = cudaStreamEndCapture(st, &g);
     if (rc) {
         if (g) cudaGraphDestroy(g);
@@ -1799,7 +1914,10 @@ extern "C" int sph_system_graph_kernels(sph_system *s, int32_t step, int64_t *ke
     const bool valid = step ? s->graph_valid : s->force_graph_valid;
     const long long k = s->graph_kernels[step ? 1 : 0];
     if (!valid || k < 0) return SPH_ERR_STATE;
-    *kernels = k;
+    int walks = 1;
+    CUDA_TRY(cudaMemcpyAsync(&walks, s->scal.p + S_ITERS, sizeof(int), cudaMemcpyDeviceToHost, s->st()));
+    CUDA_TRY(cudaStreamSynchronize(s->st()));
+    *kernels = k + s->rewalk_kernels[step ? 1 : 0] * (long long)std::max(0, walks - 1);
     return SPH_OK;
 }
 
