@@ -1248,7 +1248,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // 3. the chunks to their list offsets
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
-    sphtree::copy_lists<<<tgrid, sphtree::TRAV_WARPS * 32, 0, st>>>(a);
+    sphtree::copy_lists<<<s->ctx->sm_count * 8, sphtree::COPY_THREADS, 0, st>>>(a);
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
     const int *icount = item_count ? item_count : s->walk_count[kind];

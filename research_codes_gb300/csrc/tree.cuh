@@ -774,30 +774,28 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
     }
 }
 
-// Moves each task's chunks (PASS_CHUNK) to its scanned list offset; one warp
-// per task, coalesced.  After a pool or chain overflow nothing is copied and
-// the list-capacity error is raised (the evaluation is then repeated with
-// larger buffers).
-__global__ void copy_lists(ListArgs a) {
-    const int lane = threadIdx.x & 31;
+// Moves each task's chunks (PASS_CHUNK) to its scanned list offset: one
+// block per task, each thread copying every COPY_THREADS-th entry (all loads
+// of a round in flight together; chunk ids come from L1 after the first
+// thread).  After a pool or chain overflow nothing is copied and the
+// list-capacity error is raised (the evaluation is then repeated with larger
+// buffers).
+constexpr int COPY_THREADS = 256;
+__global__ void __launch_bounds__(COPY_THREADS) copy_lists(ListArgs a) {
     const int n_tasks = *a.n_tasks;
     if (*a.pool_error) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.error, 2);
         return;
     }
-    const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; task < n_tasks; task += warps) {
+    for (int task = blockIdx.x; task < n_tasks; task += gridDim.x) {
         const int total = a.count_out[task];
         const long long off = a.offset[task];
         const int *chain = a.chain + (size_t)task * a.chain_max;
-        for (int k0 = 0; k0 < total; k0 += 32) {
-            const int k = k0 + lane;
-            if (k < total) {
-                const int ch = chain[k0 / LIST_CHUNK];
-                const long long w = off + k;
-                if (w < a.capacity) a.j_idx[w] = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
-                else atomicOr(a.error, 2);
-            }
+        for (int k = threadIdx.x; k < total; k += COPY_THREADS) {
+            const int ch = chain[k / LIST_CHUNK];
+            const long long w = off + k;
+            if (w < a.capacity) a.j_idx[w] = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
+            else atomicOr(a.error, 2);
         }
     }
 }
