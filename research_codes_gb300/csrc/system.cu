@@ -138,16 +138,27 @@ struct KsrMaxSums : SumOp {
 };
 
 // per-particle time step, hdr_hgas.hpp:477-488
+// (f32: the candidate steps in FP32 arithmetic; GB300's FP64 divide and
+// square root cost tens of FP64 instructions each)
 struct TimestepMin : MinOp {
     static constexpr int K = 1;
     const double *ksr, *vsmx, *divv, *accg1, *accg2;
     double c_dt, dt_max;
+    bool f32;
     __device__ void operator()(int p, double *a) const {
-        const double dth = c_dt * ksr[p] / (vsmx[p] * KSRH);
-        const double dtd = (divv[p] < 0.0) ? (-c_dt / divv[p]) : dt_max;
         const double gx = accg1[3 * p] + accg2[3 * p], gy = accg1[3 * p + 1] + accg2[3 * p + 1],
                      gz = accg1[3 * p + 2] + accg2[3 * p + 2];
-        const double dtg = c_dt * sqrt(ksr[p] / sqrt(gx * gx + gy * gy + gz * gz));
+        double dth, dtd, dtg;
+        if (f32) {
+            const float c = (float)c_dt, h = (float)ksr[p], dv = (float)divv[p];
+            dth = (double)(c * h / ((float)vsmx[p] * (float)KSRH));
+            dtd = (dv < 0.0f) ? (double)(-c / dv) : dt_max;
+            dtg = (double)(c * sqrtf(h / sqrtf((float)(gx * gx + gy * gy + gz * gz))));
+        } else {
+            dth = c_dt * ksr[p] / (vsmx[p] * KSRH);
+            dtd = (divv[p] < 0.0) ? (-c_dt / divv[p]) : dt_max;
+            dtg = c_dt * sqrt(ksr[p] / sqrt(gx * gx + gy * gy + gz * gz));
+        }
         const double d = fmin(fmin(dth, dt_max), fmin(dtg, dtd));
         a[0] = fmin(a[0], d);
     }
@@ -586,18 +597,31 @@ __global__ void iteration_end(int *scal, int max_it, int it) {
     scal[S_UNCONV] = 0;
 }
 
-// EOS (hdr_hgas.hpp:339-342), Balsara (hdr_sph.hpp:79-81), softening eps^2
+// EOS (hdr_hgas.hpp:339-342), Balsara (hdr_sph.hpp:79-81), softening eps^2.
+// f32 (FP32C runs): sound speed and Balsara switch in FP32 arithmetic (they
+// feed the FP32 pair records; FP64 divide and square root cost tens of FP64
+// instructions each on GB300), with c = sqrt((1 + 1/n) P / rho) as
+// sqrt((1 + 1/n) u / n); the FP64 engine keeps the reference's FP64 forms.
 __global__ void post_density(int n, const dbl4 *pos, const double *dens, const double *uene,
                              const double *divv, const double *rotv, const double *ksr, double *pres,
-                             double *vsnd, double *bswt, double *eps2, dbl4 *pe) {
+                             double *vsnd, double *bswt, double *eps2, dbl4 *pe, bool f32) {
     const double ninv = 1.0 / 1.5;
     GRID_STRIDE(p, n) {
         const double P = ninv * dens[p] * uene[p];
-        const double c = sqrt((1.0 + ninv) * P / dens[p]);
+        double c, b;
+        if (f32) {
+            const float cf = sqrtf((float)((1.0 + ninv) * ninv * uene[p]));
+            const float ad = fabsf((float)divv[p]);
+            c = (double)cf;
+            b = (double)(ad / (ad + fabsf((float)rotv[p]) + 1e-4f * cf * (float)KSRH / (float)ksr[p]));
+        } else {
+            c = sqrt((1.0 + ninv) * P / dens[p]);
+            const double ad = fabs(divv[p]);
+            b = ad / (ad + fabs(rotv[p]) + 1e-4 * c * KSRH / ksr[p]);
+        }
         pres[p] = P;
         vsnd[p] = c;
-        const double ad = fabs(divv[p]);
-        bswt[p] = ad / (ad + fabs(rotv[p]) + 1e-4 * c * KSRH / ksr[p]);
+        bswt[p] = b;
         const double e2 = (ksr[p] / KSRH) * (ksr[p] / KSRH);
         eps2[p] = e2;
         const dbl4 x = pos[p];
@@ -608,10 +632,16 @@ __global__ void post_density(int n, const dbl4 *pos, const double *dens, const d
 // Gravity write-back, hdr_gravity.hpp:107-113
 __global__ void gravity_writeback(int n, double G, const double *acc, const double *pot, const double *etas,
                                   const double *ksr, const double *grdh, const double *dens, double *accg2,
-                                  double *pot_out, double *eta_out) {
+                                  double *pot_out, double *eta_out, bool f32) {
     GRID_STRIDE(p, n) {
         for (int c = 0; c < 3; ++c) accg2[3 * p + c] = G * acc[3 * p + c];
-        eta_out[p] = ksr[p] * ksr[p] / (KSRH * KSRH) * grdh[p] / (3.0 * dens[p]) * etas[p];
+        if (f32) {   // eta feeds the FP32 hydro records
+            const float h = (float)ksr[p];
+            eta_out[p] = (double)(h * h / (float)(KSRH * KSRH) * (float)grdh[p] / (3.0f * (float)dens[p]) *
+                                  (float)etas[p]);
+        } else {
+            eta_out[p] = ksr[p] * ksr[p] / (KSRH * KSRH) * grdh[p] / (3.0 * dens[p]) * etas[p];
+        }
         pot_out[p] = G * pot[p];
     }
 }
@@ -658,9 +688,18 @@ __global__ void __launch_bounds__(CSMAX_THREADS) walk_csmax(const int *n_walks, 
 __global__ void hydro_prep(int n, const double *ksr, const double *pres, const double *grdh,
                            const double *dens, const double *bswt, const double *vsnd, const double *alph,
                            const double *alphu, const double *uene, const double *eta, dbl4 *h1, dbl4 *h2,
-                           double2 *h3) {
+                           double2 *h3, bool f32) {
     GRID_STRIDE(p, n) {
-        h1[p] = make_dbl4(1.0 / ksr[p], pres[p], pres[p] * grdh[p] / (dens[p] * dens[p]), 0.5 * bswt[p]);
+        double hinv, presc;
+        if (f32) {   // FP32 pair records: 1/h and P Omega / rho^2 in FP32 arithmetic
+            const float d = (float)dens[p];
+            hinv = (double)(1.0f / (float)ksr[p]);
+            presc = (double)((float)pres[p] * (float)grdh[p] / (d * d));
+        } else {
+            hinv = 1.0 / ksr[p];
+            presc = pres[p] * grdh[p] / (dens[p] * dens[p]);
+        }
+        h1[p] = make_dbl4(hinv, pres[p], presc, 0.5 * bswt[p]);
         h2[p] = make_dbl4(dens[p], vsnd[p], alph[p], alphu[p]);
         h3[p] = make_double2(fmax(uene[p] - 0.0, 0.0), eta[p]);
     }
@@ -678,7 +717,7 @@ __global__ void hydro_writeback(int n, double G, const double *acch_r, const dou
                                 double *vsmx, double *diffu, const double *divv, const double *alph,
                                 const double *alphu, const double *vsnd, const double *ksr,
                                 const double *uene, const double *epsu, AlphaParams ap, double *adot,
-                                double *adotu) {
+                                double *adotu, bool f32) {
     GRID_STRIDE(p, n) {
         for (int c = 0; c < 3; ++c) {
             const double h = acch_r[3 * p + c];
@@ -692,10 +731,14 @@ __global__ void hydro_writeback(int n, double G, const double *acch_r, const dou
         const double df = diffu_r[p];
         diffu[p] = df;
         const double src = fmax(-divv[p] * (ap.amax - alph[p]), 0.0);
-        const double tauinv = (0.25 * KSRH * vsnd[p]) / ksr[p];
+        // f32: the damping rate and conduction source in FP32 arithmetic
+        const double tauinv = f32 ? (double)((0.25f * (float)KSRH * (float)vsnd[p]) / (float)ksr[p])
+                                  : (0.25 * KSRH * vsnd[p]) / ksr[p];
         adot[p] = -(alph[p] - ap.amin) * tauinv + src;
         const double u = fmax(uene[p] - 0.0, 0.0);
-        const double srcu = ksr[p] / KSRH * fabs(df) / sqrt(u + *epsu) * fmax(ap.aumax - alphu[p], 0.0);
+        const double srcu = f32 ? (double)((float)ksr[p] / (float)KSRH * fabsf((float)df) / sqrtf((float)(u + *epsu)) *
+                                           (float)fmax(ap.aumax - alphu[p], 0.0))
+                                : ksr[p] / KSRH * fabs(df) / sqrt(u + *epsu) * fmax(ap.aumax - alphu[p], 0.0);
         adotu[p] = -(alphu[p] - ap.aumin) * tauinv + srcu;
     }
 }
@@ -1492,7 +1535,8 @@ int gravity_phase(sph_system *s, bool eager) {
     sphrt::launch_gravity(a, ctx->prm.precision, ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st);
     cudaEventRecord(s->ev[EV_GK_E], st);
     gravity_writeback<<<grid_for(n), 256, 0, st>>>(n, s->prm.G, s->r_acc.p, s->r_pot.p, s->r_eta.p, s->ksr[0].p,
-                                                   s->grdh.p, s->dens.p, s->accg2.p, s->pot.p, s->eta.p);
+                                                   s->grdh.p, s->dens.p, s->accg2.p, s->pot.p, s->eta.p,
+                                                   ctx->prm.precision == SPH_PREC_FP32C);
     return SPH_OK;
 }
 
@@ -1503,7 +1547,7 @@ int hydro_phase(sph_system *s, bool eager) {
     cudaEventRecord(s->ev[EV_HLIST_B], st);
     hydro_prep<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->pres.p, s->grdh.p, s->dens.p, s->bswt.p,
                                             s->vsnd.p, s->alph[0].p, s->alphu[0].p, s->uene[0].p, s->eta.p,
-                                            s->h1.p, s->h2.p, s->h3.p);
+                                            s->h1.p, s->h2.p, s->h3.p, ctx->prm.precision == SPH_PREC_FP32C);
     if (ctx->prm.precision == SPH_PREC_FP32C)
         sphk::make_hydro_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->vel[0].p, s->h1.p, s->h2.p,
                                                               s->h3.p, s->f_phi.p, s->f_plo.p, s->f_vhi.p,
@@ -1542,7 +1586,8 @@ int hydro_phase(sph_system *s, bool eager) {
     hydro_writeback<<<grid_for(n), 256, 0, st>>>(
         n, s->prm.G, s->r_acch.p, s->r_accg.p, s->r_udot.p, s->r_vsmx.p, s->r_diffu.p, s->acch.p, s->accg1.p,
         s->accg2.p, s->acc.p, s->udot.p, s->vsmx.p, s->diffu.p, s->divv.p, s->alph[0].p, s->alphu[0].p,
-        s->vsnd.p, s->ksr[0].p, s->uene[0].p, s->dscal.p + D_EPSU, ap, s->adot.p, s->adotu.p);
+        s->vsnd.p, s->ksr[0].p, s->uene[0].p, s->dscal.p + D_EPSU, ap, s->adot.p, s->adotu.p,
+        ctx->prm.precision == SPH_PREC_FP32C);
     return SPH_OK;
 }
 
@@ -1557,7 +1602,8 @@ int force_body(sph_system *s, bool eager) {
     r = density_phase(s, eager);
     if (r) return r;
     post_density<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->dens.p, s->uene[0].p, s->divv.p, s->rotv.p,
-                                              s->ksr[0].p, s->pres.p, s->vsnd.p, s->bswt.p, s->eps2.p, s->pe.p);
+                                              s->ksr[0].p, s->pres.p, s->vsnd.p, s->bswt.p, s->eps2.p, s->pe.p,
+                                              s->ctx->prm.precision == SPH_PREC_FP32C);
     r = refit_tree(s);   // h (max h, softening) changed in the density phase
     if (r) return r;
     r = gravity_phase(s, eager);
@@ -1591,6 +1637,7 @@ int step_body(sph_system *s, bool eager) {
     TimestepMin ft{};
     ft.ksr = s->ksr[0].p; ft.vsmx = s->vsmx.p; ft.divv = s->divv.p; ft.accg1 = s->accg1.p;
     ft.accg2 = s->accg2.p; ft.c_dt = s->prm.c_dt; ft.dt_max = s->prm.dt_max;
+    ft.f32 = s->ctx->prm.precision == SPH_PREC_FP32C;
     reduce(s, ft, s->dscal.p + D_DTC);
     update_dt<<<1, 1, 0, st>>>(s->dscal.p, s->scal.p, s->prm.dt_max, s->prm.dt_min);
     predict<<<grid_for(n), 256, 0, st>>>(n, s->dscal.p, s->pos[0].p, s->vel[0].p, s->vel2[0].p, s->acc.p,
