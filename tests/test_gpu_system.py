@@ -38,12 +38,21 @@ def _two_stars(n=6000, seed=5, eta=1.18):
     return state_from_ic(s)
 
 
-@pytest.fixture(scope="module", params=["fp32c", "fp64"])
+@pytest.fixture(scope="module", params=[("fp32c", "spin"), ("fp64", "spin"), ("fp32c", "static"), ("fp64", "static")],
+                ids=["fp32c-spin4k", "fp64-spin4k", "fp32c-static10k", "fp64-static10k"])
 def evaluated(request):
     """A star whose forces were evaluated twice (the second evaluation starts
-    from converged h, so its density pass is a single walk)."""
-    prec = request.param
-    s = _star()
+    from converged h, so its density pass is a single walk): a 4k-particle
+    n=1.5 polytrope with spin and random velocities, and the 10k-particle
+    1 Msun / 1 Rsun n=1.5 polytrope at rest of the single-star relaxation
+    workload."""
+    prec, kind = request.param
+    if kind == "spin":
+        s = _star()
+    else:
+        s, _ = ic.config_system("c0")
+        s = state_from_ic(s)
+        s["vel"] = np.zeros_like(s["pos"])
     ctx = functors.Context(precision=prec, eta=1.18, ksr_max=0.0)
     sys = ParticleSystem(ctx, len(s["mass"]), n_group=64, use_graph=0, ksr_max_mode=0)
     sys.upload(s)
