@@ -394,6 +394,12 @@ typedef struct sph_system_stats {
                                              velocity terms provably could not
                                              raise any lane's maximum (skipped)  */
     int64_t hydro_sv_tiles;               /* hydro tiles tested                   */
+    int64_t hydro_pairs_marked;           /* hydro pairs inside either support
+                                             (the terms evaluated in full)       */
+    int64_t hydro_pair_slots;             /* lane slots the loops over them took
+                                             (32 x the largest per-lane count of
+                                             each tile); marked / slots is the
+                                             lane utilisation of those loops     */
     int32_t last_status;
 } sph_system_stats;
 

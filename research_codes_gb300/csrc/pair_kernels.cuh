@@ -33,11 +33,27 @@
 #ifndef SPH_GRAVITY_MIN_BLOCKS
 #define SPH_GRAVITY_MIN_BLOCKS 4
 #endif
+// Unroll factors of the full-tile FP32C loops: f32x2 iterations (two entries
+// each) of the gravity and packed density loops, entries of the hydro
+// mark-only loop.
+#ifndef SPH_GRAVITY_UNROLL
+#define SPH_GRAVITY_UNROLL 16
+#endif
+#ifndef SPH_DENSITY_UNROLL
+#define SPH_DENSITY_UNROLL 4
+#endif
+#ifndef SPH_HYDRO_MARK_UNROLL
+#define SPH_HYDRO_MARK_UNROLL 8
+#endif
 #ifndef SPH_HYDRO_MIN_BLOCKS
 #define SPH_HYDRO_MIN_BLOCKS 4
 #endif
 
 namespace sphk {
+
+constexpr int GRAVITY_UNROLL = SPH_GRAVITY_UNROLL;
+constexpr int DENSITY_UNROLL = SPH_DENSITY_UNROLL;
+constexpr int HYDRO_MARK_UNROLL = SPH_HYDRO_MARK_UNROLL;
 
 // Double-float particle records of FP32C mode.
 struct F32Part {
@@ -388,7 +404,7 @@ density_kernel(const DensityArgs a) {
                 f2 PART = f2_make(0.0f, 0.0f);
                 int c2 = 0;
                 unsigned msk = 0;
-#pragma unroll 4
+#pragma unroll DENSITY_UNROLL
                 for (int k = 0; k < 32; k += 2) {
                     const f2 DX = f2_fma(f2_lds(&s_rx[wid][head + k]), NEG, XI);
                     const f2 DY = f2_fma(f2_lds(&s_ry[wid][head + k]), NEG, YI);
@@ -712,6 +728,10 @@ struct HydroArgs {
     // when set: [0] 32-entry tiles whose signal-velocity terms were skipped,
     // [1] tiles evaluated
     unsigned long long *n_skip = nullptr;
+    // when set: [0] marked pairs (inside either support, evaluated in
+    // full), [1] lane slots their loops occupied (per 32-entry tile, 32 x
+    // the largest per-lane count)
+    unsigned long long *n_mark = nullptr;
 };
 
 template <bool F64, int WARPS>
@@ -820,7 +840,7 @@ hydro_kernel(const HydroArgs a) {
         }
         // true when no pair term of the n-entry tile at bound[] can exceed
         // any lane's running maximum
-        unsigned n_skipped = 0, n_tiles = 0;
+        unsigned n_skipped = 0, n_tiles = 0, n_marked = 0, n_slots = 0;
         auto skip_tile = [&](const R *bound, int stride, int n) -> bool {
             if (!a.sv_skip) return false;
             R b = (lane < n) ? bound[lane * stride] : (R)0;
@@ -959,7 +979,7 @@ hydro_kernel(const HydroArgs a) {
             unsigned msk = 0;
             if (skip_tile(&s_nb[wid][nhead], 1, n)) {
                 if (tpi == 1 && n == 32) {
-#pragma unroll 8
+#pragma unroll HYDRO_MARK_UNROLL
                     for (int k = 0; k < 32; ++k) mark_only(nhead + k, msk);
                 } else {
                     for (int k = sub; k < n; k += tpi) mark_only(nhead + k, msk);
@@ -969,6 +989,11 @@ hydro_kernel(const HydroArgs a) {
                 for (int k = 0; k < 32; ++k) signal(nhead + k, msk);
             } else {
                 for (int k = sub; k < n; k += tpi) signal(nhead + k, msk);
+            }
+            if (a.n_mark) {
+                const unsigned c = __popc(msk);
+                n_marked += c;
+                n_slots += 32u * __reduce_max_sync(FULL, c);
             }
             while (msk) {
                 const int k = __ffs(msk) - 1;
@@ -1112,6 +1137,13 @@ hydro_kernel(const HydroArgs a) {
         if (a.n_skip && lane == 0) {
             atomicAdd(a.n_skip, (unsigned long long)n_skipped);
             atomicAdd(a.n_skip + 1, (unsigned long long)n_tiles);
+        }
+        if (a.n_mark) {
+            const unsigned m = __reduce_add_sync(FULL, n_marked);
+            if (lane == 0) {
+                atomicAdd(a.n_mark, (unsigned long long)m);
+                atomicAdd(a.n_mark + 1, (unsigned long long)n_slots);
+            }
         }
     }
 }
@@ -1334,7 +1366,7 @@ gravity_kernel(const GravityArgs a) {
                 const f2 ZI = f2_make((float)zi, (float)zi), EI = f2_make((float)e2i, (float)e2i);
                 const f2 NEG = f2_make(-1.0f, -1.0f);
                 f2 AX = f2_make(0.0f, 0.0f), AY = AX, AZ = AX, PT = AX, ET = AX;
-#pragma unroll 4
+#pragma unroll GRAVITY_UNROLL
                 for (int k = 0; k < 32; k += 2) {
                     const f2 DX = f2_fma(f2_lds(&s_x[wid][k]), NEG, XI);
                     const f2 DY = f2_fma(f2_lds(&s_y[wid][k]), NEG, YI);

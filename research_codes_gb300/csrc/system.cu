@@ -48,7 +48,7 @@ enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN
        D_R2, D_DN, D_NI };
 // 64-bit counters
 enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_EVAL_D1,
-       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_DLISTED, L_DSWEPT, L_HSKIP, L_HTILES, L_NI };
+       L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_DLISTED, L_DSWEPT, L_HSKIP, L_HTILES, L_HMARK, L_HSLOTS, L_NI };
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
@@ -1565,6 +1565,7 @@ int hydro_phase(sph_system *s, bool eager) {
     a.n_eval_near = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HN);
     a.n_eval_far = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HF);
     a.n_skip = reinterpret_cast<unsigned long long *>(s->lscal.p + L_HSKIP);
+    a.n_mark = reinterpret_cast<unsigned long long *>(s->lscal.p + L_HMARK);
     a.walk_csmax = skip ? s->w_csmax.p : nullptr;
     a.sv_skip = skip ? 1 : 0;
     a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p;
@@ -2215,6 +2216,8 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->density_sweep_passes = lc[L_DSWEPT];
     o->hydro_sv_tiles_skipped = lc[L_HSKIP];
     o->hydro_sv_tiles = lc[L_HTILES];
+    o->hydro_pairs_marked = lc[L_HMARK];
+    o->hydro_pair_slots = lc[L_HSLOTS];
     o->last_status = s->last_status;
     return SPH_OK;
 }

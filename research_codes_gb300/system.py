@@ -47,7 +47,7 @@ class SystemStats(ctypes.Structure):
                 ("evals_density_first", _I64), ("evals_density_grad", _I64), ("evals_hydro_near", _I64),
                 ("evals_hydro_far", _I64), ("density_list_passes", _I64),
                 ("density_sweep_passes", _I64), ("hydro_sv_tiles_skipped", _I64), ("hydro_sv_tiles", _I64),
-                ("last_status", _I32)]
+                ("hydro_pairs_marked", _I64), ("hydro_pair_slots", _I64), ("last_status", _I32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
