@@ -803,7 +803,11 @@ hydro_kernel(const HydroArgs a) {
         // term undercuts; a tile whose bound (with a 1e-5 relative margin over
         // the rounding of both) stays below every lane's running maximum adds
         // nothing to it and skips those terms: the maximum is unchanged bit
-        // for bit.
+        // for bit.  The margin also covers the approximate square root of d.
+        // Entries beyond both supports are tested as each 32-entry chunk of
+        // the list arrives, against the running maximum at that point (which
+        // only grows), and are staged in the far ring only when the test
+        // fails.
         R vcx, vcy, vcz;
         float lcx = 0.0f, lcy = 0.0f, lcz = 0.0f;
         if (F64) {
@@ -818,7 +822,7 @@ hydro_kernel(const HydroArgs a) {
             const R ex = fabs(hx - vcx) + (R)fabsf(lx - lcx);
             const R ey = fabs(hy - vcy) + (R)fabsf(ly - lcy);
             const R ez = fabs(hz - vcz) + (R)fabsf(lz - lcz);
-            return sqrt(ex * ex + ey * ey + ez * ez);
+            return sqrt_bound(ex * ex + ey * ey + ez * ez);
         };
         auto sv_bound = [&](R cs, R d) -> R {
             const R b = cs + (R)3 * d;
@@ -838,12 +842,10 @@ hydro_kernel(const HydroArgs a) {
             const R v0 = cs_i + (R)a.walk_csmax[r.walk];
             vsmx = (v0 > (R)0) ? v0 : (R)0;
         }
-        // true when no pair term of the n-entry tile at bound[] can exceed
-        // any lane's running maximum
         unsigned n_skipped = 0, n_tiles = 0, n_marked = 0, n_slots = 0;
-        auto skip_tile = [&](const R *bound, int stride, int n) -> bool {
-            if (!a.sv_skip) return false;
-            R b = (lane < n) ? bound[lane * stride] : (R)0;
+        // true when no pair term with any lane's bound b can exceed any
+        // lane's running maximum
+        auto below = [&](R b) -> bool {
             R t;
             if constexpr (F64) {
                 t = b;
@@ -861,6 +863,11 @@ hydro_kernel(const HydroArgs a) {
             ++n_tiles;
             if (all) ++n_skipped;
             return all;
+        };
+        // the same for the n-entry ring tile at bound[]
+        auto skip_tile = [&](const R *bound, int stride, int n) -> bool {
+            if (!a.sv_skip) return false;
+            return below((lane < n) ? bound[lane * stride] : (R)0);
         };
         int nhead = 0, nfill = 0, fhead = 0, ffill = 0;
         long long kept_n = 0, kept_f = 0;
@@ -1084,20 +1091,29 @@ hydro_kernel(const HydroArgs a) {
                 }
                 s_id[wid][k] = a.j_id[j];
             }
+            // far entries: their signal-velocity bound, and the whole chunk's
+            // far entries dropped when none can raise any lane's maximum
+            R bfar = 0;
             if (far) {
-                const int k = (fhead + ffill + __popc(mf & lt)) & 63;
-                if (F64) {
+                if constexpr (F64)
+                    bfar = sv_bound(g2_64.y, dvel(v64.x, v64.y, v64.z, 0.0f, 0.0f, 0.0f));
+                else
+                    bfar = sv_bound((R)g2.y, dvel(vh.x, vh.y, vh.z, lcx, lcy, lcz));
+            }
+            unsigned ms = mf;
+            if (a.sv_skip && mf && below(far ? bfar : (R)0)) ms = 0;
+            if (ms & (1u << lane)) {
+                const int k = (fhead + ffill + __popc(ms & lt)) & 63;
+                if constexpr (F64) {
                     s_fp[wid][k] = Real<F64>::make4(px, py, pz, g2_64.y);
-                    s_fv[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z,
-                                                    sv_bound(g2_64.y, dvel(v64.x, v64.y, v64.z, 0.0f, 0.0f, 0.0f)));
+                    s_fv[wid][k] = Real<F64>::make4(v64.x, v64.y, v64.z, bfar);
                 } else {
                     s_fp[wid][k] = Real<F64>::make4(px, py, pz, (R)g2.y);
-                    s_fv[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z,
-                                                    sv_bound((R)g2.y, dvel(vh.x, vh.y, vh.z, lcx, lcy, lcz)));
+                    s_fv[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, bfar);
                 }
             }
             nfill += __popc(mn);
-            ffill += __popc(mf);
+            ffill += __popc(ms);
             kept_n += __popc(mn);
             kept_f += __popc(mf);
             __syncwarp();

@@ -78,6 +78,15 @@ __device__ __forceinline__ float sqrt_q(float r2, float hinv2) {
 }
 __device__ __forceinline__ double sqrt_q(double r2, double hinv2) { return sqrt(r2 * hinv2); }
 
+// sqrt for bounds that carry a relative margin far above 2^-22: FP32 by
+// sqrt.approx.ftz.f32, FP64 by the library sqrt.
+__device__ __forceinline__ float sqrt_bound(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ double sqrt_bound(double x) { return sqrt(x); }
+
 // Radial kernel-gradient factor W1(q)/c1 with u = (1-q)_+ (hdr_kernel.hpp:251-257).
 // The reference's form u^4 - u^3 (1+4q) subtracts two nearly equal terms for
 // small q; FP32 evaluates the algebraically identical -5 q u^3 instead (no
