@@ -757,6 +757,9 @@ hydro_kernel(const HydroArgs a) {
     __shared__ R4 s_fp[WARPS][64];    // far: centred position, vsnd
     __shared__ R4 s_fv[WARPS][64];    // far: velocity (hi), signal-velocity bound b_j
     __shared__ R s_nb[WARPS][64];     // near: signal-velocity bound b_j
+    // FP32C near entries for the mark test: position in the item frame as one
+    // float (as the support test has it) and h_j^2 widened by 2e-4
+    __shared__ float4 s_m[F64 ? 1 : WARPS][64];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
@@ -835,6 +838,7 @@ hydro_kernel(const HydroArgs a) {
         box.from_lanes(xc, yc, zc);
         const R hm2 = support2<R>(1.0 / (double)hi_i);
         const R hi2_i = hi_i * hi_i;
+        const R h2m_i = rcp_r(hi2_i) * (R)1.0002;   // h_i^2 widened as the support test's
 
         Acc<F64> ax, ay, az, ud, df, gx, gy, gz;
         R vsmx = 0;
@@ -906,8 +910,20 @@ hydro_kernel(const HydroArgs a) {
             const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
             if (!(r2 * hmin2 * (R)1.00002 >= (R)1)) msk |= 1u << (k & 31);
         };
-        // the mark alone (tiles whose signal-velocity terms are skipped)
+        // the mark alone (tiles whose signal-velocity terms are skipped).
+        // FP32C tests r^2 < max(h_i, h_j)^2 (1 + 2e-4) on the one-float item
+        // frame positions of the support test (whose rounding the 2e-4 margin
+        // covers), which marks every pair the exact test marks and a few
+        // beyond both supports; those add exactly zero (W1 = 0 there).
         auto mark_only = [&](int k, unsigned &msk) {
+            if constexpr (!F64) {
+                const float4 M = s_m[wid][k];
+                const float dx = xc - M.x, dy = yc - M.y, dz = zc - M.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float lim = h2m_i > M.w ? h2m_i : M.w;
+                if (!(r2 >= lim)) msk |= 1u << (k & 31);
+                return;
+            }
             const R4 P1 = s_p1[wid][k];
             R dx = xi - P1.x, dy = yi - P1.y, dz = zi - P1.z;
             if (!F64) {
@@ -1036,7 +1052,7 @@ hydro_kernel(const HydroArgs a) {
             int j = 0;
             float4 ph, pl, vh, g2;
             dbl4 p64, v64, g1_64, g2_64;
-            R px = 0, py = 0, pz = 0, hj_inv = 0;
+            R px = 0, py = 0, pz = 0, hj_inv = 0, hj2m = 0;
             if (jk < nj) {
                 j = a.j_idx ? a.j_idx[jb + jk] : jb + jk;
                 if (F64) {
@@ -1057,6 +1073,7 @@ hydro_kernel(const HydroArgs a) {
                 }
                 const R hj = rcp_r(hj_inv);
                 const R hj2 = hj * hj * (R)1.0002;
+                hj2m = hj2;
                 const R rf2 = hj2 > hm2 ? hj2 : hm2;
                 near = !(box.d2(px, py, pz) > rf2) || !(hj2 >= (R)0);
                 far = !near;
@@ -1088,6 +1105,7 @@ hydro_kernel(const HydroArgs a) {
                     s_d[wid][k] = Real<F64>::make4((R)g2.z, (R)g2.w, (R)g3.x, (R)g3.z);
                     s_f[wid][k] = make_float2(g1.y, g3.y);
                     s_nb[wid][k] = sv_bound((R)g2.y, dvel(vh.x, vh.y, vh.z, vl.x, vl.y, vl.z));
+                    if constexpr (!F64) s_m[wid][k] = make_float4(px, py, pz, hj2m);
                 }
                 s_id[wid][k] = a.j_id[j];
             }
