@@ -40,6 +40,10 @@ constexpr int RED_THREADS = 256;
 constexpr int MAX_RED = 8;
 
 // int scalars
+// Every list entry is written through a pool chunk and list offsets are
+// 32-bit: a pool of at most this many chunks keeps every scan of entry counts
+// below 2^31 (lists that would need more are a capacity error).
+constexpr long long MAX_POOL_CHUNKS = 0x7fffffffLL / sphtree::LIST_CHUNK;
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
        S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_POOLMAX, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
@@ -1030,7 +1034,7 @@ int alloc_all(sph_system *s) {
     s->task_cap = n / 16 + 4096;
     e |= s->tasks.ensure(s->task_cap) | s->tlcnt.ensure(s->task_cap + 1) | s->tloff.ensure(s->task_cap + 1);
     s->lchain_max = 64;
-    s->lpool_chunks = (long long)n * 24 / sphtree::LIST_CHUNK + s->task_cap + 1024;
+    s->lpool_chunks = std::min((long long)n * 24 / sphtree::LIST_CHUNK + s->task_cap + 1024, MAX_POOL_CHUNKS);
     e |= s->lpool.ensure((size_t)s->lpool_chunks * sphtree::LIST_CHUNK) |
          s->lchain.ensure((size_t)s->task_cap * s->lchain_max);
     e |= s->items.ensure(n);
@@ -1251,11 +1255,16 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
         const long long used = pu[0];
         const bool redo = pu[1] != 0;
         if (!redo && used + used / 4 <= s->lpool_chunks) break;
-        if (used + used / 4 > s->lpool_chunks) {
-            const long long want = used + used / 2 + 1024;
+        if (redo && used > MAX_POOL_CHUNKS)
+            return sphrt::set_error(s->ctx, SPH_ERR_CAPACITY,
+                                    "the interaction lists need %lld chunks of %d entries, more than 32-bit list "
+                                    "offsets address (smoothing lengths far beyond the particle spacing?)",
+                                    used, sphtree::LIST_CHUNK);
+        if (used + used / 4 > s->lpool_chunks && s->lpool_chunks < MAX_POOL_CHUNKS) {
+            const long long want = std::min(used + used / 2 + 1024, MAX_POOL_CHUNKS);
             if (s->lpool.ensure((size_t)want * sphtree::LIST_CHUNK))
                 return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list pool allocation of %lld chunks failed", want);
-            s->lpool_chunks = (long long)(s->lpool.cap / sphtree::LIST_CHUNK);
+            s->lpool_chunks = std::min((long long)(s->lpool.cap / sphtree::LIST_CHUNK), MAX_POOL_CHUNKS);
         }
         if (pu[1] & 2) {
             s->lchain_max *= 2;

@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(COPY_THREADS) copy_lists(ListArgs a) {
         for (int k = threadIdx.x; k < total; k += COPY_THREADS) {
             const int ch = chain[k / LIST_CHUNK];
             const long long w = off + k;
-            if (w < a.capacity) a.j_idx[w] = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
+            if (w >= 0 && w < a.capacity) a.j_idx[w] = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
             else atomicOr(a.error, 2);
         }
     }
