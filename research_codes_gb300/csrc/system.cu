@@ -1601,8 +1601,9 @@ int hydro_phase(sph_system *s, bool eager) {
     return SPH_OK;
 }
 
-// calcSPHKernel (main.cpp:300-358)
-int force_body(sph_system *s, bool eager) {
+// calcSPHKernel (main.cpp:300-358).  energy: reduce the energies of the
+// evaluated state (a step reduces them once, after its corrector, instead).
+int force_body(sph_system *s, bool eager, bool energy = true) {
     const int n = s->n;
     cudaStream_t st = s->st();
     CUDA_TRY(cudaMemsetAsync(s->lscal.p, 0, sizeof(long long) * L_NI, st));
@@ -1633,9 +1634,11 @@ int force_body(sph_system *s, bool eager) {
         reduce(s, f1, s->dscal.p + D_R2);
         finish_ksrmax<<<1, 1, 0, st>>>(s->dscal.p, 1);
     }
-    Energy fe{};
-    fe.pos = s->pos[0].p; fe.vel = s->vel[0].p; fe.uene = s->uene[0].p; fe.pot = s->pot.p;
-    reduce(s, fe, s->dscal.p + D_EKIN);
+    if (energy) {
+        Energy fe{};
+        fe.pos = s->pos[0].p; fe.vel = s->vel[0].p; fe.uene = s->uene[0].p; fe.pot = s->pot.p;
+        reduce(s, fe, s->dscal.p + D_EKIN);
+    }
     cudaEventRecord(s->ev[EV_END], st);
     return SPH_OK;
 }
@@ -1653,7 +1656,7 @@ int step_body(sph_system *s, bool eager) {
     predict<<<grid_for(n), 256, 0, st>>>(n, s->dscal.p, s->pos[0].p, s->vel[0].p, s->vel2[0].p, s->acc.p,
                                          s->uene[0].p, s->uene2[0].p, s->udot.p, s->alph[0].p, s->alph2[0].p,
                                          s->adot.p, s->alphu[0].p, s->alphu2[0].p, s->adotu.p);
-    int r = force_body(s, eager);
+    int r = force_body(s, eager, false);
     if (r) return r;
     correct<<<grid_for(n), 256, 0, st>>>(n, s->dscal.p, s->vel[0].p, s->vel2[0].p, s->acc.p, s->uene[0].p,
                                          s->uene2[0].p, s->udot.p, s->alph[0].p, s->alph2[0].p, s->adot.p,

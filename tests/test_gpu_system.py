@@ -151,6 +151,45 @@ def test_hydro_matches_oracle_on_engine_lists(evaluated):
     assert err(f["vsmx"][gi], ref["vsmx"]) < 1e-5
 
 
+@pytest.mark.parametrize("prec", ["fp32c", "fp64"])
+def test_long_lists_from_a_first_guess_spanning_the_star(prec):
+    """Every particle's first h spans the whole star, so every walk's density
+    list holds every particle: long lists (task chains grown, items split to
+    several lanes per particle, per-lane neighbour lists overflowed into
+    sweeps).  The evaluation matches the oracle on the engine's lists."""
+    s = _star(n=6000, seed=4)
+    H = 3.0 * float(np.abs(s["pos"]).max())
+    s["ksr"] = np.full(len(s["mass"]), H)
+    ctx = functors.Context(precision=prec, eta=1.18, ksr_max=0.0)
+    sys = ParticleSystem(ctx, len(s["mass"]), n_group=64, use_graph=0, ksr_max_mode=0)
+    try:
+        sys.upload(s)
+        sys.compute_forces()
+        st = sys.stats()
+        assert st["density_iterations"] == 1
+        assert st["density_sweep_passes"] > 0
+        i_first, i_count, j_off, j_idx = sys.lists(0)
+        assert (np.diff(j_off) == sys.n).all()
+        f = _sorted(sys, "pos", "vel", "mass", "id", "dens", "ksr", "grdh", "divv", "rotv", "np")
+        ksr0 = np.full(sys.n, H)
+        state = dict(pos=f["pos"], vel=f["vel"], mass=f["mass"], id=f["id"].astype(np.int64), ksr=ksr0,
+                     rs=1.1 * ksr0)
+        from research_codes_gb300 import walks
+        ref = np.zeros(sys.n, abi.Density)
+        for w in range(len(i_first)):
+            gi = np.arange(i_first[w], i_first[w] + i_count[w])
+            gj = j_idx[j_off[w]:j_off[w + 1]]
+            ref[gi] = orc.density(walks.density_epi(gi, state), walks.density_epj(gj, state), eta=1.18,
+                                  ksr_max=0.0)
+        assert np.abs(f["np"] - ref["np"]).max() <= (0 if prec == "fp64" else 1)
+        for k in ("dens", "ksr", "grdh", "divv", "rotv"):
+            e = err(f[k], ref[k], FLOOR_DERIV if k in DERIV else FLOOR)
+            assert e < _tol(prec, k in DERIV), (k, e)
+    finally:
+        sys.close()
+        ctx.close()
+
+
 def test_density_lists_are_complete(evaluated):
     """Every j within rs_i of an i-particle is in i's walk list (the gather
     rule), checked by brute force on a sample of walks."""
