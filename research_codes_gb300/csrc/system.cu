@@ -56,8 +56,8 @@ enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIR
 // error bits
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
-enum { EV_TREE_B = 0, EV_TREE_E, EV_DENS_B, EV_DENSK_B, EV_DENSK_E, EV_DENS_E, EV_GLIST_B, EV_GK_B, EV_GK_E,
-       EV_HLIST_B, EV_HK_B, EV_HK_E, EV_END, EV_N };
+enum { EV_TREE_B = 0, EV_TREE_E, EV_DENS_B, EV_DENSK_B, EV_DENSK_E, EV_DENS_E, EV_GLIST_B, EV_GLIST_E, EV_GK_B,
+       EV_GK_E, EV_HLIST_B, EV_HK_B, EV_HK_E, EV_END, EV_N };
 
 inline int grid_for(long long n, int threads = 256) {
     long long b = (n + threads - 1) / threads;
@@ -876,6 +876,30 @@ __global__ void fill_double(int n, double *a, double v) {
 }  // namespace
 
 // ======================================================================= system
+// The buffers of one list builder: traversal tasks (per group count/offset,
+// n + 1; per task (group, start node) and list count/offset, task_cap + 1),
+// the chunk pool and the chunk ids of each task, the CUB scratch of its
+// scans, the work items, and its scalars (sc: the system's for builder 0,
+// own for builder 1, whose error bits are merged into the system's before
+// its lists are used).
+struct ListScratch {
+    DevBuf<int> tcnt, toff, tlcnt, tloff;
+    DevBuf<int2> tasks;
+    int task_cap = 0;
+    DevBuf<int> lpool, lchain;
+    long long lpool_chunks = 0;
+    int lchain_max = 0;
+    DevBuf<char> cub;
+    size_t cub_bytes = 0;
+    DevBuf<WorkItem> items;
+    DevBuf<int> own_sc;
+    int *sc = nullptr;
+    void release() {
+        tcnt.release(); toff.release(); tlcnt.release(); tloff.release(); tasks.release();
+        lpool.release(); lchain.release(); cub.release(); items.release(); own_sc.release();
+    }
+};
+
 struct sph_system {
     sph_context *ctx = nullptr;
     int n = 0;
@@ -925,21 +949,14 @@ struct sph_system {
     // lists per kind: 0 density (first walk), 1 hydro, 2 gravity,
     // 3 density re-walks (search radius expanded)
     DevBuf<int> lcnt[4], loff[4], jidx[4];
-    // list traversal tasks: per group count/offset (n + 1), per task
-    // (group, start node) and list count/offset (task_cap + 1)
-    DevBuf<int> tcnt, toff, tlcnt, tloff;
-    DevBuf<int2> tasks;
-    int task_cap = 0;
-    // list chunk pool and the chunk ids of each task (single-traversal lists)
-    DevBuf<int> lpool, lchain;
-    long long lpool_chunks = 0;
-    int lchain_max = 0;
+    // list builders: [0] density, re-walk and hydro lists, [1] gravity lists
+    // (built on a second stream during graph replays, see force_body)
+    ListScratch ls[2];
     DevBuf<int> roots;   // roots of the refit's bottom subtrees
     long long lcap[4] = {0, 0, 0, 0};
     int *walk_first[4] = {nullptr, nullptr, nullptr, nullptr};
     int *walk_count[4] = {nullptr, nullptr, nullptr, nullptr};
     int *walk_num[4] = {nullptr, nullptr, nullptr, nullptr};   // device count of walks
-    DevBuf<WorkItem> items;
     // scalars
     DevBuf<int> scal;
     DevBuf<double> dscal, partial, box;
@@ -954,8 +971,6 @@ struct sph_system {
     DevBuf<double> adj_acc, adj_seed;
     DevBuf<sphadj::AdjItem> adj_items;
     DevBuf<int> adj_cnt, adj_off;
-    DevBuf<char> cub_tmp;
-    size_t cub_bytes = 0;
     // graph
     cudaGraphExec_t step_exec = nullptr;
     bool graph_valid = false;
@@ -972,6 +987,11 @@ struct sph_system {
     // capture of the re-walk loop body runs on body_stream (st_override)
     cudaStream_t st_override = nullptr;
     cudaStream_t body_stream = nullptr;
+    // the gravity list build's stream in captured graphs, and the events that
+    // fork it from and join it to the main stream
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool glist_forked = false;
     long long rewalk_kernels[2] = {0, 0};   // kernel nodes of the loop body (force / step graph)
     int capturing = -1;                     // graph being captured: 0 force, 1 step
     cudaStream_t st() const { return st_override ? st_override : ctx->stream; }
@@ -1030,15 +1050,21 @@ int alloc_all(sph_system *s) {
                          &s->aflag, &s->ascan, &s->a_node, &s->a_first, &s->a_count};
     for (auto *b : i1) e |= b->ensure(n);
     for (int k = 0; k < 4; ++k) e |= s->lcnt[k].ensure(n + 1) | s->loff[k].ensure(n + 1);
-    e |= s->tcnt.ensure(n + 1) | s->toff.ensure(n + 1) | s->roots.ensure(n);
-    s->task_cap = n / 16 + 4096;
-    e |= s->tasks.ensure(s->task_cap) | s->tlcnt.ensure(s->task_cap + 1) | s->tloff.ensure(s->task_cap + 1);
-    s->lchain_max = 64;
-    s->lpool_chunks = std::min((long long)n * 24 / sphtree::LIST_CHUNK + s->task_cap + 1024, MAX_POOL_CHUNKS);
-    e |= s->lpool.ensure((size_t)s->lpool_chunks * sphtree::LIST_CHUNK) |
-         s->lchain.ensure((size_t)s->task_cap * s->lchain_max);
-    e |= s->items.ensure(n);
+    e |= s->roots.ensure(n);
     e |= s->scal.ensure(S_NI) | s->dscal.ensure(D_NI) | s->lscal.ensure(L_NI);
+    for (int k = 0; k < 2; ++k) {
+        ListScratch &L = s->ls[k];
+        e |= L.tcnt.ensure(n + 1) | L.toff.ensure(n + 1);
+        L.task_cap = n / 16 + 4096;
+        e |= L.tasks.ensure(L.task_cap) | L.tlcnt.ensure(L.task_cap + 1) | L.tloff.ensure(L.task_cap + 1);
+        L.lchain_max = 64;
+        L.lpool_chunks = std::min((long long)n * 24 / sphtree::LIST_CHUNK + L.task_cap + 1024, MAX_POOL_CHUNKS);
+        e |= L.lpool.ensure((size_t)L.lpool_chunks * sphtree::LIST_CHUNK) |
+             L.lchain.ensure((size_t)L.task_cap * L.lchain_max);
+        e |= L.items.ensure(n);
+        if (k == 1) e |= L.own_sc.ensure(S_NI);
+        L.sc = k == 0 ? s->scal.p : L.own_sc.p;
+    }
     e |= s->partial.ensure(RED_BLOCKS * MAX_RED + MAX_RED) | s->box.ensure(8);
     e |= s->h_scal.ensure(S_NI) | s->h_dscal.ensure(D_NI) | s->h_lscal.ensure(L_NI);
     e |= s->h_guess.ensure(n);
@@ -1047,9 +1073,10 @@ int alloc_all(sph_system *s) {
     cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
     cub::DoubleBuffer<int> vb(s->perm[0].p, s->perm[1].p);
     cub::DeviceRadixSort::SortPairs(nullptr, b1, kb, vb, s->n, 0, 63);
-    cub::DeviceScan::ExclusiveSum(nullptr, b2, s->gflag.p, s->gscan.p, std::max(s->n, s->task_cap) + 1);
-    s->cub_bytes = std::max(b1, b2);
-    e |= s->cub_tmp.ensure(s->cub_bytes);
+    cub::DeviceScan::ExclusiveSum(nullptr, b2, s->gflag.p, s->gscan.p, std::max(s->n, s->ls[0].task_cap) + 1);
+    s->ls[0].cub_bytes = std::max(b1, b2);
+    s->ls[1].cub_bytes = b2;
+    for (int k = 0; k < 2; ++k) e |= s->ls[k].cub.ensure(s->ls[k].cub_bytes);
     // the first density walk covers every group, in group order
     s->walk_first[0] = s->group_first.p; s->walk_count[0] = s->group_count.p; s->walk_num[0] = s->scal.p + S_NGROUPS;
     s->walk_first[3] = s->a_first.p; s->walk_count[3] = s->a_count.p; s->walk_num[3] = s->scal.p + S_NACTIVE;
@@ -1064,9 +1091,10 @@ int alloc_all(sph_system *s) {
         if (e__ != cudaSuccess) return sphrt::cuda_error(s->ctx, e__, #x); \
     } while (0)
 
-int exclusive_scan(sph_system *s, const int *in, int *out, int count = -1) {
-    size_t bytes = s->cub_bytes;
-    CUDA_TRY(cub::DeviceScan::ExclusiveSum(s->cub_tmp.p, bytes, in, out, count < 0 ? s->n : count, s->st()));
+int exclusive_scan(sph_system *s, const int *in, int *out, int count = -1, int builder = 0) {
+    ListScratch &L = s->ls[builder];
+    size_t bytes = L.cub_bytes;
+    CUDA_TRY(cub::DeviceScan::ExclusiveSum(L.cub.p, bytes, in, out, count < 0 ? s->n : count, s->st()));
     return SPH_OK;
 }
 
@@ -1107,8 +1135,8 @@ int build_tree(sph_system *s) {
     sphtree::morton_keys<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, n, s->box.p, s->keys[0].p, s->perm[0].p);
     cub::DoubleBuffer<uint64_t> kb(s->keys[0].p, s->keys[1].p);
     cub::DoubleBuffer<int> vb(s->perm[0].p, s->perm[1].p);
-    size_t bytes = s->cub_bytes;
-    CUDA_TRY(cub::DeviceRadixSort::SortPairs(s->cub_tmp.p, bytes, kb, vb, n, 0, 63, st));
+    size_t bytes = s->ls[0].cub_bytes;
+    CUDA_TRY(cub::DeviceRadixSort::SortPairs(s->ls[0].cub.p, bytes, kb, vb, n, 0, 63, st));
     const uint64_t *keys = kb.Current();
     const int *idx = vb.Current();
     permute<<<grid_for(n), 256, 0, st>>>(n, idx, s->persist(0), s->persist(1));
@@ -1146,16 +1174,16 @@ int build_tree(sph_system *s) {
 
 // Grows the task buffers (eager evaluations only) and the CUB scratch that
 // scans them.
-int grow_tasks(sph_system *s, int cap) {
-    int e = s->tasks.ensure(cap) | s->tlcnt.ensure((size_t)cap + 1) | s->tloff.ensure((size_t)cap + 1) |
-            s->lchain.ensure((size_t)cap * s->lchain_max);
+int grow_tasks(sph_system *s, ListScratch &L, int cap) {
+    int e = L.tasks.ensure(cap) | L.tlcnt.ensure((size_t)cap + 1) | L.tloff.ensure((size_t)cap + 1) |
+            L.lchain.ensure((size_t)cap * L.lchain_max);
     if (e) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "task allocation of %d entries failed", cap);
-    s->task_cap = cap;
+    L.task_cap = cap;
     size_t b = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, b, s->tlcnt.p, s->tloff.p, cap + 1);
-    if (b > s->cub_bytes) {
-        if (s->cub_tmp.ensure(b)) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "CUB scratch allocation failed");
-        s->cub_bytes = b;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, L.tlcnt.p, L.tloff.p, cap + 1);
+    if (b > L.cub_bytes) {
+        if (L.cub.ensure(b)) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "CUB scratch allocation failed");
+        L.cub_bytes = b;
     }
     s->graph_valid = false;
     s->force_graph_valid = false;
@@ -1200,6 +1228,9 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
                           int chunk = 32) {
     const int n = s->n;
     cudaStream_t st = s->st();
+    const int builder = kind == 2 ? 1 : 0;
+    ListScratch &L = s->ls[builder];
+    int *sc = L.sc;
     sphtree::ListArgs a{};
     a.t = s->nodes();
     a.n = n;
@@ -1210,78 +1241,78 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.r_group = walk_r;
     a.n_leaf = s->prm.n_leaf;
     a.inv_theta2 = (float)(1.0 / (s->prm.theta * s->prm.theta));
-    a.error = s->scal.p + S_ERROR;
+    a.error = sc + S_ERROR;
     const int tgrid = s->ctx->sm_count * 8;
     const int mode = (kind == 0 || kind == 3) ? sphtree::GATHER : (kind == 1 ? sphtree::SYMMETRIC : sphtree::GRAVITY);
     // 1. traversal tasks per group (count, scan, grow in eager mode, write)
-    CUDA_TRY(cudaMemsetAsync(s->tcnt.p, 0, sizeof(int) * (size_t)(n + 1), st));
-    launch_tasks(mode, false, tgrid, a, s->tcnt.p, s->toff.p, s->tasks.p, s->task_cap, st);
-    int r = exclusive_scan(s, s->tcnt.p, s->toff.p, n + 1);
+    CUDA_TRY(cudaMemsetAsync(L.tcnt.p, 0, sizeof(int) * (size_t)(n + 1), st));
+    launch_tasks(mode, false, tgrid, a, L.tcnt.p, L.toff.p, L.tasks.p, L.task_cap, st);
+    int r = exclusive_scan(s, L.tcnt.p, L.toff.p, n + 1, builder);
     if (r) return r;
     if (eager) {
         int nt = 0;
-        CUDA_TRY(cudaMemcpyAsync(&nt, s->toff.p + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&nt, L.toff.p + n, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
-        if (nt + nt / 4 > s->task_cap) {
-            r = grow_tasks(s, nt + nt / 2 + 1024);
+        if (nt + nt / 4 > L.task_cap) {
+            r = grow_tasks(s, L, nt + nt / 2 + 1024);
             if (r) return r;
         }
     }
-    task_total<<<1, 1, 0, st>>>(n, s->toff.p, s->task_cap, s->scal.p);
-    launch_tasks(mode, true, tgrid, a, s->tcnt.p, s->toff.p, s->tasks.p, s->task_cap, st);
+    task_total<<<1, 1, 0, st>>>(n, L.toff.p, L.task_cap, sc);
+    launch_tasks(mode, true, tgrid, a, L.tcnt.p, L.toff.p, L.tasks.p, L.task_cap, st);
     // 2. list lengths per task, offsets per task and per group
-    a.tasks = s->tasks.p;
-    a.n_tasks = s->scal.p + S_NTASKS;
-    a.count_out = s->tlcnt.p;
-    a.offset = s->tloff.p;
-    a.pool_next = s->scal.p + S_POOL;
-    a.pool_error = s->scal.p + S_POOLERR;
+    a.tasks = L.tasks.p;
+    a.n_tasks = sc + S_NTASKS;
+    a.count_out = L.tlcnt.p;
+    a.offset = L.tloff.p;
+    a.pool_next = sc + S_POOL;
+    a.pool_error = sc + S_POOLERR;
     // one traversal: counts per task and the entries into pool chunks; in
     // eager mode the pool and the chains grow until they hold the lists with
     // a quarter of headroom (graph replays cannot allocate)
     for (;;) {
-        a.pool = s->lpool.p;
-        a.pool_chunks = s->lpool_chunks;
-        a.chain = s->lchain.p;
-        a.chain_max = s->lchain_max;
-        CUDA_TRY(cudaMemsetAsync(s->tlcnt.p, 0, sizeof(int) * (size_t)(s->task_cap + 1), st));
-        CUDA_TRY(cudaMemsetAsync(s->scal.p + S_POOL, 0, 2 * sizeof(int), st));
+        a.pool = L.lpool.p;
+        a.pool_chunks = L.lpool_chunks;
+        a.chain = L.lchain.p;
+        a.chain_max = L.lchain_max;
+        CUDA_TRY(cudaMemsetAsync(L.tlcnt.p, 0, sizeof(int) * (size_t)(L.task_cap + 1), st));
+        CUDA_TRY(cudaMemsetAsync(sc + S_POOL, 0, 2 * sizeof(int), st));
         launch_lists(mode, tgrid, a, st);
-        pool_usage<<<1, 1, 0, st>>>(s->scal.p);
+        pool_usage<<<1, 1, 0, st>>>(sc);
         if (!eager) break;
         int pu[2];
-        CUDA_TRY(cudaMemcpyAsync(pu, s->scal.p + S_POOL, sizeof(pu), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(pu, sc + S_POOL, sizeof(pu), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         const long long used = pu[0];
         const bool redo = pu[1] != 0;
-        if (!redo && used + used / 4 <= s->lpool_chunks) break;
+        if (!redo && used + used / 4 <= L.lpool_chunks) break;
         if (redo && used > MAX_POOL_CHUNKS)
             return sphrt::set_error(s->ctx, SPH_ERR_CAPACITY,
                                     "the interaction lists need %lld chunks of %d entries, more than 32-bit list "
                                     "offsets address (smoothing lengths far beyond the particle spacing?)",
                                     used, sphtree::LIST_CHUNK);
-        if (used + used / 4 > s->lpool_chunks && s->lpool_chunks < MAX_POOL_CHUNKS) {
+        if (used + used / 4 > L.lpool_chunks && L.lpool_chunks < MAX_POOL_CHUNKS) {
             const long long want = std::min(used + used / 2 + 1024, MAX_POOL_CHUNKS);
-            if (s->lpool.ensure((size_t)want * sphtree::LIST_CHUNK))
+            if (L.lpool.ensure((size_t)want * sphtree::LIST_CHUNK))
                 return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list pool allocation of %lld chunks failed", want);
-            s->lpool_chunks = std::min((long long)(s->lpool.cap / sphtree::LIST_CHUNK), MAX_POOL_CHUNKS);
+            L.lpool_chunks = std::min((long long)(L.lpool.cap / sphtree::LIST_CHUNK), MAX_POOL_CHUNKS);
         }
         if (pu[1] & 2) {
-            s->lchain_max *= 2;
-            if (s->lchain.ensure((size_t)s->task_cap * s->lchain_max))
+            L.lchain_max *= 2;
+            if (L.lchain.ensure((size_t)L.task_cap * L.lchain_max))
                 return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list chain allocation failed");
         }
         s->graph_valid = false;
         s->force_graph_valid = false;
         if (!redo) break;   // grown for headroom only: this traversal is complete
     }
-    r = exclusive_scan(s, s->tlcnt.p, s->tloff.p, s->task_cap + 1);
+    r = exclusive_scan(s, L.tlcnt.p, L.tloff.p, L.task_cap + 1, builder);
     if (r) return r;
-    sphtree::group_lists<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], s->toff.p, s->tloff.p,
-                                                         s->task_cap, s->loff[kind].p, s->lcnt[kind].p);
+    sphtree::group_lists<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], L.toff.p, L.tloff.p,
+                                                         L.task_cap, s->loff[kind].p, s->lcnt[kind].p);
     const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : (kind == 2 ? L_LIST_G : L_LIST_R));
     if (eager) {
-        list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, (long long)1 << 62, s->scal.p, s->lscal.p, lslot);
+        list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, (long long)1 << 62, sc, s->lscal.p, lslot);
         long long tot = 0;
         CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
@@ -1296,7 +1327,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
             s->force_graph_valid = false;
         }
     }
-    list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, s->lcap[kind], s->scal.p, s->lscal.p, lslot);
+    list_total<<<1, 1, 0, st>>>(n, s->lcnt[kind].p, s->loff[kind].p, s->lcap[kind], sc, s->lscal.p, lslot);
     // 3. the chunks to their list offsets
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
@@ -1307,7 +1338,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // density and hydro walks with long lists are split (their pair loops
     // drop most of the list); gravity lists are uniform and kept whole
     const int split_nj = (kind == 2) ? (1 << 30) : (s->prm.item_split_nj > 0 ? s->prm.item_split_nj : ITEM_SPLIT_NJ);
-    int *bkt = s->scal.p + S_BKT;
+    int *bkt = sc + S_BKT;
     CUDA_TRY(cudaMemsetAsync(bkt, 0, sizeof(int) * (2 * NBKT + 2), st));
     item_buckets<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj, bkt);
     bucket_offsets<<<1, 32, 0, st>>>(bkt, kind == 2 ? 0 : (s->prm.heavy_classes >= 0 ? s->prm.heavy_classes
@@ -1315,12 +1346,12 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // light items in walk order: per-walk counts (the task arrays are free
     // again once the lists are built) and their scan
     light_counts<<<grid_for(n + 1), 256, 0, st>>>(n, s->walk_num[kind], icount, s->lcnt[kind].p, chunk, split_nj,
-                                                  bkt, s->tcnt.p);
-    r = exclusive_scan(s, s->tcnt.p, s->toff.p, n + 1);
+                                                  bkt, L.tcnt.p);
+    r = exclusive_scan(s, L.tcnt.p, L.toff.p, n + 1, builder);
     if (r) return r;
     fill_items<<<grid_for(n), 256, 0, st>>>(n, s->walk_num[kind], ifirst, icount, chunk, split_nj, s->lcnt[kind].p,
-                                            bkt, s->toff.p, s->items.p, s->scal.p + S_NITEMS, pairs);
-    drop_items_on_overflow<<<1, 1, 0, st>>>(s->scal.p);
+                                            bkt, L.toff.p, L.items.p, sc + S_NITEMS, pairs);
+    drop_items_on_overflow<<<1, 1, 0, st>>>(sc);
     return SPH_OK;
 }
 
@@ -1371,7 +1402,7 @@ int density_walk(sph_system *s, int it, bool eager, cudaGraphConditionalHandle c
     a.i_pm = s->pos[0].p; a.i_vel = s->vel[0].p; a.i_id = s->id[0].p; a.i_ksr = s->ksr[0].p;
     a.i_rs = s->rs.p;
     a.j_pm = s->pos[0].p; a.j_vel = s->vel[0].p; a.j_id = s->id[0].p;
-    a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+    a.items = s->ls[0].items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
     a.j_off = s->loff[kind].p; a.j_idx = s->jidx[kind].p; a.queue = s->scal.p + S_QUEUE;
     a.i_list = s->ulist.p;
     a.fi = sphk::F32Part{s->f_phi.p, s->f_plo.p, s->f_vhi.p, s->f_vlo.p};
@@ -1511,13 +1542,47 @@ int density_phase(sph_system *s, bool eager) {
     return SPH_OK;
 }
 
-int gravity_phase(sph_system *s, bool eager) {
+// Error bits of list builder 1 into the system's.
+__global__ void merge_errors(const int *from, int *scal) {
+    if (from[S_ERROR]) atomicOr(&scal[S_ERROR], from[S_ERROR]);
+}
+
+// The gravity lists and work items (list builder 1).  They depend only on the
+// tree (node boxes and centres of mass, which the refit after the density
+// phase rewrites with the same values), so in a captured graph they are
+// built on side_stream, forked after the tree build and joined before the
+// gravity kernel, while the density phase runs on the main stream; eager
+// evaluations build them in order on the main stream.
+int gravity_lists(sph_system *s, bool eager) {
+    const cudaStream_t prev = s->st_override;
+    s->glist_forked = !eager && s->capturing >= 0 && s->side_stream != nullptr;
+    if (s->glist_forked) {
+        CUDA_TRY(cudaEventRecord(s->ev_fork, s->st()));
+        CUDA_TRY(cudaStreamWaitEvent(s->side_stream, s->ev_fork, 0));
+        s->st_override = s->side_stream;
+    }
+    const cudaStream_t st = s->st();
+    cudaEventRecord(s->ev[EV_GLIST_B], st);
+    int r = SPH_OK;
+    const cudaError_t em = cudaMemsetAsync(s->ls[1].sc, 0, sizeof(int) * S_NI, st);
+    if (em != cudaSuccess) r = sphrt::cuda_error(s->ctx, em, "cudaMemsetAsync");
+    if (!r) r = build_lists_and_items(s, 2, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_G);
+    cudaEventRecord(s->ev[EV_GLIST_E], st);
+    if (s->glist_forked) {
+        const cudaError_t ej = cudaEventRecord(s->ev_join, s->side_stream);
+        s->st_override = prev;
+        if (!r && ej != cudaSuccess) r = sphrt::cuda_error(s->ctx, ej, "cudaEventRecord");
+    }
+    return r;
+}
+
+int gravity_phase(sph_system *s) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
-    cudaEventRecord(s->ev[EV_GLIST_B], st);
-    int r = build_lists_and_items(s, 2, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_G);
-    if (r) return r;
+    if (s->glist_forked) CUDA_TRY(cudaStreamWaitEvent(st, s->ev_join, 0));
+    s->glist_forked = false;
+    merge_errors<<<1, 1, 0, st>>>(s->ls[1].sc, s->scal.p);
     if (ctx->prm.precision == SPH_PREC_FP32C) {
         sphk::make_gravity_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->eps2.p, s->f_phi.p, s->f_plo.p);
         sphk::make_gravity_records<<<grid_for(2LL * n - 1), 256, 0, st>>>(2 * n - 1, s->mom.p, s->neps2.p,
@@ -1533,7 +1598,7 @@ int gravity_phase(sph_system *s, bool eager) {
     a.f_shi = s->f_shi.p; a.f_slo = s->f_slo.p;
     a.i_list = nullptr;
     a.n_split = n;
-    a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+    a.items = s->ls[1].items.p; a.n_items = 0; a.n_items_dev = s->ls[1].sc + S_NITEMS;
     a.j_off = s->loff[2].p; a.j_idx = s->jidx[2].p; a.queue = s->scal.p + S_QUEUE;
     a.o_acc = s->r_acc.p; a.o_pot = s->r_pot.p; a.o_eta = s->r_eta.p;
     const bool q64 = s->prm.quadrupole && ctx->prm.precision == SPH_PREC_FP64;
@@ -1586,7 +1651,7 @@ int hydro_phase(sph_system *s, bool eager) {
     a.fi_g1 = s->f_g1.p; a.fi_g2 = s->f_g2.p; a.fi_g3 = s->f_g3.p;
     a.fj_g1 = s->f_g1.p; a.fj_g2 = s->f_g2.p; a.fj_g3 = s->f_g3.p;
     a.i_list = nullptr;
-    a.items = s->items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
+    a.items = s->ls[0].items.p; a.n_items = 0; a.n_items_dev = s->scal.p + S_NITEMS;
     a.j_off = s->loff[1].p; a.j_idx = s->jidx[1].p; a.queue = s->scal.p + S_QUEUE;
     a.o_acch = s->r_acch.p; a.o_accg = s->r_accg.p; a.o_udot = s->r_udot.p; a.o_vsmx = s->r_vsmx.p;
     a.o_diffu = s->r_diffu.p;
@@ -1610,6 +1675,8 @@ int force_body(sph_system *s, bool eager, bool energy = true) {
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_POOLMAX, 0, sizeof(int), st));
     int r = build_tree(s);
     if (r) return r;
+    r = gravity_lists(s, eager);
+    if (r) return r;
     r = density_phase(s, eager);
     if (r) return r;
     post_density<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->dens.p, s->uene[0].p, s->divv.p, s->rotv.p,
@@ -1617,7 +1684,7 @@ int force_body(sph_system *s, bool eager, bool energy = true) {
                                               s->ctx->prm.precision == SPH_PREC_FP32C);
     r = refit_tree(s);   // h (max h, softening) changed in the density phase
     if (r) return r;
-    r = gravity_phase(s, eager);
+    r = gravity_phase(s);
     if (r) return r;
     r = hydro_phase(s, eager);
     if (r) return r;
@@ -1701,12 +1768,14 @@ int check_headroom(sph_system *s) {
             s->graph_valid = false;
             s->force_graph_valid = false;
         }
-    int pm = 0;
-    CUDA_TRY(cudaMemcpyAsync(&pm, s->scal.p + S_POOLMAX, sizeof(int), cudaMemcpyDeviceToHost, s->st()));
-    CUDA_TRY(cudaStreamSynchronize(s->st()));
-    if ((long long)pm * 5 > s->lpool_chunks * 4) {
-        s->graph_valid = false;
-        s->force_graph_valid = false;
+    for (int k = 0; k < 2; ++k) {
+        int pm = 0;
+        CUDA_TRY(cudaMemcpyAsync(&pm, s->ls[k].sc + S_POOLMAX, sizeof(int), cudaMemcpyDeviceToHost, s->st()));
+        CUDA_TRY(cudaStreamSynchronize(s->st()));
+        if ((long long)pm * 5 > s->ls[k].lpool_chunks * 4) {
+            s->graph_valid = false;
+            s->force_graph_valid = false;
+        }
     }
     return SPH_OK;
 }
@@ -1760,6 +1829,9 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
     }
     for (int k = 0; k < EV_N; ++k) cudaEventCreate(&s->ev[k]);
     cudaStreamCreateWithFlags(&s->body_stream, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
     cudaMemset(s->scal.p, 0, sizeof(int) * S_NI);
     cudaMemset(s->dscal.p, 0, sizeof(double) * D_NI);
     cudaMemset(s->lscal.p, 0, sizeof(long long) * L_NI);
@@ -1776,6 +1848,9 @@ extern "C" int sph_system_destroy(sph_system *s) {
     for (int k = 0; k < EV_N; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->body_stream) cudaStreamDestroy(s->body_stream);
+    if (s->side_stream) cudaStreamDestroy(s->side_stream);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->vel[k].release(); s->vel2[k].release(); s->id[k].release();
         s->istar[k].release(); s->orig[k].release(); s->uene[k].release(); s->uene2[k].release();
@@ -1805,12 +1880,12 @@ extern "C" int sph_system_destroy(sph_system *s) {
     for (int k = 0; k < 4; ++k) {
         s->lcnt[k].release(); s->loff[k].release(); s->jidx[k].release();
         if (k == 0) {
-            s->tcnt.release(); s->toff.release(); s->tlcnt.release(); s->tloff.release(); s->tasks.release();
-            s->lpool.release(); s->lchain.release();
+            s->ls[0].release();
+            s->ls[1].release();
             s->roots.release();
         }
     }
-    s->items.release(); s->lscal.release(); s->cub_tmp.release(); s->an_buf.release();
+    s->lscal.release(); s->an_buf.release();
     s->h_scal.release(); s->h_dscal.release(); s->h_lscal.release();
     s->h_guess.release(); s->adj_acc.release(); s->adj_seed.release(); s->adj_items.release();
     s->adj_cnt.release(); s->adj_off.release();
@@ -2269,7 +2344,7 @@ extern "C" int sph_system_phase_times(sph_system *s, float *ms, int32_t n) {
     const cudaError_t se = cudaEventSynchronize(s->ev[EV_END]);
     if (se != cudaSuccess) return -sphrt::cuda_error(s->ctx, se, "cudaEventSynchronize");
     const int pairs[8][2] = {{EV_TREE_B, EV_TREE_E}, {EV_DENS_B, EV_DENS_E}, {EV_DENSK_B, EV_DENSK_E},
-                             {EV_GLIST_B, EV_GK_B},  {EV_GK_B, EV_GK_E},     {EV_HLIST_B, EV_HK_B},
+                             {EV_GLIST_B, EV_GLIST_E}, {EV_GK_B, EV_GK_E},   {EV_HLIST_B, EV_HK_B},
                              {EV_HK_B, EV_HK_E},     {EV_TREE_B, EV_END}};
     int k = 0;
     for (; k < n && k < 8; ++k) {
@@ -2362,14 +2437,14 @@ extern "C" int sph_system_radii_sorted(sph_system *s, int32_t star, const double
                                             r0, m0);
     size_t bytes = 0;
     CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, bytes, r0, r1, m0, m1, n, 0, 64, st));
-    if (bytes > s->cub_bytes) {
-        if (s->cub_tmp.ensure(bytes)) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "CUB scratch allocation failed");
-        s->cub_bytes = bytes;
+    if (bytes > s->ls[0].cub_bytes) {
+        if (s->ls[0].cub.ensure(bytes)) return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "CUB scratch allocation failed");
+        s->ls[0].cub_bytes = bytes;
         s->graph_valid = false;
         s->force_graph_valid = false;
     }
-    bytes = s->cub_bytes;
-    CUDA_TRY(cub::DeviceRadixSort::SortPairs(s->cub_tmp.p, bytes, r0, r1, m0, m1, n, 0, 64, st));
+    bytes = s->ls[0].cub_bytes;
+    CUDA_TRY(cub::DeviceRadixSort::SortPairs(s->ls[0].cub.p, bytes, r0, r1, m0, m1, n, 0, 64, st));
     std::vector<double> rh(n);
     CUDA_TRY(cudaMemcpyAsync(rh.data(), r1, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
