@@ -1114,14 +1114,16 @@ int refit_tree(sph_system *s) {
     CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
     if (s->prm.quadrupole) {
         sphtree::refit_bottom<true><<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
-            s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
-        sphtree::refit_top<true><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+            s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS, s->box.p);
+        sphtree::refit_top<true><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS,
+                                                                      s->box.p);
     } else {
         sphtree::refit_bottom<false><<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
-            s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
-        sphtree::refit_top<false><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+            s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS, s->box.p);
+        sphtree::refit_top<false><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS,
+                                                                       s->box.p);
     }
-    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t);
+    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t, s->box.p, s->prm.quadrupole != 0);
     return SPH_OK;
 }
 

@@ -177,29 +177,6 @@ __device__ __forceinline__ void store_node(const Nodes &t, int node, const NodeD
     t.eps2[node] = d.se;
 }
 
-// Centre of mass, mass-weighted eps^2 and the FP32 copy of the internal
-// nodes from their sums (leaves hold the particle's own values).
-__global__ void normalise_nodes(int n, Nodes t) {
-    for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < n - 1; node += gridDim.x * blockDim.x) {
-        const dbl4 s = t.mom[node];
-        dbl4 m;
-        double e2;
-        if (s.w > 0.0) {
-            const double mi = 1.0 / s.w;
-            m = make_dbl4(s.x * mi, s.y * mi, s.z * mi, s.w);
-            e2 = t.eps2[node] * mi;
-        } else {
-            const float4 lo = t.flo[node], hi = t.fhi[node];
-            m = make_dbl4(0.5 * ((double)lo.x + hi.x), 0.5 * ((double)lo.y + hi.y), 0.5 * ((double)lo.z + hi.z),
-                          0.0);
-            e2 = 0.0;
-        }
-        t.mom[node] = m;
-        t.eps2[node] = e2;
-        t.fmom[node] = make_float4((float)m.x, (float)m.y, (float)m.z, (float)m.w);
-    }
-}
-
 // A node written by another SM, back as refit data (L1 bypassed): leaves
 // hold (x, m) and eps^2, internal nodes the sums of the climb.
 __device__ __forceinline__ NodeData load_node_cg(const Nodes &t, int node, int n) {
@@ -218,58 +195,98 @@ __device__ __forceinline__ NodeData load_node_cg(const Nodes &t, int node, int n
     return d;
 }
 
-// Traceless quadrupole of a parent from its children's, about the parent's
-// centre of mass c: Q = Q_a + Q_b + sum_k m_k (3 d_k d_k^T - |d_k|^2 I),
-// d_k = c_k - c (parallel-axis rule; linear in the moments, so the traceless
-// form combines directly).
+// Quadrupole runs accumulate second moments about the step's bounding-box
+// centre o during the climb, S = sum m (x - o)(x - o)^T (plain sums, no
+// division), in t.quad; normalise_nodes turns them into the traceless
+// quadrupole about the node's centre of mass c, Q = 3 C - tr(C) I with
+// C = S - m d d^T, d = c - o (FP64: the cancellation of S against m d d^T
+// costs ~1e-9 relative at the box sizes and node sizes of a collision).
+// Leaves end with Q = 0.
 struct Quad {
     double q[6];   // xx, yy, zz, xy, xz, yz
 };
 
-__device__ __forceinline__ void add_shifted(Quad &r, const Quad &a, double m, double dx, double dy, double dz) {
-    const double d2 = dx * dx + dy * dy + dz * dz;
-    r.q[0] += a.q[0] + m * (3.0 * dx * dx - d2);
-    r.q[1] += a.q[1] + m * (3.0 * dy * dy - d2);
-    r.q[2] += a.q[2] + m * (3.0 * dz * dz - d2);
-    r.q[3] += a.q[3] + m * 3.0 * dx * dy;
-    r.q[4] += a.q[4] + m * 3.0 * dx * dz;
-    r.q[5] += a.q[5] + m * 3.0 * dy * dz;
+__device__ __forceinline__ double3 box_centre(const double *box) {
+    return make_double3(0.5 * (box[0] + box[3]), 0.5 * (box[1] + box[4]), 0.5 * (box[2] + box[5]));
 }
 
-__device__ __forceinline__ Quad combine_quad(const NodeData &a, const Quad &qa, const NodeData &b, const Quad &qb) {
+__device__ __forceinline__ Quad leaf_moments(const dbl4 &x, const double3 &o) {
+    const double dx = x.x - o.x, dy = x.y - o.y, dz = x.z - o.z, m = x.w;
+    Quad q;
+    q.q[0] = m * dx * dx; q.q[1] = m * dy * dy; q.q[2] = m * dz * dz;
+    q.q[3] = m * dx * dy; q.q[4] = m * dx * dz; q.q[5] = m * dy * dz;
+    return q;
+}
+
+__device__ __forceinline__ Quad add_moments(const Quad &a, const Quad &b) {
     Quad r;
-    for (int k = 0; k < 6; ++k) r.q[k] = 0.0;
-    const double m = a.sm.w + b.sm.w;
-    if (!(m > 0.0)) {
-        for (int k = 0; k < 6; ++k) r.q[k] = qa.q[k] + qb.q[k];
-        return r;
-    }
-    const double mi = 1.0 / m;
-    const double cx = (a.sm.x + b.sm.x) * mi, cy = (a.sm.y + b.sm.y) * mi, cz = (a.sm.z + b.sm.z) * mi;
-    const NodeData *c[2] = {&a, &b};
-    const Quad *q[2] = {&qa, &qb};
-    for (int k = 0; k < 2; ++k) {
-        const double mk = c[k]->sm.w;
-        if (mk > 0.0) {
-            const double ik = 1.0 / mk;
-            add_shifted(r, *q[k], mk, c[k]->sm.x * ik - cx, c[k]->sm.y * ik - cy, c[k]->sm.z * ik - cz);
-        } else {
-            for (int j = 0; j < 6; ++j) r.q[j] += q[k]->q[j];
-        }
-    }
+    for (int k = 0; k < 6; ++k) r.q[k] = a.q[k] + b.q[k];
     return r;
 }
 
-__device__ __forceinline__ void store_quad(const Nodes &t, int node, const Quad &q) {
+__device__ __forceinline__ void store_moments(const Nodes &t, int node, const Quad &q) {
     for (int k = 0; k < 6; ++k) t.quad[6 * (size_t)node + k] = q.q[k];
+}
+
+__device__ __forceinline__ void store_quad(const Nodes &t, int node, const Quad &q) {
+    store_moments(t, node, q);
     t.fq0[node] = make_float4((float)q.q[0], (float)q.q[1], (float)q.q[2], (float)q.q[3]);
     t.fq1[node] = make_float4((float)q.q[4], (float)q.q[5], 0.0f, 0.0f);
 }
 
-__device__ __forceinline__ Quad load_quad_cg(const Nodes &t, int node) {
+// Second moments of a node written by another SM: a leaf's from its particle
+// (the leaf itself stores Q = 0), an internal node's from the climb.
+__device__ __forceinline__ Quad load_moments_cg(const Nodes &t, int node, int n, const double3 &o) {
+    if (node >= n - 1) {
+        const double2 *p = reinterpret_cast<const double2 *>(&t.mom[node]);
+        const double2 a = __ldcg(p), b = __ldcg(p + 1);
+        return leaf_moments(make_dbl4(a.x, a.y, b.x, b.y), o);
+    }
     Quad q;
     for (int k = 0; k < 6; ++k) q.q[k] = __ldcg(&t.quad[6 * (size_t)node + k]);
     return q;
+}
+
+// Centre of mass, mass-weighted eps^2, the quadrupole (quadrupole runs) and
+// the FP32 copy of the internal nodes from their sums (leaves hold the
+// particle's own values).
+__global__ void normalise_nodes(int n, Nodes t, const double *box, bool quad) {
+    const double3 o = quad ? box_centre(box) : make_double3(0.0, 0.0, 0.0);
+    for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < n - 1; node += gridDim.x * blockDim.x) {
+        const dbl4 s = t.mom[node];
+        dbl4 m;
+        double e2;
+        if (s.w > 0.0) {
+            const double mi = 1.0 / s.w;
+            m = make_dbl4(s.x * mi, s.y * mi, s.z * mi, s.w);
+            e2 = t.eps2[node] * mi;
+        } else {
+            const float4 lo = t.flo[node], hi = t.fhi[node];
+            m = make_dbl4(0.5 * ((double)lo.x + hi.x), 0.5 * ((double)lo.y + hi.y), 0.5 * ((double)lo.z + hi.z),
+                          0.0);
+            e2 = 0.0;
+        }
+        t.mom[node] = m;
+        t.eps2[node] = e2;
+        t.fmom[node] = make_float4((float)m.x, (float)m.y, (float)m.z, (float)m.w);
+        if (quad) {
+            Quad q;
+            for (int k = 0; k < 6; ++k) q.q[k] = 0.0;
+            if (s.w > 0.0) {
+                const double dx = m.x - o.x, dy = m.y - o.y, dz = m.z - o.z;
+                const double *S = t.quad + 6 * (size_t)node;
+                const double cxx = S[0] - s.w * dx * dx, cyy = S[1] - s.w * dy * dy, czz = S[2] - s.w * dz * dz;
+                const double tr = cxx + cyy + czz;
+                q.q[0] = 3.0 * cxx - tr;
+                q.q[1] = 3.0 * cyy - tr;
+                q.q[2] = 3.0 * czz - tr;
+                q.q[3] = 3.0 * (S[3] - s.w * dx * dy);
+                q.q[4] = 3.0 * (S[4] - s.w * dx * dz);
+                q.q[5] = 3.0 * (S[5] - s.w * dy * dz);
+            }
+            store_quad(t, node, q);
+        }
+    }
 }
 
 // The refit runs in two parts.  Bottom: every maximal subtree of at most
@@ -291,12 +308,13 @@ __global__ void mark_subtrees(Nodes t, int n, int *roots, int *n_roots) {
 template <bool QUAD>
 __global__ void __launch_bounds__(REFIT_B)
 refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes t, const int *roots,
-             const int *n_roots) {
+             const int *n_roots, const double *box) {
     // slots 0..B-1: internal node (index - first), B..2B-1: leaf (particle - first)
     __shared__ NodeData sd[2 * REFIT_B];
     __shared__ Quad sq[QUAD ? 2 * REFIT_B : 1];
     __shared__ int visit[REFIT_B];
     const int nr = *n_roots;
+    const double3 o = QUAD ? box_centre(box) : make_double3(0.0, 0.0, 0.0);
     for (int r = blockIdx.x; r < nr; r += gridDim.x) {
         const int root = roots[r];
         const int a = t.first[root];
@@ -323,7 +341,7 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
             if (QUAD) {
                 Quad z;
                 for (int k = 0; k < 6; ++k) z.q[k] = 0.0;
-                sq[REFIT_B + threadIdx.x] = z;
+                sq[REFIT_B + threadIdx.x] = leaf_moments(x, o);
                 store_quad(t, node, z);
             }
             while (node != root) {
@@ -338,9 +356,9 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
                 const int sb = (ch.y >= n - 1) ? REFIT_B + (ch.y - (n - 1) - a) : ch.y - a;
                 if (sa < 0 || sa >= 2 * REFIT_B || sb < 0 || sb >= 2 * REFIT_B) break;
                 if (QUAD) {
-                    const Quad q = combine_quad(sd[sa], sq[sa], sd[sb], sq[sb]);
+                    const Quad q = add_moments(sq[sa], sq[sb]);
                     sq[node - a] = q;
-                    store_quad(t, node, q);
+                    store_moments(t, node, q);
                 }
                 d = combine(sd[sa], sd[sb]);
                 sd[node - a] = d;
@@ -353,8 +371,9 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
 
 // visit[] (internal nodes) is zero on entry.
 template <bool QUAD>
-__global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots) {
+__global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots, const double *box) {
     const int nr = *n_roots;
+    const double3 o = QUAD ? box_centre(box) : make_double3(0.0, 0.0, 0.0);
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
         int node = t.parent[roots[r]];
         while (node >= 0) {
@@ -366,7 +385,7 @@ __global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots) 
             if (arrived == 0) break;   // sibling not finished yet
             const int2 ch = t.child[node];
             const NodeData da = load_node_cg(t, ch.x, n), db = load_node_cg(t, ch.y, n);
-            if (QUAD) store_quad(t, node, combine_quad(da, load_quad_cg(t, ch.x), db, load_quad_cg(t, ch.y)));
+            if (QUAD) store_moments(t, node, add_moments(load_moments_cg(t, ch.x, n, o), load_moments_cg(t, ch.y, n, o)));
             store_node(t, node, combine(da, db));
             node = t.parent[node];
         }
