@@ -1295,13 +1295,12 @@ gravity_kernel(const GravityArgs a) {
         // like the monopole sums (halved once at the end)
         auto run_quad = [&](int n_q) {
             R qax = 0, qay = 0, qaz = 0, qpt = 0;
-            for (int k = sub; k < n_q; k += tpi) {
+            auto quad_term = [&](int k) {
                 const R4 P = q_p[wid][qhead + k];
                 const R4 A = q_a[wid][qhead + k];
                 const typename Real<F64>::T2 B = q_b[wid][qhead + k];
                 const R dx = xi - P.x, dy = yi - P.y, dz = zi - P.z;
-                const R r2 = dx * dx + dy * dy + dz * dz;
-                const R rr = rsqrt_r(r2 + P.w);
+                const R rr = rsqrt_r(dz * dz + (dy * dy + (dx * dx + P.w)));
                 const R rr2 = rr * rr;
                 const R rr5 = rr2 * rr2 * rr;
                 const R rr7 = rr5 * rr2;
@@ -1310,10 +1309,21 @@ gravity_kernel(const GravityArgs a) {
                 const R qz = B.x * dx + B.y * dy + A.z * dz;
                 const R rqr = dx * qx + dy * qy + dz * qz;
                 const R f = (R)5 * rqr * rr7;
-                qax += (R)2 * qx * rr5 - f * dx;
-                qay += (R)2 * qy * rr5 - f * dy;
-                qaz += (R)2 * qz * rr5 - f * dz;
+                const R g = (R)2 * rr5;
+                // two fused multiply-adds per component
+                qax += qx * g;
+                qax -= f * dx;
+                qay += qy * g;
+                qay -= f * dy;
+                qaz += qz * g;
+                qaz -= f * dz;
                 qpt -= rqr * rr5;
+            };
+            if (tpi == 1 && n_q == 32) {
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) quad_term(k);
+            } else {
+                for (int k = sub; k < n_q; k += tpi) quad_term(k);
             }
             ax.add(qax);
             ay.add(qay);
