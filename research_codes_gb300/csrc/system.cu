@@ -1106,13 +1106,14 @@ void reduce(sph_system *s, F f, double *out) {
 
 // Morton sort + permutation + radix tree + refit + groups.
 // Bottom-up refit of the node data (after the tree build, and again when h
-// changed).
-int refit_tree(sph_system *s) {
+// changed).  The quadrupoles depend only on positions and masses: the refit
+// after a change of h alone (quad = false) keeps those of the tree build.
+int refit_tree(sph_system *s, bool quad = true) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sphtree::Nodes t = s->nodes();
     CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
-    if (s->prm.quadrupole) {
+    if (s->prm.quadrupole && quad) {
         sphtree::refit_bottom<true><<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
             s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS, s->box.p);
         sphtree::refit_top<true><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS,
@@ -1123,7 +1124,7 @@ int refit_tree(sph_system *s) {
         sphtree::refit_top<false><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS,
                                                                        s->box.p);
     }
-    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t, s->box.p, s->prm.quadrupole != 0);
+    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t, s->box.p, s->prm.quadrupole != 0 && quad);
     return SPH_OK;
 }
 
@@ -1684,7 +1685,7 @@ int force_body(sph_system *s, bool eager, bool energy = true) {
     post_density<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->dens.p, s->uene[0].p, s->divv.p, s->rotv.p,
                                               s->ksr[0].p, s->pres.p, s->vsnd.p, s->bswt.p, s->eps2.p, s->pe.p,
                                               s->ctx->prm.precision == SPH_PREC_FP32C);
-    r = refit_tree(s);   // h (max h, softening) changed in the density phase
+    r = refit_tree(s, false);   // h (max h, softening) changed in the density phase
     if (r) return r;
     r = gravity_phase(s);
     if (r) return r;
