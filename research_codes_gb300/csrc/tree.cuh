@@ -71,9 +71,15 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v) {
 // box[0..2] = min, box[3..5] = max (filled by a reduction kernel).
 __global__ void morton_keys(const dbl4 *pos, int n, const double *box, uint64_t *keys, int *idx) {
     const double lx = box[0], ly = box[1], lz = box[2];
-    double span = fmax(fmax(box[3] - lx, box[4] - ly), box[5] - lz);
-    span = span > 0.0 ? span : 1.0;
-    const double s = 2097151.0 / span;
+    // the scale once per block (an FP64 division per thread would dominate)
+    __shared__ double s_scale;
+    if (threadIdx.x == 0) {
+        double span = fmax(fmax(box[3] - lx, box[4] - ly), box[5] - lz);
+        span = span > 0.0 ? span : 1.0;
+        s_scale = 2097151.0 / span;
+    }
+    __syncthreads();
+    const double s = s_scale;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const dbl4 x = pos[p];
         const uint64_t ix = (uint64_t)fmin(fmax((x.x - lx) * s, 0.0), 2097151.0);
