@@ -258,10 +258,24 @@ def run_ours(args):
     per_kernel["hydro"]["pair_evaluations"] = {"full": int(st_k["evals_hydro_near"]),
                                                "signal_velocity_only": int(st_k["evals_hydro_far"])}
     traffic = None
+    tree_lists = None
     if os.path.exists(PROFILE_TRAFFIC):
         tr = json.load(open(PROFILE_TRAFFIC))
         if dom in tr:
             traffic = tr[dom].get("bytes_per_launch")
+        if "tree_lists" in tr:
+            # HBM rate of the tree and list build (latency-bound traversals and
+            # scans): DRAM bytes over device time of those kernels, one ncu
+            # capture of a force evaluation of this workload
+            t = tr["tree_lists"]
+            hbm, src = 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+            peaks = os.path.join(ROOT, "MEASURED_PEAKS.json")
+            if os.path.exists(peaks) and json.load(open(peaks)).get("hbm_gbs"):
+                hbm, src = float(json.load(open(peaks))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy)"
+            gbs = t["dram_bytes"] / (t["ncu_ms"] * 1e-3) / 1e9
+            tree_lists = {"dram_bytes": t["dram_bytes"], "ncu_ms": t["ncu_ms"], "achieved_gbs": gbs,
+                          "peak_gbs": hbm, "frac": gbs / hbm, "peak_source": src,
+                          "groups": t.get("groups"), "source": t.get("_source")}
 
     line = {"metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
             "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps,
@@ -284,7 +298,7 @@ def run_ours(args):
                                  "pairs beyond the kernel support, per_kernel gives the evaluated work",
                          "frac_evaluated": per_kernel[dom]["achieved_evaluated_tflops"] / peak,
                          "per_kernel": per_kernel},
-            "gpu_launches": None, "clocks": clk, "autotune": tuned}
+            "tree_lists": tree_lists, "gpu_launches": None, "clocks": clk, "autotune": tuned}
 
     # kernel launches in the timed region: the kernel nodes of the captured
     # step graph (CUB sort/scan kernels compiled into the library included)
