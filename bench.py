@@ -41,6 +41,26 @@ FLOP_DENS_PASS, FLOP_DENS_GRAD, FLOP_HYDRO_FAR = 23.0, 63.0, 20.0
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
 
 
+def tree_lists_rate(traffic_path=PROFILE_TRAFFIC, peaks_path=os.path.join(ROOT, "MEASURED_PEAKS.json")):
+    """HBM rate of the tree and list build (latency-bound traversals, climbs
+    and scans): the DRAM bytes over the device time of those kernels from one
+    ncu capture of a force evaluation of the benchmark workload, against the
+    measured HBM copy rate (6.8 TB/s fallback).  None without a capture."""
+    if not os.path.exists(traffic_path):
+        return None
+    t = json.load(open(traffic_path)).get("tree_lists")
+    if not t or not t.get("ncu_ms"):
+        return None
+    hbm, src = 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+    if os.path.exists(peaks_path):
+        pk = json.load(open(peaks_path)).get("hbm_gbs")
+        if pk:
+            hbm, src = float(pk), "MEASURED_PEAKS.json hbm_gbs (measured copy)"
+    gbs = t["dram_bytes"] / (t["ncu_ms"] * 1e-3) / 1e9
+    return {"dram_bytes": t["dram_bytes"], "ncu_ms": t["ncu_ms"], "achieved_gbs": gbs, "peak_gbs": hbm,
+            "frac": gbs / hbm, "peak_source": src, "groups": t.get("groups"), "source": t.get("_source")}
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -258,24 +278,11 @@ def run_ours(args):
     per_kernel["hydro"]["pair_evaluations"] = {"full": int(st_k["evals_hydro_near"]),
                                                "signal_velocity_only": int(st_k["evals_hydro_far"])}
     traffic = None
-    tree_lists = None
     if os.path.exists(PROFILE_TRAFFIC):
         tr = json.load(open(PROFILE_TRAFFIC))
         if dom in tr:
             traffic = tr[dom].get("bytes_per_launch")
-        if "tree_lists" in tr:
-            # HBM rate of the tree and list build (latency-bound traversals and
-            # scans): DRAM bytes over device time of those kernels, one ncu
-            # capture of a force evaluation of this workload
-            t = tr["tree_lists"]
-            hbm, src = 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
-            peaks = os.path.join(ROOT, "MEASURED_PEAKS.json")
-            if os.path.exists(peaks) and json.load(open(peaks)).get("hbm_gbs"):
-                hbm, src = float(json.load(open(peaks))["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured copy)"
-            gbs = t["dram_bytes"] / (t["ncu_ms"] * 1e-3) / 1e9
-            tree_lists = {"dram_bytes": t["dram_bytes"], "ncu_ms": t["ncu_ms"], "achieved_gbs": gbs,
-                          "peak_gbs": hbm, "frac": gbs / hbm, "peak_source": src,
-                          "groups": t.get("groups"), "source": t.get("_source")}
+    tree_lists = tree_lists_rate()
 
     line = {"metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
             "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps,
