@@ -10,7 +10,7 @@ Tolerances (relative, per particle; vector fields by norm):
                 which are sums of strongly cancelling neighbour terms.
                 Per-particle errors are floored at 1e-3 of the field's largest
                 magnitude (1e-2 for the cancelling sums), so a particle whose
-                vector nearly cancels (symmetric neighbourhood) is judged
+                vector nearly cancels (symmetric neighbourhood) is measured
                 against the field's scale.  np and itr must match except where a neighbour sits at
                 q = 1 within FP32 rounding (at most 1% of particles).
 """
@@ -179,7 +179,7 @@ def _collision_system(seed, n=3000):
 
 @pytest.mark.parametrize("seed", [11, 12])
 def test_density_vs_oracle_collision(ctx, seed):
-    """Errors judged over all walks together (the field's own scale)."""
+    """Errors measured over all walks together (the field's own scale)."""
     s, _ = _collision_system(seed)
     groups = walks.make_groups(s["pos"], 100)
     jl = walks.gather_lists(s["pos"], s["rs"], groups)
