@@ -1837,6 +1837,11 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
     cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
     cudaMemset(s->scal.p, 0, sizeof(int) * S_NI);
     cudaMemset(s->dscal.p, 0, sizeof(double) * D_NI);
+    if (s->prm.quadrupole) {   // leaves keep Q = 0 (the refit writes internal nodes only)
+        cudaMemset(s->quad.p, 0, s->quad.cap * sizeof(double));
+        cudaMemset(s->fq0.p, 0, s->fq0.cap * sizeof(float4));
+        cudaMemset(s->fq1.p, 0, s->fq1.cap * sizeof(float4));
+    }
     cudaMemset(s->lscal.p, 0, sizeof(long long) * L_NI);
     *out = s;
     return SPH_OK;

@@ -344,12 +344,9 @@ refit_bottom(const dbl4 *pos, const double *h, const double *eps2, int n, Nodes 
             t.fmom[node] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)x.w);
             t.ptest[p] = make_float4((float)x.x, (float)x.y, (float)x.z, __double2float_ru(hp));
             sd[REFIT_B + threadIdx.x] = d;
-            if (QUAD) {
-                Quad z;
-                for (int k = 0; k < 6; ++k) z.q[k] = 0.0;
-                sq[REFIT_B + threadIdx.x] = leaf_moments(x, o);
-                store_quad(t, node, z);
-            }
+            // a leaf's stored quadrupole is 0, written once when the
+            // buffers are allocated; only its second moments enter the climb
+            if (QUAD) sq[REFIT_B + threadIdx.x] = leaf_moments(x, o);
             while (node != root) {
                 node = t.parent[node];
                 // internal nodes of the subtree have indices in [a, a + c)
