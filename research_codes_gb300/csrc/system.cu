@@ -28,6 +28,7 @@ using sphrt::HostBuf;
 namespace {
 
 constexpr double KSRH = sphk::KSRH;
+constexpr double INV_KSRH2 = 1.0 / (KSRH * KSRH);   // eps^2 = h^2 / ksrh^2 without an FP64 divide
 constexpr int ITEM_SPLIT_NJ = 4096;   // default list length above which a walk's items are halved (down to 4 i)
 // density neighbour lists: entries per lane (a lane with more sweeps) and
 // the default list radius over the first-pass h (later passes whose h grew
@@ -320,8 +321,10 @@ __global__ void permute(int n, const int *idx, Persist src, Persist dst) {
     }
 }
 
+// Softening of the first guess of h, for the refit after the tree build only
+// (the refit after the density phase and the gravity kernel use post_density's).
 __global__ void eps2_from_h(int n, const double *h, double *eps2) {
-    GRID_STRIDE(p, n) { eps2[p] = (h[p] / KSRH) * (h[p] / KSRH); }
+    GRID_STRIDE(p, n) { eps2[p] = h[p] * h[p] * INV_KSRH2; }
 }
 
 // compact group roots: position-indexed flags -> group arrays
@@ -626,7 +629,7 @@ __global__ void post_density(int n, const dbl4 *pos, const double *dens, const d
         pres[p] = P;
         vsnd[p] = c;
         bswt[p] = b;
-        const double e2 = (ksr[p] / KSRH) * (ksr[p] / KSRH);
+        const double e2 = f32 ? ksr[p] * ksr[p] * INV_KSRH2 : (ksr[p] / KSRH) * (ksr[p] / KSRH);
         eps2[p] = e2;
         const dbl4 x = pos[p];
         pe[p] = make_dbl4(x.x, x.y, x.z, e2);
