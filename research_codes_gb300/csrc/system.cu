@@ -1109,14 +1109,22 @@ void reduce(sph_system *s, F f, double *out) {
 
 // Morton sort + permutation + radix tree + refit + groups.
 // Bottom-up refit of the node data (after the tree build, and again when h
-// changed).  The quadrupoles depend only on positions and masses: the refit
-// after a change of h alone (quad = false) keeps those of the tree build.
-int refit_tree(sph_system *s, bool quad = true) {
+// changed).  Boxes, moments, centres of mass and quadrupoles depend only on
+// positions and masses: the refit after a change of h alone (full = false)
+// recomputes just the nodes' largest h and softening.
+int refit_tree(sph_system *s, bool full = true) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sphtree::Nodes t = s->nodes();
     CUDA_TRY(cudaMemsetAsync(s->visit.p, 0, sizeof(int) * (size_t)std::max(n - 1, 1), st));
-    if (s->prm.quadrupole && quad) {
+    if (!full) {
+        sphtree::refit_bottom_h<<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
+            s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS);
+        sphtree::refit_top_h<<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS);
+        sphtree::normalise_eps2<<<grid_for(n), 256, 0, st>>>(n, t);
+        return SPH_OK;
+    }
+    if (s->prm.quadrupole) {
         sphtree::refit_bottom<true><<<s->ctx->sm_count * 8, sphtree::REFIT_B, 0, st>>>(
             s->pos[0].p, s->ksr[0].p, s->eps2.p, n, t, s->roots.p, s->scal.p + S_NROOTS, s->box.p);
         sphtree::refit_top<true><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS,
@@ -1127,7 +1135,7 @@ int refit_tree(sph_system *s, bool quad = true) {
         sphtree::refit_top<false><<<s->ctx->sm_count * 2, 256, 0, st>>>(n, t, s->roots.p, s->scal.p + S_NROOTS,
                                                                        s->box.p);
     }
-    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t, s->box.p, s->prm.quadrupole != 0 && quad);
+    sphtree::normalise_nodes<<<grid_for(n), 256, 0, st>>>(n, t, s->box.p, s->prm.quadrupole != 0);
     return SPH_OK;
 }
 

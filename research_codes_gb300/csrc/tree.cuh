@@ -395,6 +395,95 @@ __global__ void refit_top(int n, Nodes t, const int *roots, const int *n_roots, 
     }
 }
 
+// Refit after a change of h alone (positions, masses, boxes, centres of mass
+// and quadrupoles unchanged): only the largest h of each node (flo.w, and a
+// particle's ptest.w) and its sum m eps^2 are recomputed, with the same
+// operations in the same order as the full refit, so the node data are bit
+// for bit those of a full refit.  Single-field stores leave the rest of each
+// record untouched.
+__global__ void __launch_bounds__(REFIT_B)
+refit_bottom_h(const double *h, const double *eps2, int n, Nodes t, const int *roots, const int *n_roots) {
+    __shared__ float sh[2 * REFIT_B];    // largest h (rounded up), slots as refit_bottom
+    __shared__ double se[2 * REFIT_B];   // sum m eps^2
+    __shared__ int visit[REFIT_B];
+    const int nr = *n_roots;
+    for (int r = blockIdx.x; r < nr; r += gridDim.x) {
+        const int root = roots[r];
+        const int a = t.first[root];
+        const int c = t.count[root];
+        if (c < 1 || c > REFIT_B) continue;   // not a bottom subtree (block-uniform)
+        visit[threadIdx.x] = 0;
+        __syncthreads();
+        if ((int)threadIdx.x < c) {
+            const int p = a + threadIdx.x;
+            int node = n - 1 + p;
+            const double hp = h[p], ep = eps2[p];
+            const double m = t.mom[node].w;   // a leaf holds its particle's (x, m)
+            float hw = __double2float_ru(hp);
+            double s = m * ep;
+            t.flo[node].w = hw;
+            t.eps2[node] = ep;
+            t.ptest[p].w = hw;
+            sh[REFIT_B + threadIdx.x] = hw;
+            se[REFIT_B + threadIdx.x] = s;
+            while (node != root) {
+                node = t.parent[node];
+                if (node < a || node >= a + c) break;
+                __threadfence_block();
+                if (atomicAdd(&visit[node - a], 1) == 0) break;   // sibling not finished yet
+                __threadfence_block();
+                const int2 ch = t.child[node];
+                const int sa = (ch.x >= n - 1) ? REFIT_B + (ch.x - (n - 1) - a) : ch.x - a;
+                const int sb = (ch.y >= n - 1) ? REFIT_B + (ch.y - (n - 1) - a) : ch.y - a;
+                if (sa < 0 || sa >= 2 * REFIT_B || sb < 0 || sb >= 2 * REFIT_B) break;
+                hw = fmaxf(sh[sa], sh[sb]);
+                s = se[sa] + se[sb];
+                sh[node - a] = hw;
+                se[node - a] = s;
+                t.flo[node].w = hw;
+                t.eps2[node] = s;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// visit[] (internal nodes) is zero on entry.
+__global__ void refit_top_h(int n, Nodes t, const int *roots, const int *n_roots) {
+    const int nr = *n_roots;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nr; r += gridDim.x * blockDim.x) {
+        int node = t.parent[roots[r]];
+        while (node >= 0) {
+            int arrived;
+            asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;"
+                         : "=r"(arrived) : "l"(&t.visit[node]) : "memory");
+            if (arrived == 0) break;   // sibling not finished yet
+            const int2 ch = t.child[node];
+            const int cs[2] = {ch.x, ch.y};
+            float hw[2];
+            double s[2];
+            for (int k = 0; k < 2; ++k) {
+                const int v = cs[k];
+                hw[k] = __ldcg(&t.flo[v].w);
+                // a leaf stores its particle's eps^2, an internal node the sum
+                s[k] = (v >= n - 1) ? __ldcg(&t.mom[v].w) * __ldcg(&t.eps2[v]) : __ldcg(&t.eps2[v]);
+            }
+            t.flo[node].w = fmaxf(hw[0], hw[1]);
+            t.eps2[node] = s[0] + s[1];
+            node = t.parent[node];
+        }
+    }
+}
+
+// Mass-weighted mean eps^2 of the internal nodes after refit_*_h (their
+// centres of mass and masses are already normalised).
+__global__ void normalise_eps2(int n, Nodes t) {
+    for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < n - 1; node += gridDim.x * blockDim.x) {
+        const double m = t.mom[node].w;
+        t.eps2[node] = (m > 0.0) ? t.eps2[node] * (1.0 / m) : 0.0;
+    }
+}
+
 // ---- 4. groups -------------------------------------------------------------
 // flag[first particle of a group root] = 1, root_at[first] = node.
 __global__ void mark_groups(Nodes t, int n, int n_group, int *flag, int *root_at) {
