@@ -2,6 +2,7 @@
 function include/sph_gb300.h declares, and its struct layouts equal both the
 numpy mirrors and the reference classes' sizes."""
 import ctypes
+import os
 
 import pytest
 
@@ -59,3 +60,35 @@ def test_no_device_is_reported_cleanly(lib):
     h = ctypes.c_void_p()
     assert lib.sph_context_create(None, ctypes.byref(h)) == abi.SPH_ERR_NO_DEVICE
     assert not h.value
+
+
+def test_c_struct_mirrors_match_the_header(tmp_path):
+    """sizeof and every member offset of the parameter and statistics structs,
+    compiled from include/sph_gb300.h by the host C compiler, equal the ctypes
+    mirrors the Python layer reads them with."""
+    import shutil
+    import subprocess
+
+    from research_codes_gb300 import system
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    mirrors = [("sph_params", _lib.Params), ("sph_system_params", system.SystemParams),
+               ("sph_system_stats", system.SystemStats)]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "sph_gb300.h"', "int main(void) {"]
+    for cname, cls in mirrors:
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", f"-I{inc}", str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = []
+    for _, cls in mirrors:
+        want.append(ctypes.sizeof(cls))
+        want += [getattr(cls, f).offset for f, _ in cls._fields_]
+    assert got == want
