@@ -1,5 +1,5 @@
 """Test infrastructure only: a numpy restatement of the reference's analysis
-scripts, the checker of research_codes_gb300.analysis.  Pinned against the
+scripts, the oracle for research_codes_gb300.analysis.  Pinned against the
 reference's own functions by tests/golden/analysis_n2000.npz.
 
   centre_of_gravity  analysis/common.py:71-90

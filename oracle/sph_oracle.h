@@ -4,7 +4,7 @@
  * Plain scalar FP64 C restatement of the reference's CPU functors
  * (yamauchi1132/Research_Codes, sph_yamauchi/run, USE_HELMHOLTZ build without
  * USE_INTRINSICS).  Only the tests, the smoke check and the CPU-baseline leg of
- * bench.py use it, always as the checker or the timed CPU reference; the
+ * bench.py use it, always as the oracle or the timed CPU reference; the
  * product library never links it.
  *
  * Parity of this restatement is pinned against the reference's own functors

@@ -1,7 +1,7 @@
 """Independent replicas of the engine on several GPUs of one node.
 
 The interaction path shards naturally (walks are independent given their
-lists), but this build runs one GPU per process without exchanging particles:
+lists), but this module runs one GPU per process without exchanging particles:
 each rank evolves its own system (seeded by its rank), and the job's
 throughput is the work of all ranks over the slowest rank's time.  The only
 collectives are these scalar reductions and barriers (NCCL between GPUs,
