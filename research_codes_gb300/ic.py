@@ -1,4 +1,5 @@
-"""Synthetic initial conditions: Lane-Emden polytropes and two-star placement.
+"""Synthetic initial conditions: Lane-Emden polytropes, rescaled stars and
+two-star placement (fixed separation and velocity, or an unbound Kepler orbit).
 
 Restates the pipeline of the reference's polytropic_initial_condition tool
 (main.cpp:12-227, lane_emden.hpp:14-53): a cubic lattice inside the unit
@@ -95,7 +96,8 @@ def polytrope(n_part, mass_msun, radius_rsun, n_index, seed=0, eta=1.6):
     """One polytropic star centred on the origin at rest.
 
     Returns a dict of FP64 arrays in code units: pos (n,3), vel (n,3), mass,
-    uene, ksr, dens (Lane-Emden density at each particle), plus scalars.
+    uene, ksr, dens (Lane-Emden density at each particle), plus the scalars
+    M, R, K, rho_c and n_index.
     """
     rng = np.random.default_rng(seed)
     xi, th, dth = lane_emden(n_index)
@@ -126,7 +128,7 @@ def polytrope(n_part, mass_msun, radius_rsun, n_index, seed=0, eta=1.6):
     uene = units.EOS_N * pres / dens
     ksr = eta * units.KSRH * (mass / dens) ** (1.0 / 3.0)
     return dict(pos=pos, vel=np.zeros_like(pos), mass=mass, uene=uene, ksr=ksr, dens=dens,
-                M=M, R=R, K=K, rho_c=rho_c)
+                M=M, R=R, K=K, rho_c=rho_c, n_index=n_index)
 
 
 def escape_speed(m_tot, separation):
@@ -156,6 +158,101 @@ def two_stars(star1, star2, separation, impact, v_rel):
     out["vel"] = np.concatenate([star1["vel"] + v1, star2["vel"] + v2])
     out["istar"] = np.concatenate([np.zeros(len(star1["mass"]), np.int64),
                                    np.ones(len(star2["mass"]), np.int64)])
+    return out
+
+
+def rescale(star, m_mul, r_mul):
+    """A relaxed star moved to mass x m_mul and radius x r_mul, as the
+    reference's change_polytropic_scale tool does (main.cpp:96-115, factors
+    user_define.hpp:9-10): positions and smoothing lengths scale with r_mul,
+    velocities with sqrt(m_mul / r_mul), specific energies with
+    m_mul / r_mul, which keeps the star in the same (scaled) equilibrium.
+    Unit-independent: works on code-unit or cgs arrays alike.  Density-like
+    extras (dens, rho_c, K) are scaled to stay consistent; the reference tool
+    leaves its density column as read, since the run recomputes it."""
+    v_mul = math.sqrt(m_mul / r_mul)
+    u_mul = m_mul / r_mul
+    out = dict(star)
+    out["mass"] = star["mass"] * m_mul
+    out["pos"] = star["pos"] * r_mul
+    out["vel"] = star["vel"] * v_mul
+    out["uene"] = star["uene"] * u_mul
+    out["ksr"] = star["ksr"] * r_mul
+    if "dens" in star:
+        out["dens"] = star["dens"] * (m_mul / r_mul ** 3)
+    if "M" in star:
+        out["M"] = star["M"] * m_mul
+    if "R" in star:
+        out["R"] = star["R"] * r_mul
+    if "rho_c" in star:
+        out["rho_c"] = star["rho_c"] * (m_mul / r_mul ** 3)
+    if "K" in star and "n_index" in star:
+        n = star["n_index"]
+        out["K"] = star["K"] * u_mul * (m_mul / r_mul ** 3) ** (-1.0 / n)
+    return out
+
+
+def unbound_orbit(m1, m2, r_peri, v_inf, r_sep, G=None):
+    """Two point masses on the Kepler orbit with relative speed `v_inf` at
+    infinity and pericentre distance `r_peri`, at separation `r_sep` before
+    pericentre, in their centre-of-mass frame; the orbital plane is z = 0 and
+    pericentre lies on +x.
+
+    The reference's two_body_initial_condition tool (main.cpp:87-140, inputs
+    user_define.hpp:13-24) derives the hyperbola from the impact parameter
+    b = r_p v_p / v_inf and the energy k = v_inf^2 / 2: eccentricity
+    e = sqrt(1 + 2 k (b v_inf)^2 / mu^2), true anomaly from
+    r = a (e^2 - 1) / (1 + e cos f) with sin f < 0, and velocity
+    sqrt(mu / p) (-sin f, e + cos f).  Here the same conic is written with
+    the angular momentum h = r_p v_p and the semi-latus rectum
+    p = h^2 / mu = r_p (1 + e), so that v_inf = 0 (the parabola, e = 1,
+    p = 2 r_p) is the same formula.  Star 1 sits at m2 / M of the relative
+    vector (star 1 minus star 2), star 2 at -m1 / M of it.
+
+    Returns (x1, x2, v1, v2, elements) with 3-vectors and
+    elements = {b, e, p, h, f}; raises ValueError when r_sep < r_peri.
+    """
+    if G is None:
+        G = units.G
+    if v_inf < 0 or r_peri <= 0:
+        raise ValueError("need v_inf >= 0 and r_peri > 0")
+    if r_sep < r_peri:
+        raise ValueError("the stars start inside the pericentre distance")
+    mu = G * (m1 + m2)
+    k_inf = 0.5 * v_inf * v_inf
+    v_p = math.sqrt(2.0 * (k_inf + mu / r_peri))
+    h = r_peri * v_p
+    e = math.sqrt(1.0 + 2.0 * k_inf * h * h / (mu * mu))
+    p = h * h / mu
+    cos_f = min(1.0, (p / r_sep - 1.0) / e)
+    sin_f = -math.sqrt(max(0.0, 1.0 - cos_f * cos_f))
+    w = math.sqrt(mu / p)
+    rel_x = np.array([r_sep * cos_f, r_sep * sin_f, 0.0])
+    rel_v = np.array([-w * sin_f, w * (cos_f + e), 0.0])
+    q1, q2 = m2 / (m1 + m2), -m1 / (m1 + m2)
+    el = {"b": h / v_inf if v_inf > 0 else math.inf, "e": e, "p": p, "h": h,
+          "f": math.atan2(sin_f, cos_f)}
+    return q1 * rel_x, q2 * rel_x, q1 * rel_v, q2 * rel_v, el
+
+
+def two_stars_on_orbit(star1, star2, r_peri, v_inf, r_sep, G=None):
+    """Places two stars on the orbit of `unbound_orbit` (the reference's
+    two_body_initial_condition tool, main.cpp:142-158): each star's particles
+    are shifted by its centre's position and velocity.  Returns the same
+    layout as `two_stars`, plus `id` (star 2 numbered after star 1, as
+    main.cpp:152 does) and the orbit's elements under `orbit`."""
+    m1, m2 = star1["mass"].sum(), star2["mass"].sum()
+    x1, x2, v1, v2, el = unbound_orbit(m1, m2, r_peri, v_inf, r_sep, G)
+    n1, n2 = len(star1["mass"]), len(star2["mass"])
+    out = {}
+    for key in ("mass", "uene", "ksr", "dens"):
+        if key in star1 and key in star2:
+            out[key] = np.concatenate([star1[key], star2[key]])
+    out["pos"] = np.concatenate([star1["pos"] + x1, star2["pos"] + x2])
+    out["vel"] = np.concatenate([star1["vel"] + v1, star2["vel"] + v2])
+    out["istar"] = np.concatenate([np.zeros(n1, np.int64), np.ones(n2, np.int64)])
+    out["id"] = np.arange(n1 + n2, dtype=np.int64)
+    out["orbit"] = el
     return out
 
 
