@@ -1,4 +1,5 @@
-"""CPU checks of the bench line's profile-derived figures (no GPU)."""
+"""CPU checks of the bench line's host-side parts: profile-derived figures,
+the clock sampler's parsing and the CPU-baseline rate mix (no GPU)."""
 import json
 
 import bench
@@ -32,3 +33,54 @@ def test_pair_kernel_traffic_entries():
     for k in ("density", "hydro", "gravity"):
         assert tr[k]["bytes_per_launch"] == round(tr[k]["read"] + tr[k]["write"])
         assert tr[k]["ncu_ms"] > 0
+
+
+class _FakeSmi:
+    """Stands in for `nvidia-smi --query-gpu=... -lms 200`: yields fixed lines."""
+    lines = []
+
+    def __init__(self, *a, **kw):
+        import io
+        self.stdout = io.StringIO("".join(self.lines))
+
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+    def kill(self):
+        pass
+
+
+def test_clock_sampler_parses_samples_and_reasons(monkeypatch):
+    _FakeSmi.lines = [
+        "1965, 2070, 900.10, Not Active, Not Active, Not Active, Not Active\n",
+        "1980, 2070, 1201.5, Not Active, Not Active, Not Active, Active\n",
+        "[N/A], [N/A], [N/A], Not Active, Not Active, Not Active, Not Active\n",
+        "2010, 2070, 1100.0, Not Active, Not Active, Not Active, Not Active\n",
+        "garbage\n",
+    ]
+    monkeypatch.setattr(bench.subprocess, "Popen", _FakeSmi)
+    c = bench.ClockSampler()
+    c.start()
+    c.thread.join(timeout=5)
+    r = c.stop()
+    assert r["samples"] == 4                 # the malformed line is dropped
+    assert r["sm_mhz"] == 1980.0 and r["sm_max_mhz"] == 2070.0   # median of the numeric samples
+    assert r["reasons"] == ["sw_power_cap"]
+
+
+def test_clock_sampler_without_nvidia_smi(monkeypatch):
+    def missing(*a, **kw):
+        raise FileNotFoundError("nvidia-smi")
+    monkeypatch.setattr(bench.subprocess, "Popen", missing)
+    c = bench.ClockSampler()
+    c.start()
+    assert c.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+
+def test_combined_rate_is_the_pair_weighted_harmonic_mean():
+    rates = {"density": (1e9, 1.0), "hydro": (4e9, 2.0)}     # 1e9 and 2e9 pairs/s
+    assert abs(bench.combined_rate(rates, {"density": 1, "hydro": 1}) - 2 / (1 / 1e9 + 1 / 2e9)) < 1e-3
+    assert abs(bench.combined_rate(rates, {"density": 3, "hydro": 0}) - 1e9) < 1e-3
