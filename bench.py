@@ -289,7 +289,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math (FP32C), f64 state",
             "data": "synthetic seeded polytropes (ic.config_system)",
-            "config": {"workload": f"{args.config}: off-axis unequal-mass collision, N={n}, n_group={args.n_group}, "
+            "config": {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, n_group={args.n_group}, "
                                    f"theta=0.5, eta={ETA}", "n_particles": n,
                        "l2": "inputs larger than L2 (particle state + lists ~2 GB per step)",
                        "pairs_per_step": pairs, "density_walks": st["density_iterations"],
@@ -497,7 +497,7 @@ def run_reference(args):
             "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * el_t / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded polytropes (ic.config_system)",
-            "config": {"workload": f"{args.config}: off-axis unequal-mass collision, N={n}, n_group={args.n_group}, "
+            "config": {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, n_group={args.n_group}, "
                                    f"theta=0.5, eta={ETA}", "n_particles": n},
             "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": nthreads, "kind": "port",
                              "sample": f"{len(take)} of {len(groups)} walks per step (density, hydro; gravity "
@@ -508,6 +508,12 @@ def run_reference(args):
 
 ETA = 1.18
 NODES = None
+# what each configuration of ic.config_system is
+WORKLOADS = {"c0": "single n=1.5 polytrope (1 Msun, 1 Rsun)",
+             "c1": "head-on collision of two n=3 polytropes (2 x 10 Msun, 4 Rsun)",
+             "c2": "off-axis unequal-mass collision",
+             "c3": "head-on collision of two n=3 polytropes (2 x 10 Msun, 4 Rsun)",
+             "c4": "off-axis unequal-mass collision, quadrupole gravity"}
 
 
 def main():

@@ -84,3 +84,34 @@ def test_combined_rate_is_the_pair_weighted_harmonic_mean():
     rates = {"density": (1e9, 1.0), "hydro": (4e9, 2.0)}     # 1e9 and 2e9 pairs/s
     assert abs(bench.combined_rate(rates, {"density": 1, "hydro": 1}) - 2 / (1 / 1e9 + 1 / 2e9)) < 1e-3
     assert abs(bench.combined_rate(rates, {"density": 3, "hydro": 0}) - 1e9) < 1e-3
+
+
+def _run_reference_arm(rank, tmp_path):
+    import os
+    import subprocess
+    import sys
+    env = dict(os.environ, RANK=str(rank), WORLD_SIZE="2" if rank else "1", OMP_NUM_THREADS="2")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    return subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--config", "c0",
+                           "--scale", "0.2", "--steps", "1", "--warmup", "0"],
+                          cwd=str(tmp_path), env=env, capture_output=True, text=True, timeout=300)
+
+
+def test_reference_arm_prints_one_contract_line(tmp_path):
+    p = _run_reference_arm(0, tmp_path)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    r = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in r, k
+    assert r["impl"] == "reference" and r["value"] > 0 and r["warmup"] >= 3
+    assert r["cpu_baseline"]["kind"] == "port" and r["cpu_baseline"]["value"] == r["value"]
+    assert r["e2e"] == {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert r["config"]["workload"].startswith("c0: single n=1.5 polytrope")
+
+
+def test_reference_arm_other_ranks_exit_quietly(tmp_path):
+    p = _run_reference_arm(1, tmp_path)
+    assert p.returncode == 0 and p.stdout.strip() == ""
