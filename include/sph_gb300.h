@@ -324,8 +324,8 @@ typedef struct sph_system_params {
     double  theta;       /* gravity opening angle (main.cpp:394: 0.5)                   */
     double  G;           /* gravitational constant in code units (hdr_heos.hpp:102)     */
     double  c_dt;        /* CoefficientOfTimestep (0.1)                                 */
-    double  dt_max;      /* MaximumTimestep (hdr_hgas.hpp:1240: 10)                     */
-    double  dt_min;      /* MinimumTimestep (1e-16)                                     */
+    double  dt_max;      /* MaximumTimestep (hdr_hgas.hpp:1240: 10); finite, >= dt_min   */
+    double  dt_min;      /* MinimumTimestep (1e-16); > 0, else INVALID_ARGUMENT         */
     double  alpha_max, alpha_min, alphu_max, alphu_min;  /* .head run parameters       */
     int32_t ksr_max_mode;/* 0: the context's fixed ksr_max; 1: the reference rule —
                             star-centre separation at start (hdr_hgas.hpp:1335), then

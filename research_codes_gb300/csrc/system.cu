@@ -1822,6 +1822,12 @@ extern "C" void sph_system_params_default(sph_system_params *p) {
     p->hydro_signal_skip = 1;
 }
 
+// update_dt halves the step until it is below the limit or at dt_min: that
+// loop ends only for a positive dt_min and a finite dt_max.
+static bool dt_range_ok(const sph_system_params &p) {
+    return p.dt_min > 0.0 && p.dt_max >= p.dt_min && p.dt_max < INFINITY;
+}
+
 extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_params *p, sph_system **out) {
     if (!ctx || !out || n < 2 || n > (1LL << 30)) return SPH_ERR_INVALID_ARGUMENT;
     *out = nullptr;
@@ -1831,7 +1837,7 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
     s->n = (int)n;
     if (p) s->prm = *p; else sph_system_params_default(&s->prm);
     if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || s->prm.n_leaf > sphtree::MAX_LEAF || !(s->prm.theta > 0.0) ||
-        s->prm.density_list_slack > MAX_NBR_SLACK) {
+        s->prm.density_list_slack > MAX_NBR_SLACK || !dt_range_ok(s->prm)) {
         delete s;
         return SPH_ERR_INVALID_ARGUMENT;
     }
@@ -2082,6 +2088,8 @@ extern "C" int sph_system_set_params(sph_system *s, const sph_system_params *p) 
                                 sphtree::MAX_LEAF);
     if (p->density_list_slack > MAX_NBR_SLACK)
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "density_list_slack above %g", (double)MAX_NBR_SLACK);
+    if (!dt_range_ok(*p))
+        return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "need 0 < dt_min <= dt_max < infinity");
     if (p->quadrupole && !s->prm.quadrupole)
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT,
                                 "quadrupole needs a system created with it (node moment buffers)");

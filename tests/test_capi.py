@@ -92,3 +92,21 @@ def test_c_struct_mirrors_match_the_header(tmp_path):
         want.append(ctypes.sizeof(cls))
         want += [getattr(cls, f).offset for f, _ in cls._fields_]
     assert got == want
+
+
+def test_time_step_limits_are_validated_before_any_device_call():
+    """dt_min <= 0 or an infinite dt_max would let the step-halving loop run
+    without end; sph_system_create rejects them before it touches the
+    context, so a zeroed stand-in context suffices here."""
+    from research_codes_gb300 import system
+    lib = system._declare(_lib.load())
+    fake_ctx = ctypes.create_string_buffer(1 << 16)
+    out = ctypes.c_void_p()
+    for dt_min, dt_max in ((0.0, 10.0), (-1e-16, 10.0), (1e-16, float("inf")), (1.0, 0.5),
+                           (float("nan"), 10.0)):
+        p = system.SystemParams()
+        lib.sph_system_params_default(ctypes.byref(p))
+        p.dt_min, p.dt_max = dt_min, dt_max
+        assert lib.sph_system_create(ctypes.cast(fake_ctx, ctypes.c_void_p), 1000, ctypes.byref(p),
+                                     ctypes.byref(out)) == abi.SPH_ERR_INVALID_ARGUMENT, (dt_min, dt_max)
+        assert not out.value
