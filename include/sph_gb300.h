@@ -400,6 +400,9 @@ typedef struct sph_system_stats {
                                              (32 x the largest per-lane count of
                                              each tile); marked / slots is the
                                              lane utilisation of those loops     */
+    int64_t hydro_rows_overflowed;        /* FP32C: particles with more marked
+                                             pairs than a list row holds (summed
+                                             over the walk's whole list instead) */
     int32_t last_status;
 } sph_system_stats;
 
@@ -477,11 +480,14 @@ int sph_system_predict(sph_system *sys);
 int sph_system_adjoint_forces(sph_system *sys, const double *seed, double *grad);
 
 /* Interaction lists of the last force evaluation (kind 0 density — the first
- * walk, which covers every group —, 1 hydro, 2 gravity), in Morton order:
- * walk w has i-particles [i_first[w], i_first[w] + i_count[w]) and list
- * entries j_idx[j_off[w] .. j_off[w+1]); for gravity an entry >= n is tree
- * node entry - n (see sph_system_get_nodes).  Call with null arrays to get
- * *n_walk and *n_entries first. */
+ * walk, which covers every group —, 1 hydro, 2 gravity, 3 the last density
+ * re-walk of the search-radius loop, calcDensityKernel hdr_density.hpp:
+ * 372-415), in Morton order: walk w has i-particles [i_first[w], i_first[w]
+ * + i_count[w]) and list entries j_idx[j_off[w] .. j_off[w+1]); for gravity
+ * an entry >= n is tree node entry - n (see sph_system_get_nodes); a re-walk
+ * evaluates only the particles of its groups that were still iterating, with
+ * their grown search radius.  Call with null arrays to get *n_walk and
+ * *n_entries first. */
 int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t *n_entries,
                          int32_t *i_first, int32_t *i_count, int64_t *j_off, int32_t *j_idx);
 

@@ -84,6 +84,7 @@ int init_grids(sph_context *ctx) {
                         &ctx->grid[1][1]);
     e |= occupancy_grid(sphk::gravity_kernel<false, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[2][0]);
     e |= occupancy_grid(sphk::gravity_kernel<true, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[2][1]);
+    e |= occupancy_grid(sphk::hydro_df_lists, sphk::HYDRO_DF_THREADS, ctx->sm_count, &ctx->grid_df);
     return e;
 }
 
@@ -101,11 +102,19 @@ void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStr
         sphk::density_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
 }
 
-void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s) {
-    if (precision == SPH_PREC_FP64)
+// FP32C: the signal-velocity / marking kernel, then the double-float pass
+// over the marked-pair rows and over the overflowed particles (a.df_novf
+// must be zero at launch; dfgrid: blocks for the two double-float kernels).
+void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid) {
+    if (precision == SPH_PREC_FP64) {
         sphk::hydro_kernel<true, HYDRO64_WARPS><<<grid, HYDRO64_WARPS * 32, 0, s>>>(a);
-    else
-        sphk::hydro_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
+        return;
+    }
+    sphk::hydro_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
+    if (a.n_i <= 0) return;
+    const int need = (a.n_i + sphk::HYDRO_DF_THREADS - 1) / sphk::HYDRO_DF_THREADS;
+    sphk::hydro_df_lists<<<std::max(1, std::min(need, dfgrid)), sphk::HYDRO_DF_THREADS, 0, s>>>(a);
+    sphk::hydro_df_sweep<<<std::max(1, std::min(need, dfgrid)), sphk::HYDRO_DF_THREADS, 0, s>>>(a);
 }
 
 void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s) {
@@ -304,7 +313,7 @@ extern "C" int sph_context_create(const sph_params *p, sph_context **out) {
     int cc_major = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, prm.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_queue, 8 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_queue, 9 * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_flags, 8 * sizeof(int));
     if (e == cudaSuccess && init_grids(ctx) != 0) e = cudaErrorInvalidDeviceFunction;
     if (e != cudaSuccess) {
@@ -674,11 +683,11 @@ extern "C" int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
     if (f32 && ni > 0)
         sphk::make_hydro_records<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(
             ni, ks.a4[0].p, ks.a4[1].p, ks.a4[4].p, ks.a4[5].p, ks.a2[0].p, ks.f4[0].p, ks.f4[1].p, ks.f4[2].p,
-            ks.f4[3].p, ks.f4[8].p, ks.f4[9].p, ks.f4[10].p);
+            ks.f4[3].p, ks.f4[8].p, ks.f4[9].p, ks.f4[10].p, ks.f4[14].p);
     if (f32 && nj > 0)
         sphk::make_hydro_records<<<eltwise_grid(nj), 256, 0, ctx->stream>>>(
             nj, ks.a4[2].p, ks.a4[3].p, ks.a4[6].p, ks.a4[7].p, ks.a2[1].p, ks.f4[4].p, ks.f4[5].p, ks.f4[6].p,
-            ks.f4[7].p, ks.f4[11].p, ks.f4[12].p, ks.f4[13].p);
+            ks.f4[7].p, ks.f4[11].p, ks.f4[12].p, ks.f4[13].p, ks.f4[15].p);
     if (!ks.items.empty()) {
         sphk::HydroArgs a{};
         a.n_eval_near = nullptr;
@@ -700,7 +709,17 @@ extern "C" int sph_dispatch_hydro(sph_context *ctx, int32_t tag, int32_t n_walk,
         a.queue = ctx->d_queue + K_HYDRO;
         a.o_acch = ks.o[0].p; a.o_accg = ks.o[1].p; a.o_udot = ks.o[2].p; a.o_vsmx = ks.o[3].p;
         a.o_diffu = ks.o[4].p;
-        launch_hydro(a, ctx->prm.precision, pair_grid(ctx, K_HYDRO, ctx->prm.precision, a.n_items), ctx->stream);
+        a.fi_g4 = ks.f4[14].p; a.fj_g4 = ks.f4[15].p;
+        a.df_list = ks.hl_list.p; a.df_cap = sphk::HYDRO_LIST_CAP; a.df_cnt = ks.hl_cnt.p;
+        a.df_ovf = ks.hl_ovf.p; a.df_novf = ctx->d_queue + 8; a.n_i = ni;
+        if (f32) {
+            // walks without items leave their rows empty; no overflow yet
+            cudaError_t e = cudaMemsetAsync(ks.hl_cnt.p, 0, sizeof(int) * (size_t)ni, ctx->stream);
+            if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_queue + 8, 0, sizeof(int), ctx->stream);
+            if (e != cudaSuccess) return cuda_error(ctx, e, "memset");
+        }
+        launch_hydro(a, ctx->prm.precision, pair_grid(ctx, K_HYDRO, ctx->prm.precision, a.n_items), ctx->stream,
+                     ctx->grid_df);
     }
     if (ni > 0)
         pack_hydro<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(

@@ -73,7 +73,9 @@ struct KindState {
     HostBuf<char> h_in, h_out;
     DevBuf<char> d_in, d_out;
     DevBuf<dbl4> a4[8];
-    DevBuf<float4> f4[14];   // FP32C double-float records
+    DevBuf<float4> f4[16];   // FP32C double-float records
+    DevBuf<int> hl_list, hl_cnt;       // FP32C hydro: marked-pair rows and counts
+    DevBuf<int2> hl_ovf;               // FP32C hydro: overflowed rows (particle, walk)
     DevBuf<double2> a2[2];
     DevBuf<long long> id[2];
     DevBuf<double> d1[2];
@@ -107,6 +109,8 @@ struct KindState {
         for (int k = 2; k < 5; ++k) e |= o[k].ensure(ni);
         for (int k = 0; k < 4; ++k) e |= f4[k].ensure(ni) | f4[4 + k].ensure(nj);
         for (int k = 8; k < 11; ++k) e |= f4[k].ensure(ni) | f4[k + 3].ensure(nj);
+        e |= f4[14].ensure(ni) | f4[15].ensure(nj);
+        e |= hl_list.ensure(ni * sphk::HYDRO_LIST_CAP) | hl_cnt.ensure(ni) | hl_ovf.ensure(ni);
         return e;
     }
     int ensure_gravity(size_t ni, size_t nj) {
@@ -123,6 +127,9 @@ struct KindState {
         d_out.release();
         for (auto &b : a4) b.release();
         for (auto &b : f4) b.release();
+        hl_list.release();
+        hl_cnt.release();
+        hl_ovf.release();
         for (auto &b : a2) b.release();
         for (auto &b : id) b.release();
         for (auto &b : d1) b.release();
@@ -142,9 +149,11 @@ struct sph_context {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     int *d_queue = nullptr;   // [0..2] work-queue counters, [3] density re-check count,
-                              // [4..6] finite flags, [7] re-check item count
+                              // [4..6] finite flags, [7] re-check item count,
+                              // [8] FP32C hydro rows that overflowed
     int *h_flags = nullptr;   // pinned copies of the flags
     int grid[3][2] = {{0}};   // persistent grid per kind and precision
+    int grid_df = 0;          // resident blocks of the double-float hydro pass
     sphrt::KindState kind[3];
     int n_systems = 0;        // live sph_system objects using this context
     char err[512] = {0};
@@ -156,6 +165,6 @@ int set_error(sph_context *ctx, int status, const char *fmt, ...);
 int cuda_error(sph_context *ctx, cudaError_t e, const char *what);
 int pair_grid(const sph_context *ctx, int kind, int precision, int n_items);
 void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStream_t s);
-void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s);
+void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid);
 void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s);
 }  // namespace sphrt

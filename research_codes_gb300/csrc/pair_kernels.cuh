@@ -22,6 +22,7 @@
 //    coordinates without compensation: the "plain FP64 GPU" comparator.
 #pragma once
 
+#include "hydro_df.cuh"
 #include "sph_device.cuh"
 
 // Minimum resident blocks per SM requested from the compiler for the FP32C
@@ -732,7 +733,26 @@ struct HydroArgs {
     // full), [1] lane slots their loops occupied (per 32-entry tile, 32 x
     // the largest per-lane count)
     unsigned long long *n_mark = nullptr;
+    // FP32C: the kernel evaluates the signal velocities and writes, per
+    // i-particle, the j indices of its marked pairs (self pairs excluded) to
+    // row i of df_list (df_cap entries) and their number to df_cnt[i]; a
+    // particle with more than df_cap appends (i, walk) to df_ovf and counts
+    // it in *df_novf.  The double-float pass (hydro_df_lists /
+    // hydro_df_sweep) then forms acch, accg, udot and diffu.  g4 records:
+    // (1/h hi, 1/h lo, h^-4 hi, h^-4 lo).
+    const float4 *fi_g4 = nullptr, *fj_g4 = nullptr;
+    int *df_list = nullptr;
+    int df_cap = 0;
+    int *df_cnt = nullptr;
+    int2 *df_ovf = nullptr;
+    int *df_novf = nullptr;
+    int n_i = 0;   // i-particles (the double-float pass covers [0, n_i))
 };
+
+// Capacity of a particle's row of marked pairs in the FP32C hydro lists
+// (~50-60 marked pairs are typical; a particle whose row overflows is summed
+// over its walk's whole list instead).
+constexpr int HYDRO_LIST_CAP = 128;
 
 template <bool F64, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_HYDRO_MIN_BLOCKS)
@@ -750,16 +770,20 @@ hydro_kernel(const HydroArgs a) {
     __shared__ R4 s_p2[WARPS][64];    // position lo parts, vsnd
     __shared__ R4 s_v1[WARPS][64];    // velocity hi, mass
     __shared__ R4 s_v2[WARPS][64];    // velocity lo, hinv^4
-    __shared__ R4 s_c[WARPS][64];     // P (hi), presc, bswt, dens
-    __shared__ R4 s_d[WARPS][64];     // alph, alphu, u (hi), eta
-    __shared__ float2 s_f[WARPS][64]; // P lo, u lo
+    // pair-formula fields (FP64 mode only: FP32C forms the pair sums in a
+    // separate double-float pass)
+    __shared__ R4 s_c[F64 ? WARPS : 1][64];     // P (hi), presc, bswt, dens
+    __shared__ R4 s_d[F64 ? WARPS : 1][64];     // alph, alphu, u (hi), eta
+    __shared__ float2 s_f[F64 ? WARPS : 1][64]; // P lo, u lo
     __shared__ long long s_id[WARPS][64];
     __shared__ R4 s_fp[WARPS][64];    // far: centred position, vsnd
     __shared__ R4 s_fv[WARPS][64];    // far: velocity (hi), signal-velocity bound b_j
     __shared__ R s_nb[WARPS][64];     // near: signal-velocity bound b_j
     // FP32C near entries for the mark test: position in the item frame as one
-    // float (as the support test has it) and h_j^2 widened by 2e-4
+    // float (as the support test has it) and h_j^2 widened by 2e-4; and the
+    // entry's j index (written to the marked-pair lists)
     __shared__ float4 s_m[F64 ? 1 : WARPS][64];
+    __shared__ int s_jx[F64 ? 1 : WARPS][64];
     const int lane = threadIdx.x & 31;
     const int wid = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
@@ -874,6 +898,7 @@ hydro_kernel(const HydroArgs a) {
             return below((lane < n) ? bound[lane * stride] : (R)0);
         };
         int nhead = 0, nfill = 0, fhead = 0, ffill = 0;
+        int lcount = 0;   // FP32C: marked pairs of this lane's particle so far
         long long kept_n = 0, kept_f = 0;
         R pax = 0, pay = 0, paz = 0, pud = 0, pdf = 0, pgx = 0, pgy = 0, pgz = 0;
         // pair separation and velocity difference of near entry k
@@ -908,7 +933,7 @@ hydro_kernel(const HydroArgs a) {
             vsmx = vs > vsmx ? vs : vsmx;
             const R hj = s_p1[wid][k].w;
             const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
-            if (!(r2 * hmin2 * (R)1.00002 >= (R)1)) msk |= 1u << (k & 31);
+            if (!(r2 * hmin2 >= (R)1.00002)) msk |= 1u << (k & 31);
         };
         // the mark alone (tiles whose signal-velocity terms are skipped).
         // FP32C tests r^2 < max(h_i, h_j)^2 (1 + 2e-4) on the one-float item
@@ -935,7 +960,7 @@ hydro_kernel(const HydroArgs a) {
             const R r2 = dx * dx + dy * dy + dz * dz;
             const R hj = P1.w;
             const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
-            if (!(r2 * hmin2 * (R)1.00002 >= (R)1)) msk |= 1u << (k & 31);
+            if (!(r2 * hmin2 >= (R)1.00002)) msk |= 1u << (k & 31);
         };
         // The remaining terms of a marked pair, hdr_hydro.hpp:349-398
         auto pair = [&](int k) {
@@ -1018,19 +1043,45 @@ hydro_kernel(const HydroArgs a) {
                 n_marked += c;
                 n_slots += 32u * __reduce_max_sync(FULL, c);
             }
-            while (msk) {
-                const int k = __ffs(msk) - 1;
-                msk &= msk - 1;
-                pair(nhead + k);
+            if constexpr (F64) {
+                while (msk) {
+                    const int k = __ffs(msk) - 1;
+                    msk &= msk - 1;
+                    pair(nhead + k);
+                }
+                ax.add(pax);
+                ay.add(pay);
+                az.add(paz);
+                ud.add(pud);
+                df.add(pdf);
+                gx.add(pgx);
+                gy.add(pgy);
+                gz.add(pgz);
+            } else {
+                // append the marked j to the particle's row, self pairs (equal
+                // ids, hdr_hydro.hpp:356) dropped; the tpi lanes of one
+                // particle write consecutive segments (prefix over the lanes)
+                unsigned m = r.act ? msk : 0u;
+                for (unsigned t = m; t; t &= t - 1) {
+                    const int k = __ffs(t) - 1;
+                    if (s_id[wid][nhead + k] == idi) m &= ~(1u << k);
+                }
+                const int c = __popc(m);
+                int incl = c;
+                for (int o = 1; o < tpi; o <<= 1) {
+                    const int v = __shfl_up_sync(FULL, incl, o, tpi);
+                    if (sub >= o) incl += v;
+                }
+                const int tot = __shfl_sync(FULL, incl, tpi - 1, tpi);
+                int pos = lcount + incl - c;
+                int *row = a.df_list + (size_t)ii * a.df_cap;
+                for (; m; m &= m - 1) {
+                    const int k = __ffs(m) - 1;
+                    if (pos < a.df_cap) row[pos] = s_jx[wid][nhead + k];
+                    ++pos;
+                }
+                lcount += tot;
             }
-            ax.add(pax);
-            ay.add(pay);
-            az.add(paz);
-            ud.add(pud);
-            df.add(pdf);
-            gx.add(pgx);
-            gy.add(pgy);
-            gz.add(pgz);
             __syncwarp();
         };
         auto run_far = [&](int n) {
@@ -1094,18 +1145,20 @@ hydro_kernel(const HydroArgs a) {
                     s_f[wid][k] = make_float2(0.0f, 0.0f);
                     s_nb[wid][k] = sv_bound(g2_64.y, dvel(v64.x, v64.y, v64.z, 0.0f, 0.0f, 0.0f));
                 } else {
-                    const float4 vl = a.fj.vlo[j], g1 = a.fj_g1[j], g3 = a.fj_g3[j];
+                    // the signal velocity and the mark only: the pair sums are
+                    // formed in double-float from the lists (hydro_df_lists)
+                    const float4 vl = a.fj.vlo[j];
                     s_p1[wid][k] = Real<F64>::make4((R)(ph.x - cph.x), (R)(ph.y - cph.y), (R)(ph.z - cph.z),
                                                     (R)vh.w);
                     s_p2[wid][k] = Real<F64>::make4((R)(pl.x - cpl.x), (R)(pl.y - cpl.y), (R)(pl.z - cpl.z),
                                                     (R)g2.y);
                     s_v1[wid][k] = Real<F64>::make4((R)vh.x, (R)vh.y, (R)vh.z, (R)ph.w);
                     s_v2[wid][k] = Real<F64>::make4((R)vl.x, (R)vl.y, (R)vl.z, (R)vl.w);
-                    s_c[wid][k] = Real<F64>::make4((R)g1.x, (R)g1.z, (R)g1.w, (R)g2.x);
-                    s_d[wid][k] = Real<F64>::make4((R)g2.z, (R)g2.w, (R)g3.x, (R)g3.z);
-                    s_f[wid][k] = make_float2(g1.y, g3.y);
                     s_nb[wid][k] = sv_bound((R)g2.y, dvel(vh.x, vh.y, vh.z, vl.x, vl.y, vl.z));
-                    if constexpr (!F64) s_m[wid][k] = make_float4(px, py, pz, hj2m);
+                    if constexpr (!F64) {
+                        s_m[wid][k] = make_float4(px, py, pz, hj2m);
+                        s_jx[wid][k] = j;
+                    }
                 }
                 s_id[wid][k] = a.j_id[j];
             }
@@ -1148,21 +1201,30 @@ hydro_kernel(const HydroArgs a) {
         }
         if (nfill > 0) run_near(nfill);
         if (ffill > 0) run_far(ffill);
-        const double sax = seg_sum(ax.value(), tpi), say = seg_sum(ay.value(), tpi);
-        const double saz = seg_sum(az.value(), tpi), sud = seg_sum(ud.value(), tpi);
-        const double sdf = seg_sum(df.value(), tpi), sgx = seg_sum(gx.value(), tpi);
-        const double sgy = seg_sum(gy.value(), tpi), sgz = seg_sum(gz.value(), tpi);
         const double svs = seg_max((double)vsmx, tpi);
-        if (r.act && sub == 0) {
-            a.o_acch[3 * ii + 0] = 0.5 * sax;
-            a.o_acch[3 * ii + 1] = 0.5 * say;
-            a.o_acch[3 * ii + 2] = 0.5 * saz;
-            a.o_accg[3 * ii + 0] = 0.5 * sgx;
-            a.o_accg[3 * ii + 1] = 0.5 * sgy;
-            a.o_accg[3 * ii + 2] = 0.5 * sgz;
-            a.o_udot[ii] = 0.5 * sud;
+        if constexpr (F64) {
+            const double sax = seg_sum(ax.value(), tpi), say = seg_sum(ay.value(), tpi);
+            const double saz = seg_sum(az.value(), tpi), sud = seg_sum(ud.value(), tpi);
+            const double sdf = seg_sum(df.value(), tpi), sgx = seg_sum(gx.value(), tpi);
+            const double sgy = seg_sum(gy.value(), tpi), sgz = seg_sum(gz.value(), tpi);
+            if (r.act && sub == 0) {
+                a.o_acch[3 * ii + 0] = 0.5 * sax;
+                a.o_acch[3 * ii + 1] = 0.5 * say;
+                a.o_acch[3 * ii + 2] = 0.5 * saz;
+                a.o_accg[3 * ii + 0] = 0.5 * sgx;
+                a.o_accg[3 * ii + 1] = 0.5 * sgy;
+                a.o_accg[3 * ii + 2] = 0.5 * sgz;
+                a.o_udot[ii] = 0.5 * sud;
+                a.o_vsmx[ii] = svs;
+                a.o_diffu[ii] = 2.0 * sdf;
+            }
+        } else if (r.act && sub == 0) {
             a.o_vsmx[ii] = svs;
-            a.o_diffu[ii] = 2.0 * sdf;
+            a.df_cnt[ii] = lcount;
+            if (lcount > a.df_cap) {
+                const int e = atomicAdd(a.df_novf, 1);
+                a.df_ovf[e] = make_int2(ii, r.walk);
+            }
         }
         if (a.n_eval_near && lane == 0) {
             atomicAdd(a.n_eval_near, (unsigned long long)kept_n * (unsigned long long)r.ni);
@@ -1178,6 +1240,85 @@ hydro_kernel(const HydroArgs a) {
                 atomicAdd(a.n_mark, (unsigned long long)m);
                 atomicAdd(a.n_mark + 1, (unsigned long long)n_slots);
             }
+        }
+    }
+}
+
+// FP32C hydro, double-float pass over the marked-pair rows: one thread per
+// i-particle (particles in index order, so a warp's particles share most of
+// their neighbours in L1).  Rows that overflowed are left to hydro_df_sweep.
+constexpr int HYDRO_DF_THREADS = 128;
+__global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_lists(const HydroArgs a) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n_i; p += gridDim.x * blockDim.x) {
+        const int c = a.df_cnt[p];
+        if (c > a.df_cap) continue;
+        const HydroDFI I = hydro_df_i(a.fi.phi[p], a.fi.plo[p], a.fi.vhi[p], a.fi.vlo[p], a.fi_g1[p], a.fi_g2[p],
+                                      a.fi_g3[p], a.fi_g4[p]);
+        HydroDFAcc acc = hydro_df_zero();
+        const int *row = a.df_list + (size_t)p * a.df_cap;
+        for (int k = 0; k < c; ++k) {
+            const int j = row[k];
+            hydro_df_pair(I, a.fj.phi[j], a.fj.plo[j], a.fj.vhi[j], a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j],
+                          a.fj_g3[j], a.fj_g4[j], acc);
+        }
+        double h[3], g[3], ud, dif;
+        hydro_df_finish(acc, CEFF1, h, g, &ud, &dif);
+        a.o_acch[3 * p + 0] = h[0];
+        a.o_acch[3 * p + 1] = h[1];
+        a.o_acch[3 * p + 2] = h[2];
+        a.o_accg[3 * p + 0] = g[0];
+        a.o_accg[3 * p + 1] = g[1];
+        a.o_accg[3 * p + 2] = g[2];
+        a.o_udot[p] = ud;
+        a.o_diffu[p] = dif;
+    }
+}
+
+// The same for the particles whose row overflowed: one warp per particle
+// over its walk's whole j-list (pairs beyond both supports add exactly
+// zero), the lanes' double-float sums combined by shuffles.
+__device__ __forceinline__ dfk::df warp_sum_df(dfk::df x) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const dfk::df y = dfk::make(__shfl_xor_sync(FULL, x.h, o), __shfl_xor_sync(FULL, x.l, o));
+        x = dfk::add(x, y);
+    }
+    return x;
+}
+__global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_sweep(const HydroArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int n_ovf = *a.df_novf;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < n_ovf; e += warps) {
+        const int2 ent = a.df_ovf[e];
+        const int p = ent.x, w = ent.y;
+        const int jb = a.j_off[w], je = a.j_off[w + 1];
+        const long long idi = a.i_id[p];
+        const HydroDFI I = hydro_df_i(a.fi.phi[p], a.fi.plo[p], a.fi.vhi[p], a.fi.vlo[p], a.fi_g1[p], a.fi_g2[p],
+                                      a.fi_g3[p], a.fi_g4[p]);
+        HydroDFAcc acc = hydro_df_zero();
+        for (int k = jb + lane; k < je; k += 32) {
+            const int j = a.j_idx ? a.j_idx[k] : k;
+            if (a.j_id[j] == idi) continue;
+            hydro_df_pair(I, a.fj.phi[j], a.fj.plo[j], a.fj.vhi[j], a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j],
+                          a.fj_g3[j], a.fj_g4[j], acc);
+        }
+        acc.ax = warp_sum_df(acc.ax);
+        acc.ay = warp_sum_df(acc.ay);
+        acc.az = warp_sum_df(acc.az);
+        acc.gx = warp_sum_df(acc.gx);
+        acc.gy = warp_sum_df(acc.gy);
+        acc.gz = warp_sum_df(acc.gz);
+        acc.ud = warp_sum_df(acc.ud);
+        acc.dif = warp_sum_df(acc.dif);
+        if (lane == 0) {
+            double h[3], g[3], ud, dif;
+            hydro_df_finish(acc, CEFF1, h, g, &ud, &dif);
+            for (int c = 0; c < 3; ++c) {
+                a.o_acch[3 * p + c] = h[c];
+                a.o_accg[3 * p + c] = g[c];
+            }
+            a.o_udot[p] = ud;
+            a.o_diffu[p] = dif;
         }
     }
 }
@@ -1514,22 +1655,28 @@ __global__ inline void make_gravity_records_pe(int n, const dbl4 *pe, float4 *ph
     }
 }
 
+// Hydro records (layout in hydro_df.cuh): from h1 = (1/h, P, P Omega / rho^2,
+// bswt / 2), h2 = (rho, c_s, alpha, alpha_u), h3 = (thrm, eta); 1/h, h^-4 and
+// P Omega / rho^2 also as hi/lo splits of their FP64 values.
 __global__ inline void make_hydro_records(int n, const dbl4 *pm, const dbl4 *vel, const dbl4 *h1, const dbl4 *h2,
                                           const double2 *h3, float4 *phi, float4 *plo, float4 *vhi, float4 *vlo,
-                                          float4 *g1, float4 *g2, float4 *g3) {
+                                          float4 *g1, float4 *g2, float4 *g3, float4 *g4) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const dbl4 p = pm[k], v = vel[k], a = h1[k], b = h2[k];
         const double2 c = h3[k];
         const float2 x = df_split(p.x), y = df_split(p.y), z = df_split(p.z);
         const float2 u = df_split(v.x), w = df_split(v.y), s = df_split(v.z);
-        const float2 P = df_split(a.y), T = df_split(c.x);
+        const float2 P = df_split(a.y), T = df_split(c.x), Q = df_split(a.z);
+        const double h4d = (a.x * a.x) * (a.x * a.x);
+        const float2 H = df_split(a.x), H4 = df_split(h4d);
         phi[k] = make_float4(x.x, y.x, z.x, (float)p.w);
         plo[k] = make_float4(x.y, y.y, z.y, 0.0f);
-        vhi[k] = make_float4(u.x, w.x, s.x, (float)a.x);
-        vlo[k] = make_float4(u.y, w.y, s.y, (float)(a.x * a.x * a.x * a.x));
-        g1[k] = make_float4(P.x, P.y, (float)a.z, (float)a.w);
+        vhi[k] = make_float4(u.x, w.x, s.x, H.x);
+        vlo[k] = make_float4(u.y, w.y, s.y, H4.x);
+        g1[k] = make_float4(P.x, P.y, Q.x, (float)a.w);
         g2[k] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
-        g3[k] = make_float4(T.x, T.y, (float)c.y, 0.0f);
+        g3[k] = make_float4(T.x, T.y, (float)c.y, Q.y);
+        g4[k] = make_float4(H.x, H.y, H4.x, H4.y);
     }
 }
 

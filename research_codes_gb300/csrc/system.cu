@@ -47,7 +47,7 @@ constexpr int MAX_RED = 8;
 constexpr long long MAX_POOL_CHUNKS = 0x7fffffffLL / sphtree::LIST_CHUNK;
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_POOLMAX, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
+       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_POOLMAX, S_HOVF, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -696,16 +696,12 @@ __global__ void hydro_prep(int n, const double *ksr, const double *pres, const d
                            const double *dens, const double *bswt, const double *vsnd, const double *alph,
                            const double *alphu, const double *uene, const double *eta, dbl4 *h1, dbl4 *h2,
                            double2 *h3, bool f32) {
+    (void)f32;
     GRID_STRIDE(p, n) {
-        double hinv, presc;
-        if (f32) {   // FP32 pair records: 1/h and P Omega / rho^2 in FP32 arithmetic
-            const float d = (float)dens[p];
-            hinv = (double)(1.0f / (float)ksr[p]);
-            presc = (double)((float)pres[p] * (float)grdh[p] / (d * d));
-        } else {
-            hinv = 1.0 / ksr[p];
-            presc = pres[p] * grdh[p] / (dens[p] * dens[p]);
-        }
+        // FP64 in both precisions: the FP32C records carry 1/h, h^-4 and
+        // P Omega / rho^2 as double-float splits for the cancelling sums
+        const double hinv = 1.0 / ksr[p];
+        const double presc = pres[p] * grdh[p] / (dens[p] * dens[p]);
         h1[p] = make_dbl4(hinv, pres[p], presc, 0.5 * bswt[p]);
         h2[p] = make_dbl4(dens[p], vsnd[p], alph[p], alphu[p]);
         h3[p] = make_double2(fmax(uene[p] - 0.0, 0.0), eta[p]);
@@ -934,7 +930,11 @@ struct sph_system {
     DevBuf<double> neps2;
     DevBuf<float4> flo, fhi, fmom, ptest;
     // FP32C double-float records (particles, hydro fields, tree monopoles)
-    DevBuf<float4> f_phi, f_plo, f_vhi, f_vlo, f_g1, f_g2, f_g3, f_shi, f_slo;
+    DevBuf<float4> f_phi, f_plo, f_vhi, f_vlo, f_g1, f_g2, f_g3, f_g4, f_shi, f_slo;
+    // FP32C hydro: per particle the j indices of its marked pairs
+    // (HYDRO_LIST_CAP per row), their number, and the rows that overflowed
+    DevBuf<int> hl_list, hl_cnt;
+    DevBuf<int2> hl_ovf;
     // re-walk index list (particles still iterating) and its per-walk segments
     DevBuf<int> uflag, uscan, ulist, a_sfirst, a_scount;
     // FP64 re-check queue of decision-ambiguous density results
@@ -1041,8 +1041,9 @@ int alloc_all(sph_system *s) {
     e |= s->visit.ensure(n) | s->mom.ensure(nn) | s->neps2.ensure(nn);
     if (s->prm.quadrupole) e |= s->quad.ensure(6 * nn) | s->fq0.ensure(nn) | s->fq1.ensure(nn);
     e |= s->flo.ensure(nn) | s->fhi.ensure(nn) | s->fmom.ensure(nn) | s->ptest.ensure(n);
-    DevBuf<float4> *f1[] = {&s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo, &s->f_g1, &s->f_g2, &s->f_g3};
+    DevBuf<float4> *f1[] = {&s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo, &s->f_g1, &s->f_g2, &s->f_g3, &s->f_g4};
     for (auto *b : f1) e |= b->ensure(n);
+    e |= s->hl_list.ensure(n * sphk::HYDRO_LIST_CAP) | s->hl_cnt.ensure(n) | s->hl_ovf.ensure(n);
     e |= s->f_shi.ensure(nn) | s->f_slo.ensure(nn);
     e |= s->uflag.ensure(n) | s->uscan.ensure(n) | s->ulist.ensure(n) | s->a_sfirst.ensure(n) | s->a_scount.ensure(n);
     s->amb_cap = std::max<int>(1024, s->n / 16);
@@ -1639,7 +1640,8 @@ int hydro_phase(sph_system *s, bool eager) {
     if (ctx->prm.precision == SPH_PREC_FP32C)
         sphk::make_hydro_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->vel[0].p, s->h1.p, s->h2.p,
                                                               s->h3.p, s->f_phi.p, s->f_plo.p, s->f_vhi.p,
-                                                              s->f_vlo.p, s->f_g1.p, s->f_g2.p, s->f_g3.p);
+                                                              s->f_vlo.p, s->f_g1.p, s->f_g2.p, s->f_g3.p,
+                                                              s->f_g4.p);
     int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
     if (r) return r;
     const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
@@ -1669,7 +1671,17 @@ int hydro_phase(sph_system *s, bool eager) {
     a.j_off = s->loff[1].p; a.j_idx = s->jidx[1].p; a.queue = s->scal.p + S_QUEUE;
     a.o_acch = s->r_acch.p; a.o_accg = s->r_accg.p; a.o_udot = s->r_udot.p; a.o_vsmx = s->r_vsmx.p;
     a.o_diffu = s->r_diffu.p;
-    sphrt::launch_hydro(a, ctx->prm.precision, ctx->grid[1][ctx->prm.precision == SPH_PREC_FP64], st);
+    a.fi_g4 = s->f_g4.p; a.fj_g4 = s->f_g4.p;
+    a.df_list = s->hl_list.p; a.df_cap = sphk::HYDRO_LIST_CAP; a.df_cnt = s->hl_cnt.p;
+    a.df_ovf = s->hl_ovf.p; a.df_novf = s->scal.p + S_HOVF; a.n_i = n;
+    if (f32) {
+        // rows of particles no work item reaches (a failed list build) stay
+        // empty; the overflow queue starts empty
+        CUDA_TRY(cudaMemsetAsync(s->hl_cnt.p, 0, sizeof(int) * (size_t)n, st));
+        CUDA_TRY(cudaMemsetAsync(s->scal.p + S_HOVF, 0, sizeof(int), st));
+    }
+    sphrt::launch_hydro(a, ctx->prm.precision, ctx->grid[1][ctx->prm.precision == SPH_PREC_FP64], st,
+                        ctx->grid_df);
     cudaEventRecord(s->ev[EV_HK_E], st);
     AlphaParams ap{s->prm.alpha_max, s->prm.alpha_min, s->prm.alphu_max, s->prm.alphu_min};
     hydro_writeback<<<grid_for(n), 256, 0, st>>>(
@@ -1894,8 +1906,9 @@ extern "C" int sph_system_destroy(sph_system *s) {
     s->count.release(); s->visit.release(); s->mom.release(); s->quad.release(); s->fq0.release();
     s->fq1.release();
     DevBuf<float4> *f1[] = {&s->flo, &s->fhi, &s->fmom, &s->ptest, &s->f_phi, &s->f_plo, &s->f_vhi, &s->f_vlo,
-                            &s->f_g1, &s->f_g2, &s->f_g3, &s->f_shi, &s->f_slo};
+                            &s->f_g1, &s->f_g2, &s->f_g3, &s->f_g4, &s->f_shi, &s->f_slo};
     for (auto *b : f1) b->release();
+    s->hl_list.release(); s->hl_cnt.release(); s->hl_ovf.release();
     s->uflag.release(); s->uscan.release(); s->ulist.release(); s->a_sfirst.release(); s->a_scount.release();
     s->amb_i.release(); s->amb_w.release(); s->fitems.release(); s->nbr.release(); s->w_csmax.release();
     DevBuf<int> *i1[] = {&s->gflag, &s->groot, &s->gscan, &s->group_node, &s->group_first, &s->group_count,
@@ -2332,21 +2345,31 @@ extern "C" int sph_system_get_stats(sph_system *s, sph_system_stats *o) {
     o->hydro_sv_tiles = lc[L_HTILES];
     o->hydro_pairs_marked = lc[L_HMARK];
     o->hydro_pair_slots = lc[L_HSLOTS];
+    o->hydro_rows_overflowed = sc[S_HOVF];
     o->last_status = s->last_status;
     return SPH_OK;
 }
 
 extern "C" int sph_system_get_lists(sph_system *s, int32_t kind, int32_t *n_walk, int64_t *n_entries,
                                     int32_t *i_first, int32_t *i_count, int64_t *j_off, int32_t *j_idx) {
-    if (!s || kind < 0 || kind > 2 || !n_walk || !n_entries) return SPH_ERR_INVALID_ARGUMENT;
+    if (!s || kind < 0 || kind > 3 || !n_walk || !n_entries) return SPH_ERR_INVALID_ARGUMENT;
     cudaSetDevice(s->ctx->prm.device);
     cudaStream_t st = s->st();
     int nw = 0;
     long long tot = 0;
     CUDA_TRY(cudaMemcpyAsync(&nw, s->walk_num[kind], sizeof(int), cudaMemcpyDeviceToHost, st));
-    const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : L_LIST_G);
-    CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    if (kind < 3) {
+        const int lslot = kind == 0 ? L_LIST_D : (kind == 1 ? L_LIST_H : L_LIST_G);
+        CUDA_TRY(cudaMemcpyAsync(&tot, s->lscal.p + lslot, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    }
     CUDA_TRY(cudaStreamSynchronize(st));
+    if (kind == 3 && nw > 0) {   // the last re-walk: its entries end where its last walk's list ends
+        int last[2] = {0, 0};
+        CUDA_TRY(cudaMemcpyAsync(&last[0], s->loff[3].p + nw - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(&last[1], s->lcnt[3].p + nw - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        tot = (long long)last[0] + last[1];
+    }
     *n_walk = nw;
     *n_entries = tot;
     if (!i_first || !i_count || !j_off || !j_idx) return SPH_OK;

@@ -14,9 +14,11 @@
 //   4. i-groups ("walks"): maximal subtrees with <= n_group particles.
 //   5. Lists: each group's region is first expanded breadth-first into
 //      traversal tasks (subtrees), then one warp per task runs a
-//      warp-cooperative batched-DFS traversal with a shared-memory stack;
-//      two passes (count, then fill at scanned offsets) so list order is
-//      deterministic:
+//      warp-cooperative batched-DFS traversal with a shared-memory stack,
+//      once: it counts the task's entries and appends them, in traversal
+//      order, to 128-entry chunks taken from a pool; after a scan of the
+//      counts, copy_lists moves each task's chunks to its list offset, so
+//      list order is deterministic:
 //        gather    : j with dist(x_j, box_g) <= max_{i in g, unconverged} rs_i
 //        symmetric : j with dist(x_j, box_g) <= max(max_{i in g} h_i, h_j)
 //        gravity   : node accepted as a monopole when

@@ -47,7 +47,8 @@ class SystemStats(ctypes.Structure):
                 ("evals_density_first", _I64), ("evals_density_grad", _I64), ("evals_hydro_near", _I64),
                 ("evals_hydro_far", _I64), ("density_list_passes", _I64),
                 ("density_sweep_passes", _I64), ("hydro_sv_tiles_skipped", _I64), ("hydro_sv_tiles", _I64),
-                ("hydro_pairs_marked", _I64), ("hydro_pair_slots", _I64), ("last_status", _I32)]
+                ("hydro_pairs_marked", _I64), ("hydro_pair_slots", _I64), ("hydro_rows_overflowed", _I64),
+                ("last_status", _I32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -224,7 +225,9 @@ class ParticleSystem:
 
     def lists(self, kind):
         """(i_first, i_count, j_off, j_idx) of the last evaluation; kind 0/1/2 =
-        density / hydro / gravity, in the system's sorted order."""
+        density / hydro / gravity, 3 = the last density re-walk (its groups;
+        it evaluates their still-iterating particles), in the system's sorted
+        order."""
         nw = _I32()
         ne = _I64()
         check(self.lib.sph_system_get_lists(self.handle, kind, ctypes.byref(nw), ctypes.byref(ne),
