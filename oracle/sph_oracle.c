@@ -9,6 +9,7 @@
 #include "sph_oracle.h"
 
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -317,4 +318,303 @@ double oracle_timestep_min(int64_t n, const double *ksr, const double *vsmx,
         if (d < dtc) dtc = d;
     }
     return dtc;
+}
+
+/* sumAcceleration (hdr_sph.hpp:95-97): a = a_h + a_g1 + a_g2 (n x 3). */
+void oracle_sum_acceleration(int64_t n, const double *acch, const double *accg1,
+                             const double *accg2, double *acc) {
+    for (int64_t k = 0; k < 3 * n; ++k) acc[k] = acch[k] + accg1[k] + accg2[k];
+}
+
+/* HelmholtzGas::predict (hdr_hgas.hpp:646-657) with dnuc = 0 (no nuclear
+ * network) and without the Paczynski-Wiita gcor3 channel: in place. */
+void oracle_predict(int64_t n, double dt, double *pos, double *vel, const double *acc,
+                    double *vel2, double *uene, double *uene2, const double *udot,
+                    double *alph, double *alph2, const double *adot,
+                    double *alphu, double *alphu2, const double *adotu) {
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            const int64_t k = 3 * i + c;
+            pos[k] = pos[k] + vel[k] * dt + 0.5 * acc[k] * dt * dt;
+            vel2[k] = vel[k] + 0.5 * acc[k] * dt;
+            vel[k] = vel[k] + acc[k] * dt;
+        }
+        uene2[i] = uene[i] + 0.5 * udot[i] * dt;
+        uene[i] = uene[i] + udot[i] * dt;
+        alph2[i] = alph[i] + 0.5 * adot[i] * dt;
+        alph[i] = alph[i] + adot[i] * dt;
+        alphu2[i] = alphu[i] + 0.5 * adotu[i] * dt;
+        alphu[i] = alphu[i] + adotu[i] * dt;
+    }
+}
+
+/* HelmholtzGas::correct (hdr_hgas.hpp:659-665), dnuc = 0: in place. */
+void oracle_correct(int64_t n, double dt, double *vel, const double *vel2, const double *acc,
+                    double *uene, const double *uene2, const double *udot,
+                    double *alph, const double *alph2, const double *adot,
+                    double *alphu, const double *alphu2, const double *adotu) {
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) vel[3 * i + c] = vel2[3 * i + c] + 0.5 * acc[3 * i + c] * dt;
+        uene[i] = uene2[i] + 0.5 * udot[i] * dt;
+        alph[i] = alph2[i] + 0.5 * adot[i] * dt;
+        alphu[i] = alphu2[i] + 0.5 * adotu[i] * dt;
+    }
+}
+
+/* calcEnergy (main.cpp:199-219) over HelmholtzGas::calcEnergy
+ * (hdr_hgas.hpp:630-634), gcor3 = 0: sum m (v^2/2 + u + pot/2), summed in
+ * index order.  parts[3] (optional) receives the kinetic, thermal and
+ * potential sums. */
+double oracle_energy(int64_t n, const double *mass, const double *vel, const double *uene,
+                     const double *pot, double *parts) {
+    double e = 0.0, ek = 0.0, eu = 0.0, ep = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double *v = vel + 3 * i;
+        const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        e += mass[i] * (0.5 * v2 + uene[i] + 0.5 * pot[i]);
+        ek += mass[i] * 0.5 * v2;
+        eu += mass[i] * uene[i];
+        ep += mass[i] * 0.5 * pot[i];
+    }
+    if (parts) {
+        parts[0] = ek;
+        parts[1] = eu;
+        parts[2] = ep;
+    }
+    return e;
+}
+
+/* calcCenterOfMass (hdr_util.hpp:8-34): mass, centre of mass and its velocity
+ * over the particles of star `star` (all particles when star < 0).
+ * out = {m, x, y, z, vx, vy, vz}. */
+void oracle_center_of_mass(int64_t n, const double *mass, const double *pos, const double *vel,
+                           const int32_t *istar, int32_t star, double *out) {
+    double m = 0.0, x[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0};
+    for (int64_t i = 0; i < n; ++i) {
+        if (star >= 0 && istar[i] != star) continue;
+        m += mass[i];
+        for (int c = 0; c < 3; ++c) {
+            x[c] += mass[i] * pos[3 * i + c];
+            v[c] += mass[i] * vel[3 * i + c];
+        }
+    }
+    const double minv = 1.0 / m;
+    out[0] = m;
+    for (int c = 0; c < 3; ++c) {
+        out[1 + c] = x[c] * minv;
+        out[4 + c] = v[c] * minv;
+    }
+}
+
+/* calcKernelSupportRadiusMaximum (hdr_util.hpp:489-506, FlagBinary 0): the
+ * density-weighted rms distance from star 0's centre of mass,
+ * sqrt(sum rho |x - x_c|^2 / sum rho) over all particles. */
+double oracle_ksrmax(int64_t n, const double *mass, const double *pos, const double *vel,
+                     const int32_t *istar, const double *dens) {
+    double c[7];
+    oracle_center_of_mass(n, mass, pos, vel, istar, 0, c);
+    double r2 = 0.0, dn = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double dx = pos[3 * i] - c[1], dy = pos[3 * i + 1] - c[2], dz = pos[3 * i + 2] - c[3];
+        r2 += dens[i] * (dx * dx + dy * dy + dz * dz);
+        dn += dens[i];
+    }
+    return sqrt(r2 / dn);
+}
+
+/* The global time step of calcTimestep (main.cpp:242-273): from the previous
+ * step dt (RP::Timestep) and the particles' minimum dtc, halve while
+ * dt > dtc (failing at dt <= dt_min, where the reference aborts), or double
+ * when 2 dt <= dtc, 2 dt <= dt_max and the time is a multiple of 2 dt.
+ * Returns the new dt, or a negative value where the reference aborts. */
+double oracle_timestep_pow2(double dt, double dtc, double time, double dt_max, double dt_min) {
+    if (dt > dtc) {
+        while (dt > dtc) {
+            dt *= 0.5;
+            if (dt <= dt_min) return -1.0;
+        }
+    } else if (2.0 * dt <= dtc && 2.0 * dt <= dt_max) {
+        const double dt2 = 2.0 * dt;
+        if (time - (double)(int64_t)(time / dt2) * dt2 == 0.0) dt *= 2.0;
+    }
+    return dt;
+}
+
+/* ---- host tree and theta-criterion gravity lists ------------------------
+ * The reference gets its gravity lists from FDPS's TreeForForceLong walk
+ * (hdr_gravity.hpp:385-402, theta from the run parameters, n_group i-groups,
+ * main.cpp:380-394); FDPS is not part of the reference tree.  This is a
+ * plain octree of the same kind for the CPU arm of the benchmark: particles
+ * sorted by 63-bit Morton key, a node is a run of keys with a common prefix
+ * of 3 bits per level, leaves hold <= n_leaf particles.  Node monopoles are
+ * hdr_gravity.hpp:37-49's (mass, centre of mass, mass-weighted eps^2); a
+ * node is accepted for a group when the squared distance from the group's
+ * bounding box to the node's centre of mass exceeds (node size / theta)^2
+ * (size: the largest side of the node's particle bounding box), otherwise
+ * opened; leaves that are not accepted enter as particles. */
+typedef struct {
+    int64_t first, count;
+    int32_t child0, nchild;   /* children: consecutive node indices */
+    double com[3], mass, eps2, size;
+} otree_node;
+
+typedef struct {
+    otree_node *nodes;
+    int64_t n_nodes, cap;
+    int32_t *kids;            /* scratch for child lists */
+} otree;
+
+static int64_t key_bound(const uint64_t *keys, int64_t lo, int64_t hi, uint64_t v) {
+    while (lo < hi) {         /* first index in [lo, hi) with keys >= v */
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (keys[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+static int64_t otree_push(otree *t) {
+    if (t->n_nodes == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 1024;
+        t->nodes = (otree_node *)realloc(t->nodes, sizeof(otree_node) * (size_t)t->cap);
+    }
+    return t->n_nodes++;
+}
+
+/* node index v covers keys [first, first + count) sharing the key prefix above
+ * bit 3 * (21 - level) */
+static void otree_build(otree *t, int64_t v, const uint64_t *keys, const double *pos, const double *mass,
+                        const double *eps2, int level, int n_leaf) {
+    otree_node nd = t->nodes[v];
+    double m = 0.0, c[3] = {0.0, 0.0, 0.0}, e = 0.0, lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+    for (int64_t i = nd.first; i < nd.first + nd.count; ++i) {
+        m += mass[i];
+        e += mass[i] * eps2[i];
+        for (int k = 0; k < 3; ++k) {
+            const double x = pos[3 * i + k];
+            c[k] += mass[i] * x;
+            if (x < lo[k]) lo[k] = x;
+            if (x > hi[k]) hi[k] = x;
+        }
+    }
+    nd.mass = m;
+    nd.eps2 = e / m;
+    nd.size = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        nd.com[k] = c[k] / m;
+        if (hi[k] - lo[k] > nd.size) nd.size = hi[k] - lo[k];
+    }
+    nd.child0 = -1;
+    nd.nchild = 0;
+    t->nodes[v] = nd;
+    if (nd.count <= n_leaf || level >= 21) return;
+    const int shift = 3 * (20 - level);
+    const uint64_t base = keys[nd.first] >> (shift + 3) << (shift + 3);
+    int64_t starts[9];
+    starts[0] = nd.first;
+    for (int o = 1; o < 8; ++o) starts[o] = key_bound(keys, nd.first, nd.first + nd.count, base | ((uint64_t)o << shift));
+    starts[8] = nd.first + nd.count;
+    int32_t first_child = -1, nk = 0;
+    for (int o = 0; o < 8; ++o) {
+        if (starts[o + 1] == starts[o]) continue;
+        const int64_t u = otree_push(t);
+        t->nodes[u].first = starts[o];
+        t->nodes[u].count = starts[o + 1] - starts[o];
+        if (first_child < 0) first_child = (int32_t)u;
+        ++nk;
+    }
+    t->nodes[v].child0 = first_child;
+    t->nodes[v].nchild = nk;
+    for (int32_t u = first_child; u < first_child + nk; ++u)
+        otree_build(t, u, keys, pos, mass, eps2, level + 1, n_leaf);
+}
+
+/* Walk of group g: appends particle indices to ep (if non-null) and node
+ * indices to sp; returns the counts. */
+static void otree_walk(const otree *t, const double *glo, const double *ghi, double inv_theta2,
+                       int32_t *ep, int64_t *nep, int32_t *sp, int64_t *nsp, int32_t *stack) {
+    int64_t top = 0, ne = 0, ns = 0;
+    stack[top++] = 0;
+    while (top > 0) {
+        const otree_node *nd = &t->nodes[stack[--top]];
+        const int32_t v = (int32_t)(nd - t->nodes);
+        double d2 = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            double d = 0.0;
+            if (nd->com[k] < glo[k]) d = glo[k] - nd->com[k];
+            else if (nd->com[k] > ghi[k]) d = nd->com[k] - ghi[k];
+            d2 += d * d;
+        }
+        if (d2 > nd->size * nd->size * inv_theta2) {
+            if (sp) sp[ns] = v;
+            ++ns;
+        } else if (nd->nchild == 0) {
+            for (int64_t i = nd->first; i < nd->first + nd->count; ++i) {
+                if (ep) ep[ne] = (int32_t)i;
+                ++ne;
+            }
+        } else {
+            for (int32_t u = nd->child0 + nd->nchild - 1; u >= nd->child0; --u) stack[top++] = u;
+        }
+    }
+    *nep = ne;
+    *nsp = ns;
+}
+
+/* keys: sorted 63-bit Morton keys of pos (n x 3, same order); groups
+ * [gfirst[g], gfirst[g] + gcount[g]).  Fills ep_off / sp_off (ng + 1) and,
+ * when ep_idx / sp_idx are non-null, the lists; node_mom (4 per node: x, y,
+ * z, mass) and node_eps2 when non-null.  Returns the node count (call once
+ * with null outputs to size them). */
+int64_t oracle_gravity_lists(int64_t n, const uint64_t *keys, const double *pos, const double *mass,
+                             const double *eps2, int32_t ng, const int64_t *gfirst, const int64_t *gcount,
+                             double theta, int32_t n_leaf, int64_t *ep_off, int64_t *sp_off,
+                             int32_t *ep_idx, int32_t *sp_idx, double *node_mom, double *node_eps2,
+                             int nthreads) {
+    set_threads(nthreads);
+    otree t = {0, 0, 0, 0};
+    const int64_t root = otree_push(&t);
+    t.nodes[root].first = 0;
+    t.nodes[root].count = n;
+    otree_build(&t, root, keys, pos, mass, eps2, 0, n_leaf);
+    const double inv_theta2 = 1.0 / (theta * theta);
+    const int fill = ep_idx != NULL;
+#pragma omp parallel
+    {
+        int32_t *stack = (int32_t *)malloc(sizeof(int32_t) * (size_t)(8 * 22 + 64));
+#pragma omp for schedule(dynamic, 4)
+        for (int32_t g = 0; g < ng; ++g) {
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (int64_t i = gfirst[g]; i < gfirst[g] + gcount[g]; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    if (pos[3 * i + k] < lo[k]) lo[k] = pos[3 * i + k];
+                    if (pos[3 * i + k] > hi[k]) hi[k] = pos[3 * i + k];
+                }
+            int64_t ne, ns;
+            if (fill)
+                otree_walk(&t, lo, hi, inv_theta2, ep_idx + ep_off[g], &ne, sp_idx + sp_off[g], &ns, stack);
+            else {
+                otree_walk(&t, lo, hi, inv_theta2, NULL, &ne, NULL, &ns, stack);
+                ep_off[g + 1] = ne;
+                sp_off[g + 1] = ns;
+            }
+        }
+        free(stack);
+    }
+    if (!fill) {
+        ep_off[0] = sp_off[0] = 0;
+        for (int32_t g = 0; g < ng; ++g) {
+            ep_off[g + 1] += ep_off[g];
+            sp_off[g + 1] += sp_off[g];
+        }
+    }
+    if (node_mom)
+        for (int64_t v = 0; v < t.n_nodes; ++v) {
+            for (int k = 0; k < 3; ++k) node_mom[4 * v + k] = t.nodes[v].com[k];
+            node_mom[4 * v + 3] = t.nodes[v].mass;
+            if (node_eps2) node_eps2[v] = t.nodes[v].eps2;
+        }
+    const int64_t nn = t.n_nodes;
+    free(t.nodes);
+    return nn;
 }

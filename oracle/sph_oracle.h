@@ -81,6 +81,48 @@ double oracle_timestep_min(int64_t n, const double *ksr, const double *vsmx,
                            const double *divv, const double *accg,  /* n*3 */
                            double c_dt, double dt_max);
 
+/* sumAcceleration (hdr_sph.hpp:95-97), n x 3 arrays. */
+void oracle_sum_acceleration(int64_t n, const double *acch, const double *accg1,
+                             const double *accg2, double *acc);
+
+/* Leapfrog predictor and corrector (hdr_hgas.hpp:646-665), in place. */
+void oracle_predict(int64_t n, double dt, double *pos, double *vel, const double *acc,
+                    double *vel2, double *uene, double *uene2, const double *udot,
+                    double *alph, double *alph2, const double *adot,
+                    double *alphu, double *alphu2, const double *adotu);
+void oracle_correct(int64_t n, double dt, double *vel, const double *vel2, const double *acc,
+                    double *uene, const double *uene2, const double *udot,
+                    double *alph, const double *alph2, const double *adot,
+                    double *alphu, const double *alphu2, const double *adotu);
+
+/* Total energy (main.cpp:199-219, hdr_hgas.hpp:630-634); parts: optional
+ * {kinetic, thermal, potential}. */
+double oracle_energy(int64_t n, const double *mass, const double *vel, const double *uene,
+                     const double *pot, double *parts);
+
+/* Centre of mass of star `star` (< 0: all), hdr_util.hpp:8-34;
+ * out = {m, x, y, z, vx, vy, vz}. */
+void oracle_center_of_mass(int64_t n, const double *mass, const double *pos, const double *vel,
+                           const int32_t *istar, int32_t star, double *out);
+
+/* Maximum kernel support radius (hdr_util.hpp:489-506, FlagBinary 0). */
+double oracle_ksrmax(int64_t n, const double *mass, const double *pos, const double *vel,
+                     const int32_t *istar, const double *dens);
+
+/* Power-of-two global time step (main.cpp:242-273); < 0 where the
+ * reference aborts (dt would fall to dt_min). */
+double oracle_timestep_pow2(double dt, double dtc, double time, double dt_max, double dt_min);
+
+/* Host octree over Morton-sorted particles and theta-criterion gravity lists
+ * per i-group (the CPU arm's stand-in for FDPS's TreeForForceLong walk).
+ * Call with null ep_idx/sp_idx/node arrays to get the offsets and the node
+ * count, then again to fill. */
+int64_t oracle_gravity_lists(int64_t n, const uint64_t *keys, const double *pos, const double *mass,
+                             const double *eps2, int32_t ng, const int64_t *gfirst, const int64_t *gcount,
+                             double theta, int32_t n_leaf, int64_t *ep_off, int64_t *sp_off,
+                             int32_t *ep_idx, int32_t *sp_idx, double *node_mom, double *node_eps2,
+                             int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,7 +1,7 @@
 """Generates tests/golden/ic_tools_n40.npz: the reference's own initial-condition
 tools run on a small synthetic star.
 
-    python tests/golden/make_ic_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_ic_golden.py REFERENCE_ROOT
 
 Compiles change_polytropic_scale/main.cpp and two_body_initial_condition/main.cpp
 from the reference tree with g++ (as their Makefiles do, plus -fpermissive for
@@ -88,4 +88,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference root>")
+    main(sys.argv[1])

@@ -152,3 +152,87 @@ def test_reference_avx2_build_agrees(golden):
     for f in ("dens", "ksr", "grdh"):
         assert rel_err(out[f], ref[f]).max() < 1e-9, f
     del a
+
+
+# ---- per-particle step glue ------------------------------------------------------
+GLUE = "glue_n256.npz"
+
+
+@pytest.fixture(scope="module")
+def glue():
+    import os
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", GLUE)))
+
+
+def _glue_oracle(g):
+    """The C restatement on the golden inputs, named like the golden outputs."""
+    i = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    o = {}
+    o["pres"], o["vsnd"] = orc.eos(i["dens"], i["uene"])
+    o["bswt"] = orc.balsara(i["divv"], i["rotv"], o["vsnd"], i["ksr"])
+    o["adot"], _ = orc.alpha_dot(i["divv"], i["alph"], i["alphu"], o["vsnd"], i["ksr"], i["uene"],
+                                 np.zeros_like(i["uene"]), float(g["alpha_max"]), float(g["alpha_min"]), 0.0, 0.0,
+                                 1.0)
+    vsmx = g["ref_vsmx_in"]
+    c_dt, dt_max = float(g["c_dt"]), float(g["dt_max"])
+    o["dt_min"] = orc.timestep_min(i["ksr"], vsmx, i["divv"], i["accg1"] + i["accg2"], c_dt, dt_max)
+    o["energy"] = orc.energy(i["mass"], i["vel"], i["uene"], i["pot"])[0]
+    dt = float(i["dt"])
+    p = orc.predict(dt, i)
+    for k, v in p.items():
+        o["pred_" + k] = v
+    new = dict(p, acc=i["acc"][::-1], udot=i["udot"][::-1], adot=i["adot"][::-1], adotu=i["adotu"])
+    for k, v in orc.correct(dt, new).items():
+        o["corr_" + k] = v
+    o["acc_sum"] = orc.sum_acceleration(i["acch"], i["accg1"], i["accg2"])
+    o["ksrmax"] = orc.ksrmax(i["mass"], i["pos"], i["vel"], i["istar"], i["dens"])
+    return o
+
+
+def test_glue_matches_reference_golden(glue):
+    """EOS, Balsara switch, alpha derivative, time step, energy, predictor,
+    corrector, sumAcceleration and ksrmax of the restatement against the
+    reference's own glue (hdr_hgas.hpp, hdr_sph.hpp, hdr_util.hpp) on the
+    same inputs: identical formulas in FP64, so identical to rounding."""
+    g = glue
+    o = _glue_oracle(g)
+    for k in ("pres", "vsnd", "bswt", "adot", "pred_pos", "pred_vel", "pred_vel2", "pred_uene", "pred_uene2",
+              "pred_alph", "pred_alph2", "pred_alphu", "pred_alphu2", "corr_vel", "corr_uene", "corr_alph",
+              "corr_alphu", "acc_sum"):
+        assert rel_err(o[k], g["ref_" + k], 1e-12).max() <= 1e-14, k
+    # the particles' minimum step and the energy sum in index order
+    assert o["dt_min"] == pytest.approx(min(float(g["dt_max"]), g["ref_dt_particle"].min()), rel=1e-15)
+    e_ref = 0.0
+    for e in g["ref_energy_particle"]:
+        e_ref += e
+    assert o["energy"] == pytest.approx(e_ref, rel=1e-14)
+    assert float(o["ksrmax"]) == pytest.approx(float(g["ref_ksrmax"]), rel=1e-14)
+    # the inputs reach every branch: compression and none, both stars
+    assert (g["in_divv"] == 0).any() and (g["in_divv"] < 0).any() and (g["in_istar"] == 0).any()
+
+
+@pytest.mark.skipif(not orc.ref_glue_available(), reason="oracle/_ref/libsph_ref_glue.so not built here")
+def test_glue_golden_is_the_live_reference(glue):
+    """The stored outputs are what the reference's glue computes now."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "make_glue_golden", os.path.join(os.path.dirname(__file__), "golden", "make_glue_golden.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    live = mk.reference_outputs(mk.inputs())
+    for k, v in live.items():
+        assert np.array_equal(v, glue["ref_" + k]), k
+
+
+def test_timestep_pow2_known_answers():
+    """main.cpp:242-273: halve while dt > dtc, abort at dt_min; double only
+    when 2 dt fits under dtc and dt_max and the time is a multiple of 2 dt."""
+    f = orc.timestep_pow2
+    assert f(10.0, 3.0, 0.0, 10.0, 1e-6) == 2.5          # 10 -> 5 -> 2.5
+    assert f(2.5, 7.0, 5.0, 10.0, 1e-6) == 5.0           # 5 is a multiple of 5
+    assert f(2.5, 7.0, 7.5, 10.0, 1e-6) == 2.5           # 7.5 is not
+    assert f(5.0, 12.0, 10.0, 10.0, 1e-6) == 10.0        # 2 dt == dt_max is allowed
+    assert f(5.0, 12.0, 10.0, 9.0, 1e-6) == 5.0          # 2 dt above dt_max
+    assert f(2.5, 2.5, 0.0, 10.0, 1e-6) == 2.5           # dt == dtc: kept
+    assert f(1.0, 1e-9, 0.0, 10.0, 1e-6) < 0             # would fall to dt_min: the reference aborts
