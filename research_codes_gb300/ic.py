@@ -92,6 +92,20 @@ def unit_lattice_sphere(n_target, rng):
     return p
 
 
+def polytrope_scalings(n_index, M, R, G):
+    """Lane-Emden solution and the scalings of a polytrope of mass M and
+    radius R (any consistent units): (xi, theta, theta', a = R / xi_1,
+    rho_c, K) with rho = rho_c theta^n, r = a xi and P = K rho^(1 + 1/n)
+    (the tool's convert_real_quantities, polytropic_initial_condition/
+    main.cpp:205-227, with the first zero xi_1 located exactly)."""
+    xi, th, dth = lane_emden(n_index)
+    xi1, dth1 = xi[-1], dth[-1]
+    a = R / xi1
+    rho_c = M / (4.0 * math.pi * a ** 3 * (-xi1 * xi1 * dth1))
+    K = 4.0 * math.pi * G * a * a * rho_c ** (1.0 - 1.0 / n_index) / (n_index + 1.0)
+    return xi, th, dth, a, rho_c, K
+
+
 def polytrope(n_part, mass_msun, radius_rsun, n_index, seed=0, eta=1.6):
     """One polytropic star centred on the origin at rest.
 
@@ -100,7 +114,9 @@ def polytrope(n_part, mass_msun, radius_rsun, n_index, seed=0, eta=1.6):
     M, R, K, rho_c and n_index.
     """
     rng = np.random.default_rng(seed)
-    xi, th, dth = lane_emden(n_index)
+    M = mass_msun * units.SOLAR_MASS / units.UNIT_MASS
+    R = radius_rsun * units.SOLAR_RADIUS / units.UNIT_LENGTH
+    xi, th, dth, a, rho_c, K = polytrope_scalings(n_index, M, R, units.G)
     xi1, dth1 = xi[-1], dth[-1]
     # enclosed-mass fraction m(xi)/M = xi^2 theta'(xi) / (xi1^2 theta'(xi1))
     mfrac = (xi * xi * dth) / (xi1 * xi1 * dth1)
@@ -112,12 +128,6 @@ def polytrope(n_part, mass_msun, radius_rsun, n_index, seed=0, eta=1.6):
     f = np.empty(n_part)
     f[order] = (np.arange(n_part) + 0.5) / n_part
     xi_p = np.interp(f, mfrac, xi)
-
-    M = mass_msun * units.SOLAR_MASS / units.UNIT_MASS
-    R = radius_rsun * units.SOLAR_RADIUS / units.UNIT_LENGTH
-    a = R / xi1
-    rho_c = M / (4.0 * math.pi * a ** 3 * (-xi1 * xi1 * dth1))
-    K = 4.0 * math.pi * units.G * a * a * rho_c ** (1.0 - 1.0 / n_index) / (n_index + 1.0)
 
     scale = np.where(r_u > 0, (xi_p * a) / np.maximum(r_u, 1e-300), 0.0)
     pos = p * scale[:, None]

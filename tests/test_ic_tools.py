@@ -117,3 +117,60 @@ def test_rescaled_polytrope_stays_on_its_adiabat():
     assert abs(d["K"] - t["K"]) < 1e-9 * d["K"]
     assert np.allclose(d["pos"], t["pos"], rtol=1e-9, atol=1e-9 * t["R"])
     assert np.allclose(d["uene"], t["uene"], rtol=1e-9)
+
+
+# ---- the polytropic-star generator (polytropic_initial_condition/) -------------
+
+def test_polytrope_pinned_to_the_reference_generator():
+    """ic.polytrope against the reference's own generator, run as shipped
+    (tests/golden/make_polytrope_golden.py; 1 Msun, 1 Rsun, n = 1.5):
+
+    * the Lane-Emden table (lane_emden.hpp:14-53, RK4 from r0 = 1e-4, dr =
+      1e-3): the tool stores theta after each step against the step's start
+      radius, so its row k holds our theta at row k + 1;
+    * the polytropic constant and central density (main.cpp:205-213), which
+      the tool takes at its last table row instead of the exact first zero;
+    * the density theta^n of a particle at the tool's table index;
+    * the radial map from enclosed-mass fraction to Lane-Emden radius: given
+      the tool's own mass profile, our interpolation lands on the tool's
+      binary-search radius to within one table step.
+    Deliberate differences (documented in ic.py): the tool integrates theta
+    rather than rho = theta^n for the mass profile (main.cpp:107-110) and
+    writes u = n P (main.cpp:225); the lattice here has a seeded phase and
+    rotation."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "polytrope_tool_n15.npz")))
+    n = float(g["n_index"])
+    xi, th, dth, a, rho_c, K = ic.polytrope_scalings(n, float(g["mass"]), float(g["radius"]), float(g["G"]))
+    dr, r0 = 1e-3, 1e-4
+    rows = np.round((g["le_r"] - r0) / dr).astype(int)
+    assert np.abs(xi[rows] - g["le_r"]).max() < 1e-6
+    assert np.abs(th[rows + 1] - g["le_theta"]).max() < 1e-6
+    assert np.abs(dth[rows + 1] - g["le_dtheta"]).max() < 1e-6
+    assert int(g["le_rows"]) == len(xi) - 2        # the tool stops one row before the zero
+    # K and rho_c: the tool's ones from its last row, ours from the exact zero
+    r_last, th_last, v_last = g["le_last"]
+    rho_ave = 3.0 * float(g["mass"]) / (4.0 * np.pi * float(g["radius"]) ** 3)
+    rho_c_tool = -rho_ave / (3.0 * v_last / r_last)
+    G, R = float(g["G"]), float(g["radius"])
+    k_tool = 4 * np.pi * G * R * R * rho_c_tool ** ((n - 1) / n) / ((n + 1) * r_last * r_last)
+    assert k_tool == pytest.approx(float(g["k_cgs"]), rel=1e-6)     # printed with 7 digits
+    assert K == pytest.approx(k_tool, rel=2e-3)
+    assert rho_c == pytest.approx(rho_c_tool, rel=2e-3)
+    # density at the tool's table index: rho_c theta(index + 1)^n
+    lane = g["sp_lane"].astype(int)
+    dens = rho_c_tool * th[lane + 1] ** n
+    assert np.allclose(dens, g["real_dens"], rtol=1e-5, atol=6e-7)   # printed with 6 decimals
+    # P = K rho^(1 + 1/n) and c^2 = (1 + 1/n) P / rho; the tool's u = n P
+    pres = k_tool * dens ** (1 + 1 / n)
+    big = g["real_pres"] > 1e7
+    assert np.allclose(g["real_pres"][big], pres[big], rtol=1e-5)
+    assert np.allclose(g["real_vsnd"][big], np.sqrt((1 + 1 / n) * pres / dens)[big], rtol=1e-5)
+    assert np.allclose(g["real_uene"][big], n * pres[big], rtol=1e-5)
+    # radial map with the tool's mass profile (cumulative 4/3 pi dr^3 theta)
+    rt, tt = xi[:-1][: int(g["le_rows"])], th[1:][: int(g["le_rows"])]
+    m = np.empty(len(rt))
+    m[0] = rt[0] ** 3 * tt[0]
+    m[1:] = m[0] + np.cumsum((rt[1:] ** 3 - rt[:-1] ** 3) * tt[1:])
+    m /= m[-1]
+    r_map = np.interp(g["sp_mfrac"], m, rt)
+    assert np.abs(r_map - g["sp_r_pori"]).max() < 2.5 * dr
