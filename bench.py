@@ -112,23 +112,81 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU oracle
-def oracle_rates(samples, nthreads):
+def oracle_rates(samples, nthreads, warm=True):
     """Times the oracle's walk-batched functors on host-built EPI/EPJ samples.
 
     samples: {"density": (epi, epj, i_off, j_off), "hydro": ..., "gravity": ...}
-    Returns {phase: (pairs, seconds)}."""
+    Returns ({phase: (pairs, seconds)}, {phase: functor outputs})."""
     from oracle import oracle as orc
-    out = {}
+    out, res = {}, {}
     for phase, (epi, epj, io, jo) in samples.items():
-        pairs = int(sum((io[w + 1] - io[w]) * (jo[w + 1] - jo[w]) for w in range(len(io) - 1)))
+        pairs = int(np.sum(np.diff(io) * np.diff(jo)))
         fn = {"density": lambda: orc.density_walks(io, jo, epi, epj, eta=ETA, nthreads=nthreads),
               "hydro": lambda: orc.hydro_walks(io, jo, epi, epj, nthreads=nthreads),
               "gravity": lambda: orc.gravity_walks(io, jo, epi, epj, nthreads=nthreads)}[phase]
-        fn()  # warm-up (page-in, thread pool)
+        if warm:
+            fn()  # warm-up (page-in, thread pool)
         t = time.perf_counter()
-        fn()
+        res[phase] = fn()[0]
         out[phase] = (pairs, time.perf_counter() - t)
-    return out
+    return out, res
+
+
+def field_parity(a, b, floor_frac):
+    """Per-particle |a - b| / max(|b|, floor_frac x max|b|) (vector norms for
+    n x 3 fields): max, p99, median and the count above 1e-5."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    if a.ndim > 1:
+        d, s_ = np.linalg.norm(a - b, axis=1), np.linalg.norm(b, axis=1)
+    else:
+        d, s_ = np.abs(a - b), np.abs(b)
+    r = d / np.maximum(s_, max(floor_frac * s_.max(), 1e-300))
+    return {"max": float(r.max()), "p99": float(np.quantile(r, 0.99)), "median": float(np.median(r)),
+            "n_above_1e-5": int((r > 1e-5).sum()), "n": int(len(r)), "floor": floor_frac}
+
+
+def parity_vs_oracle(ps, idx, outs, G):
+    """Every output of the evaluation against the FP64 oracle run on the same
+    walks, lists and inputs (the engine's exported i-groups, j-lists, tree
+    monopoles and per-particle fields: the functor-level comparison)."""
+    n = ps.n
+    f = {k: ps.download(k, sorted_order=True) for k in
+         ("dens", "ksr", "grdh", "divv", "rotv", "np", "acch", "accg1", "accg2", "acc", "udot", "vsmx", "diffu",
+          "pot")}
+    par = {}
+    d, i = outs["density"], idx["density"]
+    one = ~d["itr"].astype(bool)   # particles that finished in the first walk (all of them when converged)
+    for k in ("dens", "ksr", "grdh"):
+        par[k] = field_parity(f[k][i][one], d[k][one], 1e-3)
+    for k in ("divv", "rotv"):
+        par[k] = field_parity(f[k][i][one], d[k][one], 1e-2)
+    par["np_mismatches"] = int((f["np"][i][one].astype(np.int64) != d["np"][one]).sum())
+    par["density_rewalked_not_compared"] = int((~one).sum())
+    h, i = outs["hydro"], idx["hydro"]
+    ref = {"acch": np.zeros((n, 3)), "accg1": np.zeros((n, 3)), "accg2": np.zeros((n, 3)), "pot": np.zeros(n)}
+    ref["acch"][i], ref["accg1"][i] = h["acch"], G * h["accg"]
+    par["acch"] = field_parity(f["acch"][i], h["acch"], 1e-3)
+    par["accg1"] = field_parity(f["accg1"][i], G * h["accg"], 1e-3)
+    par["udot"] = field_parity(f["udot"][i], h["udot"], 1e-3)
+    par["vsmx"] = field_parity(f["vsmx"][i], h["vsmx"], 1e-3)
+    par["diffu"] = field_parity(f["diffu"][i], h["diffu"], 1e-2)
+    g, i = outs["gravity"], idx["gravity"]
+    ref["accg2"][i], ref["pot"][i] = G * g["acc"], G * g["pot"]
+    par["accg2"] = field_parity(f["accg2"][i], G * g["acc"], 1e-3)
+    par["pot"] = field_parity(f["pot"][i], G * g["pot"], 1e-3)
+    a_ref = ref["acch"] + ref["accg1"] + ref["accg2"]
+    par["acc_total"] = field_parity(f["acc"], a_ref, 1e-3)
+    parts = (np.linalg.norm(ref["acch"], axis=1) + np.linalg.norm(ref["accg1"], axis=1)
+             + np.linalg.norm(ref["accg2"], axis=1))
+    r = np.linalg.norm(f["acc"] - a_ref, axis=1) / np.maximum(parts, 1e-300)
+    par["acc_total_over_parts"] = {"max": float(r.max()), "p99": float(np.quantile(r, 0.99)),
+                                   "median": float(np.median(r)), "n_above_1e-5": int((r > 1e-5).sum())}
+    par["note"] = ("FP32C engine vs the FP64 oracle (C restatement of the reference functors, pinned to them by "
+                   "golden vectors) on the engine's own walks, lists, tree monopoles and inputs; per particle "
+                   "|d| / max(|ref|, floor x max|ref|) with the floor given per field (1e-2 for div v, |rot v|, "
+                   "diffu); acc_total = acch + accg1 + accg2, also relative to |acch| + |accg1| + |accg2| "
+                   "(the stars are near hydrostatic equilibrium: the total is a small difference of the parts)")
+    return par
 
 
 def combined_rate(rates, mix):
@@ -139,7 +197,8 @@ def combined_rate(rates, mix):
 
 
 def samples_from_engine(ps, rng, frac):
-    """EPI/EPJ arrays of a random subset of the engine's own walks."""
+    """EPI/EPJ arrays of a random subset of the engine's own walks, and per
+    phase the sorted-order indices of their i-particles."""
     from research_codes_gb300 import abi, units, walks
     n = ps.n
     f = {k: ps.download(k, sorted_order=True) for k in
@@ -147,11 +206,12 @@ def samples_from_engine(ps, rng, frac):
           "eta")}
     f["id"] = f["id"].astype(np.int64)
     f["rs"] = 1.1 * f["ksr"]
-    out = {}
+    out, idx = {}, {}
     for kind, phase in ((0, "density"), (1, "hydro"), (2, "gravity")):
         i_first, i_count, j_off, j_idx = ps.lists(kind)
         nw = len(i_first)
         take = np.sort(rng.choice(nw, min(nw, max(4, int(nw * frac))), replace=False))
+        idx[phase] = np.concatenate([np.arange(i_first[w], i_first[w] + i_count[w]) for w in take])
         items = []
         for w in take:
             gi = np.arange(i_first[w], i_first[w] + i_count[w])
@@ -173,7 +233,7 @@ def samples_from_engine(ps, rng, frac):
                 epj["eps2"][len(pj):] = neps2[sj]
                 items.append((epi, epj))
         out[phase] = walks.concat_walks(items)
-    return out
+    return out, idx
 
 
 # ------------------------------------------------------------------ our arm
@@ -203,18 +263,20 @@ def run_ours(args):
     ps.compute_forces()
     tuned = None
     if not args.no_autotune:
-        # work shaping only: n_group stays the reference's (it defines the
-        # listed pairs of the metric)
+        # n_group (i-group size), the gravity j-tile, the item split (lanes
+        # per i-particle) and the item order, by coordinate descent on the
+        # device time of force evaluations of this state
         from research_codes_gb300 import autotune
         ps.compute_forces()
-        best, table = autotune.autotune(ps, candidates={k: v for k, v in autotune.CANDIDATES.items()
-                                                        if k != "n_group"})
-        tuned = {"chosen": best, "force_ms": [{"params": p, "ms": round(ms, 3)} for p, ms in table[:6]]}
+        best, table = autotune.autotune(ps)
+        tuned = {"chosen": best, "force_ms": [{"params": p, "ms": round(ms, 3)} for p, ms in table[:8]],
+                 "evaluated": len(table)}
         log(f"[bench] autotune: {best}")
     stream = torch.cuda.ExternalStream(ctx.stream())
     for _ in range(args.warmup):
         ps.step(1)
     torch.cuda.synchronize()
+    st0 = ps.stats()   # energy and clock before the timed steps
 
     # ---- timed region: K graph-captured steps, CUDA events on the engine's stream
     clocks = ClockSampler(local)
@@ -234,10 +296,15 @@ def run_ours(args):
     clk = clocks.stop()
     st = ps.stats()
     pairs = {"density": st["pairs_density"], "hydro": st["pairs_hydro"], "gravity": st["pairs_gravity"]}
+    # energy drift of the timed steps (FP64 sums of m (v^2/2 + u + pot/2))
+    energy = {"e_start": st0["e_tot"], "e_end": st["e_tot"], "steps": args.steps,
+              "time_start": st0["time"], "time_end": st["time"],
+              "drift_per_step": (st["e_tot"] - st0["e_tot"]) / abs(st0["e_tot"]) / args.steps}
     inter = sum(pairs.values())
     # every rank evolves its own replica: the job's pairs over the slowest rank
-    value, ms = replicas.aggregate_rate(inter, ms, args.steps, device="cuda")
+    rate_listed, ms = replicas.aggregate_rate(inter, ms, args.steps, device="cuda")
     ms_step = ms / args.steps
+    value = ms_step * 1e-3   # s/step, the headline
     log(f"[bench] {ms_step:.2f} ms/step, {inter:.3e} pairs/step, iters {st['density_iterations']}")
 
     # ---- per-kernel durations: CUDA events on the engine's stream around each
@@ -284,16 +351,41 @@ def run_ours(args):
             traffic = tr[dom].get("bytes_per_launch")
     tree_lists = tree_lists_rate()
 
-    line = {"metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
-            "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math (FP32C), f64 state",
-            "data": "synthetic seeded polytropes (ic.config_system)",
-            "config": {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, n_group={args.n_group}, "
-                                   f"theta=0.5, eta={ETA}", "n_particles": n,
-                       "l2": "inputs larger than L2 (particle state + lists ~2 GB per step)",
-                       "pairs_per_step": pairs, "density_walks": st["density_iterations"],
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+    # pairs per step three ways: listed (sum n_i n_j over the walks' lists at
+    # n_group, the reference's work), evaluated by the kernels (list entries
+    # beyond every i-particle's support are dropped before the pair loops),
+    # and useful (inside a support: 4 x the neighbour counts for the density's
+    # three h passes and gradient pass, the marked hydro pairs, every gravity
+    # pair)
+    evaluated = {"density": st["evals_density_first"] + st["evals_density_grad"],
+                 "hydro": st["evals_hydro_near"] + st["evals_hydro_far"], "gravity": st["pairs_gravity"]}
+    useful_d = 4.0 * float(ps.download("np").sum())
+    useful = {"density": useful_d, "hydro": st["hydro_pairs_marked"], "gravity": st["pairs_gravity"]}
+    listed_256 = pairs
+    if ps.params.n_group != 256:
+        # the listed pairs at the reference's n_group = 256 (main.cpp:380,386,394),
+        # from one eager evaluation of the same state outside the timed region
+        g = ps.params.n_group
+        ps.set_params(n_group=256)
+        ps.set_graph(False)
+        ps.compute_forces()
+        s256 = ps.stats()
+        listed_256 = {"density": s256["pairs_density"], "hydro": s256["pairs_hydro"],
+                      "gravity": s256["pairs_gravity"]}
+        ps.set_params(n_group=g)
+        ps.set_graph(True)
+    ips = {k: world * sum(v.values()) / (ms_step * 1e-3) for k, v in
+           (("listed", pairs), ("evaluated", evaluated), ("useful", useful))}
+    line = {"metric": METRIC, "value": value, "unit": "s/step", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pair math (FP32C, double-float hydro sums), "
+                                                          "f64 state",
+            "data": DATA, "config": workload_config(args, n),
+            "interactions_per_s": ips,
+            "pairs_per_step": {"listed": pairs, "listed_at_n_group_256": listed_256, "evaluated": evaluated,
+                               "useful": useful, "n_group": ps.params.n_group},
+            "density_walks": st["density_iterations"],
+            "parallelism": "replicas" if world > 1 else "single GPU",
             "phases_ms": {k: round(v, 4) for k, v in phases.items()},
             "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
@@ -305,7 +397,8 @@ def run_ours(args):
                                  "pairs beyond the kernel support, per_kernel gives the evaluated work",
                          "frac_evaluated": per_kernel[dom]["achieved_evaluated_tflops"] / peak,
                          "per_kernel": per_kernel},
-            "tree_lists": tree_lists, "gpu_launches": None, "clocks": clk, "autotune": tuned}
+            "tree_lists": tree_lists, "gpu_launches": None, "clocks": clk, "autotune": tuned,
+            "energy": energy}
 
     # kernel launches in the timed region: the kernel nodes of the captured
     # step graph (CUB sort/scan kernels compiled into the library included)
@@ -391,8 +484,9 @@ def run_ours(args):
             ste = ps.stats()
             pairs_e += ste["pairs_density"] + ste["pairs_hydro"] + ste["pairs_gravity"]
         el = time.perf_counter() - t
-        line["e2e"] = {"value": pairs_e / el, "unit": "interactions/s", "h2d_bytes_per_step": int(h2d),
+        line["e2e"] = {"value": el / ke, "unit": "s/step", "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * el / ke,
+                       "interactions_per_s": pairs_e / el,
                        "path": "sph_system_upload -> sph_system_compute_forces -> sph_system_download "
                                "(pinned host buffers, converged state)"}
 
@@ -402,11 +496,15 @@ def run_ours(args):
         ps.compute_forces()   # eager evaluation: every list is exported as used
         NODES = ps.nodes()
         rng = np.random.default_rng(1)
-        smp = samples_from_engine(ps, rng, args.cpu_frac)
+        smp, idx = samples_from_engine(ps, rng, args.cpu_frac)
         nthreads = os.cpu_count() or 1
-        rates = oracle_rates(smp, nthreads)
+        rates, outs = oracle_rates(smp, nthreads)
         cpu_rate = combined_rate(rates, {k: float(v) for k, v in pairs.items()})
-        line["cpu_baseline"] = {"value": cpu_rate, "unit": "interactions/s", "cores": nthreads, "kind": "port",
+        cpu_s = sum(float(pairs[p]) / (rates[p][0] / rates[p][1]) for p in pairs)   # this step's pairs
+        if args.cpu_frac >= 1.0:
+            line["parity_vs_oracle"] = parity_vs_oracle(ps, idx, outs, ps.params.G)
+        line["cpu_baseline"] = {"value": cpu_s, "unit": "s/step", "interactions_per_s": cpu_rate,
+                                "cores": nthreads, "kind": "port",
                                 "sample": f"{args.cpu_frac:.1%} of the walks of each phase of this step "
                                           f"({', '.join(f'{k} {v[0]:.2e} pairs in {v[1]:.1f}s' for k, v in rates.items())}); "
                                           "scalar FP64 C restatement of the reference functors, OpenMP over walks; "
@@ -419,91 +517,193 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------------ reference arm
+def host_walks_density(tree, s, groups, rs, active=None):
+    """Gather lists (hdr_density.hpp:389-397; FDPS's Gather search): for each
+    group with iterating particles, every j within the largest search radius
+    of those particles from the group's bounding box.  Returns EPI/EPJ walk
+    arrays and the i-particle indices, in walk order."""
+    from research_codes_gb300 import walks
+    items, idx = [], []
+    for g in groups:
+        gi = g if active is None else g[active[g]]
+        if len(gi) == 0:
+            continue
+        lo, hi = s["pos"][g].min(0), s["pos"][g].max(0)
+        r = rs[gi].max()
+        cand = np.array(tree.query_ball_point(0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo) + r), dtype=np.int64)
+        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
+        items.append((walks.density_epi(gi, s, rs), walks.density_epj(np.sort(cand[(d * d).sum(1) <= r * r]), s)))
+        idx.append(gi)
+    return walks.concat_walks(items), np.concatenate(idx)
+
+
+def host_walks_hydro(tree, s, groups):
+    """Symmetric lists (main.cpp:336-344; FDPS's Symmetry search): every j
+    within max(max_{i in g} h_i, h_j) of the group's bounding box."""
+    from research_codes_gb300 import walks
+    hmax = s["ksr"].max()
+    items = []
+    for g in groups:
+        lo, hi = s["pos"][g].min(0), s["pos"][g].max(0)
+        rg = s["ksr"][g].max()
+        cand = np.array(tree.query_ball_point(0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo) + max(rg, hmax)),
+                        dtype=np.int64)
+        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
+        rj = np.maximum(rg, s["ksr"][cand])
+        items.append((walks.hydro_epi(g, s), walks.hydro_epj(np.sort(cand[(d * d).sum(1) <= rj * rj]), s)))
+    return walks.concat_walks(items)
+
+
+def host_walks_gravity(s, keys, groups, theta, nthreads):
+    """theta-criterion group walk of a host octree (oracle_gravity_lists; the
+    role of FDPS's TreeForForceLong walk, hdr_gravity.hpp:385-402): particle
+    entries as GravityEPJ, accepted nodes' monopoles as GravitySPJ (same
+    layout) after them."""
+    from oracle import oracle as orc
+    from research_codes_gb300 import abi, units, walks
+    eps2 = (s["ksr"] / units.KSRH) ** 2
+    gf = np.array([g[0] for g in groups], np.int64)
+    gc = np.array([len(g) for g in groups], np.int64)
+    ep_off, ep_idx, sp_off, sp_idx, mom, neps2 = orc.gravity_tree_lists(keys, s["pos"], s["mass"], eps2, gf, gc,
+                                                                        theta, 8, nthreads)
+    items = []
+    for k, g in enumerate(groups):
+        e = ep_idx[ep_off[k]:ep_off[k + 1]]
+        sp = sp_idx[sp_off[k]:sp_off[k + 1]]
+        epj = np.zeros(len(e) + len(sp), abi.GravityEPJ)
+        epj["mass"][:len(e)], epj["pos"][:len(e)], epj["eps2"][:len(e)] = s["mass"][e], s["pos"][e], eps2[e]
+        epj["mass"][len(e):], epj["pos"][len(e):], epj["eps2"][len(e):] = mom[sp, 3], mom[sp, :3], neps2[sp]
+        items.append((walks.gravity_epi(g, s), epj))
+    return walks.concat_walks(items)
+
+
+def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, timed=None):
+    """One calcSPHKernel (main.cpp:300-358) on the host: the density with its
+    search-radius re-walks (hdr_density.hpp:372-415), EOS and Balsara switch,
+    tree gravity and the hydro force, every functor the oracle's (OpenMP over
+    walks), every list the host's.  Updates s in place; returns the functor
+    seconds and listed pairs per phase."""
+    from scipy.spatial import cKDTree
+
+    from oracle import oracle as orc
+    from research_codes_gb300 import units
+    tree = cKDTree(s["pos"])
+    n = len(s["mass"])
+    sec = {"density": 0.0, "gravity": 0.0, "hydro": 0.0}
+    pairs = {"density": 0, "gravity": 0, "hydro": 0}
+    walks_d = 0
+    h0 = s["ksr"].copy()
+    rs = 1.1 * h0
+    active = np.ones(n, bool)
+    while active.any():
+        (epi, epj, io, jo), idx = host_walks_density(tree, dict(s, ksr=h0), groups, rs, active)
+        t = time.perf_counter()
+        out, _ = orc.density_walks(io, jo, epi, epj, eta=ETA, nthreads=nthreads)
+        sec["density"] += time.perf_counter() - t
+        pairs["density"] += int(np.sum(np.diff(io) * np.diff(jo)))
+        walks_d += 1
+        done = ~out["itr"].astype(bool)
+        for k in ("dens", "divv", "rotv", "grdh", "ksr"):
+            s[k][idx[done]] = out[k][done]
+        active[idx[done]] = False
+        rs[idx[~done]] *= 1.1
+        if walks_d >= 20:
+            break
+    s["pres"], s["vsnd"] = orc.eos(s["dens"], s["uene"])
+    s["bswt"] = orc.balsara(s["divv"], s["rotv"], s["vsnd"], s["ksr"])
+    epi, epj, io, jo = host_walks_gravity(s, keys, groups, theta, nthreads)
+    t = time.perf_counter()
+    gout, _ = orc.gravity_walks(io, jo, epi, epj, nthreads=nthreads)
+    sec["gravity"] += time.perf_counter() - t
+    pairs["gravity"] = int(np.sum(np.diff(io) * np.diff(jo)))
+    gi = np.concatenate(groups)
+    s["eta"] = np.empty(n)
+    s["eta"][gi] = s["ksr"][gi] ** 2 / units.KSRH ** 2 * s["grdh"][gi] / (3.0 * s["dens"][gi]) * gout["eta"]
+    epi, epj, io, jo = host_walks_hydro(tree, s, groups)
+    t = time.perf_counter()
+    orc.hydro_walks(io, jo, epi, epj, nthreads=nthreads)
+    sec["hydro"] += time.perf_counter() - t
+    pairs["hydro"] = int(np.sum(np.diff(io) * np.diff(jo)))
+    return sec, pairs, walks_d
+
+
 def run_reference(args):
     """The reference's CPU functors for this path, timed on the host cores.
 
-    The reference tree is not available here at run time, so the timed code
-    is the oracle's C restatement of the reference's scalar FP64 functors
-    (kind "port"), pinned bit-for-bit-close to the reference by the golden
-    vectors.  Walks are built on the host (Morton groups of n_group, KD-tree
-    neighbour lists, near-particle + far-cell monopole gravity lists) from the
-    same synthetic initial conditions; FDPS's tree cost is not included."""
+    The reference tree is not available at run time and its compiled
+    functors are x86-only here, so the timed code is the oracle's C
+    restatement of the reference's scalar FP64 functors (kind "port"), pinned
+    to them by the golden vectors.  A step is one force evaluation
+    (calcSPHKernel) of the same configuration: the density with its
+    search-radius re-walks over every i-group, EOS and Balsara switch, theta
+    = 0.5 tree gravity and the hydro force, on lists the host builds (groups
+    of n_group Morton-ordered particles, KD-tree gather and symmetric lists, a
+    host octree walk for gravity).  The state is the configuration's initial
+    conditions after one evaluation (so the timed one starts from converged
+    smoothing lengths, as the GPU arm's steps do).  ms_per_step is the wall
+    time of the functor calls of a step; FDPS's tree and list construction has
+    no counterpart here and is not included."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from scipy.spatial import cKDTree
-
-    from research_codes_gb300 import abi, ic, units, walks
+    from research_codes_gb300 import ic, walks
+    from research_codes_gb300.system import state_from_ic
 
     global ETA
     s, ETA = ic.config_system(args.config, scale=args.scale, seed=args.seed)
+    s = state_from_ic(s)
     n = len(s["mass"])
-    s["id"] = np.arange(n, dtype=np.int64)
-    s["rs"] = 1.1 * s["ksr"]
-    rng = np.random.default_rng(7)
-    groups = walks.make_groups(s["pos"], args.n_group)
-    take = rng.choice(len(groups), max(8, int(len(groups) * args.ref_frac)), replace=False)
-    tree = cKDTree(s["pos"])
-    hmax = s["ksr"].max()
-    # hydro fields from the initial conditions (EOS of the Lane-Emden density)
-    s["dens"] = s["dens"]
-    s["pres"] = s["dens"] * s["uene"] / units.EOS_N
-    s["vsnd"] = np.sqrt(units.GAMMA * s["pres"] / s["dens"])
-    s["grdh"] = np.ones(n)
-    s["bswt"] = np.full(n, 0.1)
-    s["alph"] = np.ones(n)
-    s["alphu"] = np.zeros(n)
-    s["eta"] = np.full(n, 0.05)
-    eps2 = (s["ksr"] / units.KSRH) ** 2
-    d_items, h_items, g_items = [], [], []
-    for g in take:
-        gi = groups[g]
-        lo, hi = s["pos"][gi].min(0), s["pos"][gi].max(0)
-        c, half = 0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo)
-        r = s["rs"][gi].max()
-        cand = np.array(tree.query_ball_point(c, half + r), dtype=np.int64)
-        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
-        d2 = (d * d).sum(1)
-        d_items.append((walks.density_epi(gi, s), walks.density_epj(np.sort(cand[d2 <= r * r]), s)))
-        rh = max(s["ksr"][gi].max(), hmax)
-        cand = np.array(tree.query_ball_point(c, half + rh), dtype=np.int64)
-        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
-        d2 = (d * d).sum(1)
-        rj = np.maximum(s["ksr"][gi].max(), s["ksr"][cand])
-        h_items.append((walks.hydro_epi(gi, s), walks.hydro_epj(np.sort(cand[d2 <= rj * rj]), s)))
-    el, sl = walks.gravity_lists(s["pos"], s["mass"], eps2, [groups[g] for g in take[:max(4, len(take) // 4)]],
-                                 near_factor=2.0, cell_frac=1.0 / 64)
-    for g, e, sp in zip(take, el, sl):
-        epj = np.concatenate([walks.gravity_epj(e, s), sp.view(abi.GravityEPJ)])
-        g_items.append((walks.gravity_epi(groups[g], s), epj))
-    smp = {"density": walks.concat_walks(d_items), "hydro": walks.concat_walks(h_items),
-           "gravity": walks.concat_walks(g_items)}
+    keys = walks.morton_keys(s["pos"])
+    order = np.argsort(keys, kind="stable")
+    keys = keys[order]
+    s = {k: (np.asarray(v)[order].copy() if np.ndim(v) > 0 and len(v) == n else v) for k, v in s.items()}
+    for k in ("dens", "divv", "rotv", "grdh"):
+        s[k] = np.zeros(n)
+    groups = [np.arange(k, min(k + args.n_group, n)) for k in range(0, n, args.n_group)]
     nthreads = os.cpu_count() or 1
-    # pair mix per step of this workload as sampled (scaled to all groups)
-    mix = {}
-    for k, (epi, epj, io, jo) in smp.items():
-        mix[k] = float(sum((io[w + 1] - io[w]) * (jo[w + 1] - jo[w]) for w in range(len(io) - 1)))
-    for _ in range(args.warmup):
-        oracle_rates({"gravity": smp["gravity"]}, nthreads)
-    vals = []
     t0 = time.perf_counter()
+    host_force_evaluation(s, keys, groups, nthreads)   # from the initial guess of h
+    log(f"[bench/ref] set-up evaluation {time.perf_counter() - t0:.1f}s")
+    for _ in range(args.warmup):
+        host_force_evaluation(dict(s), keys, groups, nthreads)
+    secs, rates = [], []
     for _ in range(args.steps):
-        rates = oracle_rates(smp, nthreads)
-        vals.append(combined_rate(rates, mix))
-    el_t = time.perf_counter() - t0
-    value = float(np.mean(vals))
-    line = {"impl": "reference", "metric": "pair-interactions/s per step (density+hydro+gravity), N=1M collision",
-            "value": value, "unit": "interactions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * el_t / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded polytropes (ic.config_system)",
-            "config": {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, n_group={args.n_group}, "
-                                   f"theta=0.5, eta={ETA}", "n_particles": n},
-            "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": nthreads, "kind": "port",
-                             "sample": f"{len(take)} of {len(groups)} walks per step (density, hydro; gravity "
-                                       f"{len(g_items)}), host-built lists; tree construction not included"},
-            "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        st = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
+        sec, pairs, walks_d = host_force_evaluation(st, keys, groups, nthreads)
+        secs.append(sum(sec.values()))
+        rates.append(sum(pairs.values()) / secs[-1])
+    value = float(np.mean(secs))   # s/step
+    ms_step = 1e3 * value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s/step", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+            "config": workload_config(args, n),
+            "interactions_per_s": {"listed": float(sum(pairs.values()) / value)},
+            "pairs_per_step": {"listed": pairs}, "density_walks": walks_d,
+            "phases_s": {k: round(v, 3) for k, v in sec.items()},
+            "cpu_baseline": {"value": value, "unit": "s/step", "cores": nthreads, "kind": "port",
+                             "sample": f"every walk of one force evaluation per step ({len(groups)} groups of "
+                                       f"{args.n_group}; density {pairs['density']:.2e}, hydro "
+                                       f"{pairs['hydro']:.2e}, gravity {pairs['gravity']:.2e} pairs); scalar FP64 C "
+                                       "restatement of the reference functors, OpenMP over walks; host-built "
+                                       "lists (KD-tree gather/symmetric, octree theta = 0.5); list construction "
+                                       "not timed"},
+            "e2e": {"value": value, "unit": "s/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+METRIC = "s/step of the SPH interaction path (density+EOS+gravity+hydro), N=1M collision, FP32C"
+DATA = "synthetic seeded polytropes (ic.config_system)"
+
+
+def workload_config(args, n):
+    """The config dict of both arms' lines (the workload, not the machine)."""
+    big = n >= 500_000
+    return {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, n_group={args.n_group}, "
+                        f"theta=0.5, eta={ETA}", "n_particles": n,
+            "l2": ("inputs larger than L2 (particle state + lists ~2 kB per particle, 2 GB at N=1M)" if big else
+                   "inputs smaller than L2 (a test-size configuration)")}
 
 
 ETA = 1.18

@@ -246,10 +246,12 @@ int sph_calc_gravity_sp(sph_context *ctx,
                         sph_Gravity *force);
 
 /* Allocation-free variant of sph_calc_gravity_ep for callers that cannot
- * allocate device memory: host callbacks and library hooks that may not
- * synchronise the device (an allocation can), runtimes that own all device
- * memory through a fixed arena, loops that cannot afford an allocation's
- * latency or failure in mid-run.  No counterpart in the reference.
+ * allocate device memory: host code that must not synchronise the device (an
+ * allocation can), such as a hook another library calls on its hot path —
+ * not a CUDA stream callback or cudaLaunchHostFunc function, where no CUDA
+ * call is allowed —, runtimes that own all device memory through a fixed
+ * arena, loops that cannot afford an allocation's latency or failure in
+ * mid-run.  No counterpart in the reference.
  *
  * epi, epj and force are DEVICE pointers owned by the caller; the work is
  * queued on `stream` (a cudaStream_t, NULL = default stream) and the call
@@ -257,11 +259,14 @@ int sph_calc_gravity_sp(sph_context *ctx,
  * reference functor.  Scratch lives in one file-scope __device__ array of the
  * library (~2.4 MB, held by every GPU that loads the library until the process
  * exits), which bounds a call to n_i <= SPH_NOALLOC_MAX_I and
- * n_j <= SPH_NOALLOC_MAX_J (larger calls return SPH_ERR_CAPACITY).  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress
- * with that device current): make that first call before any stream capture.
- * All calls share the array; calls that overlap on the GPU race and must be
- * serialised by the caller. */
+ * n_j <= SPH_NOALLOC_MAX_J (larger calls return SPH_ERR_CAPACITY).  Every call
+ * looks up the array's device address with the caller's device current
+ * (cudaGetSymbolAddress); the first call on a device may load the library's
+ * module, which can allocate and synchronise: make it during set-up, before
+ * any stream capture.  A CUDA error pending from the caller's earlier work is
+ * returned as SPH_ERR_CUDA and left for the caller to read.  All calls share
+ * the array; calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 #define SPH_NOALLOC_MAX_I 4096
 #define SPH_NOALLOC_MAX_J 65536
 int sph_calc_gravity_ep_noalloc(const sph_GravityEPI *epi, int32_t n_i,
@@ -351,6 +356,9 @@ typedef struct sph_system_params {
                             signal-velocity terms provably cannot raise any i-particle's
                             maximum skip those terms (results unchanged bit for bit);
                             0: every term is evaluated                                 */
+    int32_t gravity_jtile; /* FP32C gravity: list entries a warp stages in shared
+                            memory and sums per pass, 32 (default) or 64; other values
+                            fail with INVALID_ARGUMENT                                 */
 } sph_system_params;
 
 /* Fields for sph_system_download / sph_system_download_sorted. */

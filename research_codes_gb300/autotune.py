@@ -10,7 +10,9 @@ system's current state (CUDA events of eager evaluations, median of `reps`):
   16, 8 or 4 i-particles, i.e. more lanes (threads) per i-particle, each
   taking a share of the j-tile stream;
 * heavy_classes — how many of the most expensive work-item classes start
-  first before the rest run in walk order.
+  first before the rest run in walk order;
+* gravity_jtile — the j-tile of the gravity kernel: list entries a warp
+  stages in shared memory and sums per pass (32 or 64).
 
 Every candidate evaluates the same state, so the physics results differ only
 through the list composition (pairs beyond the kernel support contribute
@@ -22,7 +24,7 @@ import itertools
 import numpy as np
 
 CANDIDATES = {"n_group": (64, 128, 256, 512), "item_split_nj": (2048, 4096, 8192, 1 << 30),
-              "heavy_classes": (0, 1, 2, 4)}
+              "heavy_classes": (0, 1, 2, 4), "gravity_jtile": (32, 64)}
 
 
 def time_forces(ps, reps=3):

@@ -85,6 +85,7 @@ int init_grids(sph_context *ctx) {
     e |= occupancy_grid(sphk::gravity_kernel<false, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[2][0]);
     e |= occupancy_grid(sphk::gravity_kernel<true, PAIR_WARPS>, th, ctx->sm_count, &ctx->grid[2][1]);
     e |= occupancy_grid(sphk::hydro_df_lists, sphk::HYDRO_DF_THREADS, ctx->sm_count, &ctx->grid_df);
+    e |= occupancy_grid(sphk::gravity_kernel<false, PAIR_WARPS, 64>, th, ctx->sm_count, &ctx->grid_g64);
     return e;
 }
 
@@ -114,12 +115,16 @@ void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_
     if (a.n_i <= 0) return;
     const int need = (a.n_i + sphk::HYDRO_DF_THREADS - 1) / sphk::HYDRO_DF_THREADS;
     sphk::hydro_df_lists<<<std::max(1, std::min(need, dfgrid)), sphk::HYDRO_DF_THREADS, 0, s>>>(a);
-    sphk::hydro_df_sweep<<<std::max(1, std::min(need, dfgrid)), sphk::HYDRO_DF_THREADS, 0, s>>>(a);
+    // one block per overflowed particle, up to one per SM and round
+    sphk::hydro_df_sweep<<<std::max(1, std::min(a.n_i, 2 * dfgrid / 5 + 1)), sphk::HYDRO_SWEEP_THREADS, 0, s>>>(a);
 }
 
-void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s) {
+// jtile: entries a warp stages per pass in FP32C (32 or 64; FP64 uses 32).
+void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s, int jtile) {
     if (precision == SPH_PREC_FP64)
         sphk::gravity_kernel<true, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
+    else if (jtile == 64)
+        sphk::gravity_kernel<false, PAIR_WARPS, 64><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
     else
         sphk::gravity_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
 }
@@ -796,7 +801,7 @@ extern "C" int sph_dispatch_gravity(sph_context *ctx, int32_t tag, int32_t n_wal
         a.queue = ctx->d_queue + K_GRAV;
         a.o_acc = ks.o[0].p; a.o_pot = ks.o[1].p; a.o_eta = ks.o[2].p;
         a.s_quad = nullptr; a.f_sq0 = nullptr; a.f_sq1 = nullptr;   // SPJ are monopoles
-        launch_gravity(a, ctx->prm.precision, pair_grid(ctx, K_GRAV, ctx->prm.precision, a.n_items), ctx->stream);
+        launch_gravity(a, ctx->prm.precision, pair_grid(ctx, K_GRAV, ctx->prm.precision, a.n_items), ctx->stream, 32);
     }
     if (ni > 0)
         pack_gravity<<<eltwise_grid(ni), 256, 0, ctx->stream>>>(ni, ks.o[0].p, ks.o[1].p, ks.o[2].p,

@@ -154,6 +154,7 @@ struct sph_context {
     int *h_flags = nullptr;   // pinned copies of the flags
     int grid[3][2] = {{0}};   // persistent grid per kind and precision
     int grid_df = 0;          // resident blocks of the double-float hydro pass
+    int grid_g64 = 0;         // persistent grid of the FP32C gravity kernel with a 64-entry j-tile
     sphrt::KindState kind[3];
     int n_systems = 0;        // live sph_system objects using this context
     char err[512] = {0};
@@ -166,5 +167,5 @@ int cuda_error(sph_context *ctx, cudaError_t e, const char *what);
 int pair_grid(const sph_context *ctx, int kind, int precision, int n_items);
 void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStream_t s);
 void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid);
-void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s);
+void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s, int jtile);
 }  // namespace sphrt

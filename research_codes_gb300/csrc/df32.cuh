@@ -110,6 +110,20 @@ DF_HD df sqr(df x) {
     e = fma(add(x.h, x.h), x.l, e);
     return fast_two_sum(p, e);
 }
+// Accumulation s += x: TwoSum of the hi parts, the rounding error and x's lo
+// part gathered in s.l without renormalising (an accumulator's lo part only
+// collects small terms; to_double adds it at the end).
+DF_HD void accumulate(df &s, df x) {
+    const df t = two_sum(s.h, x.h);
+    s.l = add(s.l, add(t.l, x.l));
+    s.h = t.h;
+}
+DF_HD void accumulate(df &s, float x) {
+    const df t = two_sum(s.h, x);
+    s.l = add(s.l, t.l);
+    s.h = t.h;
+}
+
 // (ah + al) - (bh + bl) for two double-float splits of FP64 values (the hi
 // difference is not exact in general: different signs or magnitudes).
 DF_HD df diff(float ah, float al, float bh, float bl) {

@@ -44,8 +44,11 @@ struct HydroDFI {
     float eta, dens, vsnd, bswt, alph, alphu, ph, pl, th, tl;
 };
 
+// Sums over j: acceleration a, softening correction g, the pressure part
+// of du/dt without its factor P_i Omega_i / rho_i^2 (ud: sum ka w), the
+// viscous part (uv: sum ka visc, FP32 terms) and diffu (dif).
 struct HydroDFAcc {
-    dfk::df ax, ay, az, gx, gy, gz, ud, dif;
+    dfk::df ax, ay, az, gx, gy, gz, ud, uv, dif;
 };
 
 DF_HD HydroDFI hydro_df_i(float4 phi, float4 plo, float4 vhi, float4 vlo, float4 g1, float4 g2, float4 g3,
@@ -65,7 +68,7 @@ DF_HD HydroDFI hydro_df_i(float4 phi, float4 plo, float4 vhi, float4 vlo, float4
 
 DF_HD HydroDFAcc hydro_df_zero() {
     const dfk::df z = dfk::make(0.0f, 0.0f);
-    return HydroDFAcc{z, z, z, z, z, z, z, z};
+    return HydroDFAcc{z, z, z, z, z, z, z, z, z};
 }
 
 // q u^3 h^-4 with q = r / h, u = max(1 - q, 0): the kernel-gradient factor
@@ -73,7 +76,9 @@ DF_HD HydroDFAcc hydro_df_zero() {
 DF_HD dfk::df hydro_df_grad(dfk::df r, dfk::df hinv, dfk::df h4) {
     using namespace dfk;
     const df q = mul(r, hinv);
-    const df s = two_sum(1.0f, -q.h);
+    // 1 - q.h is exact for q.h in [1/2, 2] and Fast2Sum-exact below; beyond,
+    // u < 0 and the factor is zero
+    const df s = fast_two_sum(1.0f, -q.h);
     const df u = fast_two_sum(s.h, sub(s.l, q.l));
     if (!(u.h > 0.0f)) return make(0.0f, 0.0f);
     return mul(mul(q, mul(sqr(u), u)), h4);
@@ -105,29 +110,31 @@ DF_HD void hydro_df_pair(const HydroDFI &i, float4 phi, float4 plo, float4 vhi, 
     // pressure gradient with the viscous pressure, :378-382
     const df pf = add(add(i.presc, make(g1.z, g3.w)), -0.5f * av * rhi);
     const df fa = mul(mul(pf, ka), ri);
-    acc.ax = add(acc.ax, mul(fa, dx));
-    acc.ay = add(acc.ay, mul(fa, dy));
-    acc.az = add(acc.az, mul(fa, dz));
-    // energy equation with conduction, :384-393
+    accumulate(acc.ax, mul(fa, dx));
+    accumulate(acc.ay, mul(fa, dy));
+    accumulate(acc.az, mul(fa, dz));
+    // energy equation with conduction, :384-393: ka (P_i Omega_i / rho_i^2 w
+    // - visc), the first part summed without its constant factor
     const float du = (i.th - g3.x) + (i.tl - g3.y);
     const float dp = (i.ph - g1.x) + (i.pl - g1.y);
     const float vsu2 = fabsf(dp) * rhi * 2.0f;
     const float vsu = vsu2 > 0.0f ? sqrtf(vsu2) : 0.0f;
     const float visc = rhi * (0.25f * av * wneg - (i.alphu + g2.w) * vsu * du);
-    acc.ud = add(acc.ud, mul(ka, add(mul(i.presc, w), -visc)));
-    acc.dif = add(acc.dif, rhi * du * ka.h * ri.h);
+    accumulate(acc.ud, mul(ka, w));
+    accumulate(acc.uv, ka.h * visc);
+    accumulate(acc.dif, rhi * du * ka.h * ri.h);
     // softening correction, :395-398
     const df dg = mul(mul(add(mul(dwi, i.eta), mul(dwj, g3.z)), ri), phi.w);
-    acc.gx = add(acc.gx, mul(dg, dx));
-    acc.gy = add(acc.gy, mul(dg, dy));
-    acc.gz = add(acc.gz, mul(dg, dz));
+    accumulate(acc.gx, mul(dg, dx));
+    accumulate(acc.gy, mul(dg, dy));
+    accumulate(acc.gz, mul(dg, dz));
 }
 
 // The reference's outputs from the sums: acch = 0.5 sum(-fa dx),
 // accg = 0.5 sum(dg dx), udot = 0.5 sum(...), diffu = 2 sum(...)
 // (hdr_hydro.hpp:401-421), with the factor -5 c1 of every term.
-DF_HD void hydro_df_finish(const HydroDFAcc &a, double c1, double *acch, double *accg, double *udot,
-                           double *diffu) {
+DF_HD void hydro_df_finish(const HydroDFAcc &a, const HydroDFI &i, double c1, double *acch, double *accg,
+                           double *udot, double *diffu) {
     const double k = -5.0 * c1;
     acch[0] = -0.5 * k * dfk::to_double(a.ax);
     acch[1] = -0.5 * k * dfk::to_double(a.ay);
@@ -135,7 +142,7 @@ DF_HD void hydro_df_finish(const HydroDFAcc &a, double c1, double *acch, double 
     accg[0] = 0.5 * k * dfk::to_double(a.gx);
     accg[1] = 0.5 * k * dfk::to_double(a.gy);
     accg[2] = 0.5 * k * dfk::to_double(a.gz);
-    *udot = 0.5 * k * dfk::to_double(a.ud);
+    *udot = 0.5 * k * (dfk::to_double(i.presc) * dfk::to_double(a.ud) - dfk::to_double(a.uv));
     *diffu = 2.0 * k * dfk::to_double(a.dif);
 }
 

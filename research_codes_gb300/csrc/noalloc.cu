@@ -1,12 +1,13 @@
 // noalloc.cu — sph_calc_gravity_ep_noalloc: the gravity functor for callers
 // that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc: code inside a host callback or a
-// library hook that may not synchronise the device (an allocation can
-// synchronise it), embedded runtimes that own all device memory through a
-// fixed arena, and loops that cannot afford an allocation's latency or its
-// failure in mid-run.  Such a caller still has its input and output buffers in device
-// memory.  This entry point works on those buffers and keeps its own scratch
+// Some callers cannot call cudaMalloc: host code that must not synchronise
+// the device (an allocation can synchronise it), such as a hook another
+// library calls on its hot path, embedded runtimes that own all device memory
+// through a fixed arena, and loops that cannot afford an allocation's latency
+// or its failure in mid-run.  (Not CUDA stream callbacks or cudaLaunchHostFunc
+// functions: no CUDA call is allowed there, and this one launches kernels.)
+// Such a caller still has its input and output buffers in device memory.  This entry point works on those buffers and keeps its own scratch
 // (the FP32 double-float records, the per-particle results before they are
 // added to the caller's forces, the work items and the work-queue counter) in
 // one file-scope __device__ array, so it allocates nothing.
@@ -18,9 +19,14 @@
 // work-queue counter itself before the kernels use it.  Calls that overlap on
 // the GPU (different streams, or different host threads on one device) race
 // on the shared array and must be serialised by the caller.
+//
+// The array's device address is looked up on every call, with the caller's
+// device current (cheap once the library's module is loaded on that device;
+// nothing is cached, so a device reset leaves no stale pointer).  The first
+// call on a device may load the module (CUDA loads modules lazily), which can
+// allocate and synchronise: make that first call during set-up, before any
+// stream capture.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/sph_gb300.h"
 #include "pair_kernels.cuh"
@@ -48,10 +54,6 @@ constexpr size_t SCRATCH_BYTES = align256(OFF_QUEUE + sizeof(int));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch per device ordinal, looked up once.
-constexpr int MAX_DEVICES = 64;
-std::mutex g_lock;
-void *g_addr[MAX_DEVICES] = {nullptr};
 
 // Unpacks the caller's AoS inputs into double-float records, writes the work
 // items (chunks of <= 32 i-particles) and the j range, clears the queue.
@@ -103,25 +105,15 @@ __global__ void noalloc_accumulate(int ni, const unsigned char *scr, sph_Gravity
     }
 }
 
+// Device address of g_noalloc_scratch on the current device.
 int scratch_address(unsigned char **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) {
-        cudaGetLastError();
-        return SPH_ERR_NO_DEVICE;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();   // this call's own lookup error
+        return e == cudaErrorNoDevice || e == cudaErrorInvalidDevice ? SPH_ERR_NO_DEVICE : SPH_ERR_CUDA;
     }
-    if (dev < 0 || dev >= MAX_DEVICES) return SPH_ERR_NO_DEVICE;
-    std::lock_guard<std::mutex> guard(g_lock);
-    if (!g_addr[dev]) {
-        // once per device, with that device current
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return SPH_ERR_CUDA;
-        }
-        g_addr[dev] = p;
-    }
-    *out = static_cast<unsigned char *>(g_addr[dev]);
+    *out = static_cast<unsigned char *>(p);
     return SPH_OK;
 }
 
@@ -133,12 +125,15 @@ extern "C" int sph_calc_gravity_ep_noalloc(const sph_GravityEPI *epi, int32_t n_
         return SPH_ERR_INVALID_ARGUMENT;
     if (n_i > MAX_I || n_j > MAX_J) return SPH_ERR_CAPACITY;
     if (n_i == 0) return SPH_OK;
+    // an error left by the caller's earlier work is reported, not consumed
+    if (cudaPeekAtLastError() != cudaSuccess) return SPH_ERR_CUDA;
     unsigned char *scr = nullptr;
     int st = scratch_address(&scr);
     if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int pb = (n_j + n_i + 255) / 256;
     noalloc_prepare<<<pb < 1024 ? pb : 1024, 256, 0, s>>>(epi, n_i, epj, n_j, scr);
+    if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;   // this launch's own error
     sphk::GravityArgs a;
     a.i_pe = nullptr; a.j_pm = nullptr; a.j_eps2 = nullptr; a.s_pm = nullptr; a.s_eps2 = nullptr;
     a.s_quad = nullptr; a.f_sq0 = nullptr; a.f_sq1 = nullptr;
@@ -161,7 +156,7 @@ extern "C" int sph_calc_gravity_ep_noalloc(const sph_GravityEPI *epi, int32_t n_
     a.o_eta = reinterpret_cast<double *>(scr + OFF_ETA);
     const int blocks = (a.n_items + NOALLOC_WARPS - 1) / NOALLOC_WARPS;
     sphk::gravity_kernel<false, NOALLOC_WARPS><<<blocks, NOALLOC_WARPS * 32, 0, s>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return SPH_ERR_CUDA;
     noalloc_accumulate<<<(n_i + 255) / 256, 256, 0, s>>>(n_i, scr, force);
-    const cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? SPH_OK : SPH_ERR_CUDA;
 }

@@ -1262,7 +1262,7 @@ __global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_lists(const 
                           a.fj_g3[j], a.fj_g4[j], acc);
         }
         double h[3], g[3], ud, dif;
-        hydro_df_finish(acc, CEFF1, h, g, &ud, &dif);
+        hydro_df_finish(acc, I, CEFF1, h, g, &ud, &dif);
         a.o_acch[3 * p + 0] = h[0];
         a.o_acch[3 * p + 1] = h[1];
         a.o_acch[3 * p + 2] = h[2];
@@ -1274,9 +1274,12 @@ __global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_lists(const 
     }
 }
 
-// The same for the particles whose row overflowed: one warp per particle
-// over its walk's whole j-list (pairs beyond both supports add exactly
-// zero), the lanes' double-float sums combined by shuffles.
+// The same for the particles whose row overflowed: one block per particle
+// over its walk's whole j-list (such walks have long lists: a warp alone
+// would wait on one load after another), pairs beyond both supports skipped
+// (they add exactly zero), the threads' double-float sums combined by warp
+// shuffles and then across the warps in a fixed order.
+constexpr int HYDRO_SWEEP_THREADS = 512;
 __device__ __forceinline__ dfk::df warp_sum_df(dfk::df x) {
     for (int o = 16; o > 0; o >>= 1) {
         const dfk::df y = dfk::make(__shfl_xor_sync(FULL, x.h, o), __shfl_xor_sync(FULL, x.l, o));
@@ -1284,11 +1287,12 @@ __device__ __forceinline__ dfk::df warp_sum_df(dfk::df x) {
     }
     return x;
 }
-__global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_sweep(const HydroArgs a) {
-    const int lane = threadIdx.x & 31;
+__global__ inline void __launch_bounds__(HYDRO_SWEEP_THREADS) hydro_df_sweep(const HydroArgs a) {
+    constexpr int NW = HYDRO_SWEEP_THREADS / 32;
+    __shared__ dfk::df part[9][NW];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int n_ovf = *a.df_novf;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < n_ovf; e += warps) {
+    for (int e = blockIdx.x; e < n_ovf; e += gridDim.x) {
         const int2 ent = a.df_ovf[e];
         const int p = ent.x, w = ent.y;
         const int jb = a.j_off[w], je = a.j_off[w + 1];
@@ -1296,23 +1300,35 @@ __global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_sweep(const 
         const HydroDFI I = hydro_df_i(a.fi.phi[p], a.fi.plo[p], a.fi.vhi[p], a.fi.vlo[p], a.fi_g1[p], a.fi_g2[p],
                                       a.fi_g3[p], a.fi_g4[p]);
         HydroDFAcc acc = hydro_df_zero();
-        for (int k = jb + lane; k < je; k += 32) {
+        const float hi2 = 1.0f / (I.hinv.h * I.hinv.h);
+        for (int k = jb + threadIdx.x; k < je; k += HYDRO_SWEEP_THREADS) {
             const int j = a.j_idx ? a.j_idx[k] : k;
             if (a.j_id[j] == idi) continue;
-            hydro_df_pair(I, a.fj.phi[j], a.fj.plo[j], a.fj.vhi[j], a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j],
-                          a.fj_g3[j], a.fj_g4[j], acc);
+            // pairs beyond both supports add exactly zero: skip them on an
+            // FP32 distance test with a margin far above its rounding
+            const float4 ph = a.fj.phi[j], pl = a.fj.plo[j], vh = a.fj.vhi[j];
+            const float dx = (I.xh - ph.x) + (I.xl - pl.x), dy = (I.yh - ph.y) + (I.yl - pl.y);
+            const float dz = (I.zh - ph.z) + (I.zl - pl.z);
+            const float hj2 = 1.0f / (vh.w * vh.w);
+            if (dx * dx + dy * dy + dz * dz > fmaxf(hi2, hj2) * 1.001f) continue;
+            hydro_df_pair(I, ph, pl, vh, a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j], a.fj_g3[j], a.fj_g4[j], acc);
         }
-        acc.ax = warp_sum_df(acc.ax);
-        acc.ay = warp_sum_df(acc.ay);
-        acc.az = warp_sum_df(acc.az);
-        acc.gx = warp_sum_df(acc.gx);
-        acc.gy = warp_sum_df(acc.gy);
-        acc.gz = warp_sum_df(acc.gz);
-        acc.ud = warp_sum_df(acc.ud);
-        acc.dif = warp_sum_df(acc.dif);
-        if (lane == 0) {
+        dfk::df *v[9] = {&acc.ax, &acc.ay, &acc.az, &acc.gx, &acc.gy, &acc.gz, &acc.ud, &acc.uv, &acc.dif};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const dfk::df t = warp_sum_df(*v[q]);
+            if (lane == 0) part[q][wid] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                dfk::df t = part[q][0];
+                for (int u = 1; u < NW; ++u) t = dfk::add(t, part[q][u]);
+                *v[q] = t;
+            }
             double h[3], g[3], ud, dif;
-            hydro_df_finish(acc, CEFF1, h, g, &ud, &dif);
+            hydro_df_finish(acc, I, CEFF1, h, g, &ud, &dif);
             for (int c = 0; c < 3; ++c) {
                 a.o_acch[3 * p + c] = h[c];
                 a.o_accg[3 * p + c] = g[c];
@@ -1320,6 +1336,7 @@ __global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_sweep(const 
             a.o_udot[p] = ud;
             a.o_diffu[p] = dif;
         }
+        __syncthreads();   // part[] is rewritten by the next particle
     }
 }
 
@@ -1354,22 +1371,28 @@ struct GravityArgs {
     const float4 *f_sq0, *f_sq1;
 };
 
-template <bool F64, int WARPS>
+// JT: the j-tile, list entries a warp stages in shared memory per pass (32
+// or 64; each lane loads JT / 32 of them one tile ahead) and sums in FP32
+// before folding into the compensated accumulators.
+template <bool F64, int WARPS, int JT = 32>
 __global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_GRAVITY_MIN_BLOCKS)
 gravity_kernel(const GravityArgs a) {
     typedef typename Real<F64>::T R;
     typedef typename Real<F64>::T4 R4;
+    static_assert(JT == 32 || JT == 64, "j-tile of 32 or 64 entries");
+    constexpr int S = JT / 32;        // entries per lane and tile
+    constexpr int QR = 64 * S;        // quadrupole ring: < 32 left + a tile
     // FP64: one record per entry; FP32C: structure of arrays, so that two
     // consecutive entries load as one f32x2 operand
-    __shared__ R4 s_p[F64 ? WARPS : 1][32];   // dx, dy, dz, mass
-    __shared__ R s_e[F64 ? WARPS : 1][32];    // eps2
-    __shared__ __align__(16) float s_x[F64 ? 1 : WARPS][32], s_y[F64 ? 1 : WARPS][32], s_z[F64 ? 1 : WARPS][32],
-        s_m[F64 ? 1 : WARPS][32], s_q[F64 ? 1 : WARPS][32];
+    __shared__ R4 s_p[F64 ? WARPS : 1][JT];   // dx, dy, dz, mass
+    __shared__ R s_e[F64 ? WARPS : 1][JT];    // eps2
+    __shared__ __align__(16) float s_x[F64 ? 1 : WARPS][JT], s_y[F64 ? 1 : WARPS][JT], s_z[F64 ? 1 : WARPS][JT],
+        s_m[F64 ? 1 : WARPS][JT], s_q[F64 ? 1 : WARPS][JT];
     // tree-node entries of the list with their quadrupoles, compacted into a
-    // 64-entry ring (position in the item frame + eps^2; Q xx yy zz xy; Q xz yz)
-    __shared__ R4 q_p[WARPS][64];
-    __shared__ R4 q_a[WARPS][64];
-    __shared__ typename Real<F64>::T2 q_b[WARPS][64];
+    // ring (position in the item frame + eps^2; Q xx yy zz xy; Q xz yz)
+    __shared__ R4 q_p[WARPS][QR];
+    __shared__ R4 q_a[WARPS][QR];
+    __shared__ typename Real<F64>::T2 q_b[WARPS][QR];
     const unsigned lt = lanemask_lt();
     const bool quad = F64 ? (a.s_quad != nullptr) : (a.f_sq0 != nullptr);
     const int lane = threadIdx.x & 31;
@@ -1401,34 +1424,43 @@ gravity_kernel(const GravityArgs a) {
         // j records are loaded one tile ahead of their use, list indices
         // two tiles ahead, so that their latency overlaps the pair loop
         auto jlist = [&](int k) -> int { return a.j_idx ? a.j_idx[jb + k] : jb + k; };
-        float4 nh = make_float4(0, 0, 0, 0), nl = nh;   // next tile (FP32C)
-        dbl4 np64 = make_dbl4(0, 0, 0, 0);              // next tile (FP64)
-        double ne64 = 0.0;
-        auto load = [&](int j) {
+        float4 nh[S], nl[S];   // next tile (FP32C)
+        dbl4 np64[S];          // next tile (FP64)
+        double ne64[S];
+        auto load = [&](int s, int j) {
             if constexpr (F64) {
                 if (j < a.n_split) {
-                    np64 = a.j_pm[j];
-                    ne64 = a.j_eps2[j];
+                    np64[s] = a.j_pm[j];
+                    ne64[s] = a.j_eps2[j];
                 } else {
-                    np64 = a.s_pm[j - a.n_split];
-                    ne64 = a.s_eps2[j - a.n_split];
+                    np64[s] = a.s_pm[j - a.n_split];
+                    ne64[s] = a.s_eps2[j - a.n_split];
                 }
             } else {
                 if (j < a.n_split) {
-                    nh = a.f_phi[j];
-                    nl = a.f_plo[j];
+                    nh[s] = a.f_phi[j];
+                    nl[s] = a.f_plo[j];
                 } else {
-                    nh = a.f_shi[j - a.n_split];
-                    nl = a.f_slo[j - a.n_split];
+                    nh[s] = a.f_shi[j - a.n_split];
+                    nl[s] = a.f_slo[j - a.n_split];
                 }
             }
         };
-        int jn = 0, jnx = 0;   // list index two tiles ahead, of the next tile
-        if (lane < nj) {
-            jnx = jlist(lane);
-            load(jnx);
+        int jn[S], jnx[S];   // list index two tiles ahead, of the next tile
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            nh[s] = make_float4(0, 0, 0, 0);
+            nl[s] = nh[s];
+            np64[s] = make_dbl4(0, 0, 0, 0);
+            ne64[s] = 0.0;
+            jn[s] = 0;
+            jnx[s] = 0;
+            if (32 * s + lane < nj) {
+                jnx[s] = jlist(32 * s + lane);
+                load(s, jnx[s]);
+            }
+            if (JT + 32 * s + lane < nj) jn[s] = jlist(JT + 32 * s + lane);
         }
-        if (32 + lane < nj) jn = jlist(32 + lane);
         int qhead = 0, qfill = 0;
         // quadrupole terms of the node entries in the ring: the potential
         // -(1/2) r.Q.r R^5 and acceleration Q r R^5 - (5/2)(r.Q.r) r R^7 with
@@ -1472,52 +1504,57 @@ gravity_kernel(const GravityArgs a) {
             pt.add(qpt);
             __syncwarp();
         };
-        for (int t = 0; t < nj; t += 32) {
-            const int jk = t + lane;
-            const float4 h = nh, l = nl;
-            const dbl4 p64 = np64;
-            const double e64 = ne64;
-            const int jcur = jnx;
-            if (t + 32 + lane < nj) {
-                jnx = jn;
-                load(jn);
-            }
-            if (t + 64 + lane < nj) jn = jlist(t + 64 + lane);
-            if (quad) {
-                const bool node = jk < nj && jcur >= a.n_split;
-                const unsigned mq = __ballot_sync(FULL, node);
-                if (node) {
-                    const int slot = (qhead + qfill + __popc(mq & lt)) & 63;
-                    const int nd = jcur - a.n_split;
-                    if constexpr (F64) {
-                        const double *q = a.s_quad + 6 * (size_t)nd;
-                        q_p[wid][slot] = Real<F64>::make4(p64.x, p64.y, p64.z, e64);
-                        q_a[wid][slot] = Real<F64>::make4(q[0], q[1], q[2], q[3]);
-                        q_b[wid][slot] = Real<F64>::make2(q[4], q[5]);
-                    } else {
-                        const float4 q0 = a.f_sq0[nd], q1 = a.f_sq1[nd];
-                        q_p[wid][slot] = Real<F64>::make4(df_diff(h.x, l.x, ch.x, cl.x), df_diff(h.y, l.y, ch.y, cl.y),
-                                                          df_diff(h.z, l.z, ch.z, cl.z), l.w);
-                        q_a[wid][slot] = q0;
-                        q_b[wid][slot] = make_float2(q1.x, q1.y);
-                    }
+        for (int t = 0; t < nj; t += JT) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const int jk = t + 32 * s + lane;
+                const float4 h = nh[s], l = nl[s];
+                const dbl4 p64 = np64[s];
+                const double e64 = ne64[s];
+                const int jcur = jnx[s];
+                if (jk + JT < nj) {
+                    jnx[s] = jn[s];
+                    load(s, jn[s]);
                 }
-                qfill += __popc(mq);
-            }
-            if (jk < nj) {
-                if (F64) {
-                    s_p[wid][lane] = Real<F64>::make4(p64.x, p64.y, p64.z, p64.w);
-                    s_e[wid][lane] = e64;
-                } else {
-                    s_x[wid][lane] = df_diff(h.x, l.x, ch.x, cl.x);
-                    s_y[wid][lane] = df_diff(h.y, l.y, ch.y, cl.y);
-                    s_z[wid][lane] = df_diff(h.z, l.z, ch.z, cl.z);
-                    s_m[wid][lane] = h.w;
-                    s_q[wid][lane] = l.w;
+                if (jk + 2 * JT < nj) jn[s] = jlist(jk + 2 * JT);
+                if (quad) {
+                    const bool node = jk < nj && jcur >= a.n_split;
+                    const unsigned mq = __ballot_sync(FULL, node);
+                    if (node) {
+                        const int slot = (qhead + qfill + __popc(mq & lt)) & (QR - 1);
+                        const int nd = jcur - a.n_split;
+                        if constexpr (F64) {
+                            const double *q = a.s_quad + 6 * (size_t)nd;
+                            q_p[wid][slot] = Real<F64>::make4(p64.x, p64.y, p64.z, e64);
+                            q_a[wid][slot] = Real<F64>::make4(q[0], q[1], q[2], q[3]);
+                            q_b[wid][slot] = Real<F64>::make2(q[4], q[5]);
+                        } else {
+                            const float4 q0 = a.f_sq0[nd], q1 = a.f_sq1[nd];
+                            q_p[wid][slot] = Real<F64>::make4(df_diff(h.x, l.x, ch.x, cl.x),
+                                                              df_diff(h.y, l.y, ch.y, cl.y),
+                                                              df_diff(h.z, l.z, ch.z, cl.z), l.w);
+                            q_a[wid][slot] = q0;
+                            q_b[wid][slot] = make_float2(q1.x, q1.y);
+                        }
+                    }
+                    qfill += __popc(mq);
+                }
+                if (jk < nj) {
+                    const int e = 32 * s + lane;
+                    if (F64) {
+                        s_p[wid][e] = Real<F64>::make4(p64.x, p64.y, p64.z, p64.w);
+                        s_e[wid][e] = e64;
+                    } else {
+                        s_x[wid][e] = df_diff(h.x, l.x, ch.x, cl.x);
+                        s_y[wid][e] = df_diff(h.y, l.y, ch.y, cl.y);
+                        s_z[wid][e] = df_diff(h.z, l.z, ch.z, cl.z);
+                        s_m[wid][e] = h.w;
+                        s_q[wid][e] = l.w;
+                    }
                 }
             }
             __syncwarp();
-            const int n = min(32, nj - t);
+            const int n = min(JT, nj - t);
             R pax = 0, pay = 0, paz = 0, ppt = 0, pet = 0;
             auto pair = [&](int k) {
                 R4 pj;
@@ -1542,7 +1579,7 @@ gravity_kernel(const GravityArgs a) {
                 paz -= dz * g;
                 pet += pj.w * rei3;
             };
-            if (!F64 && tpi == 1 && n == 32) {
+            if (!F64 && tpi == 1 && n == JT) {
                 // full tile, FP32C: two entries per instruction (f32x2); the
                 // even and odd entries are summed separately and combined
                 // at the end of the tile.  Sums of -x are kept as sums of x
@@ -1552,7 +1589,7 @@ gravity_kernel(const GravityArgs a) {
                 const f2 NEG = f2_make(-1.0f, -1.0f);
                 f2 AX = f2_make(0.0f, 0.0f), AY = AX, AZ = AX, PT = AX, ET = AX;
 #pragma unroll GRAVITY_UNROLL
-                for (int k = 0; k < 32; k += 2) {
+                for (int k = 0; k < JT; k += 2) {
                     const f2 DX = f2_fma(f2_lds(&s_x[wid][k]), NEG, XI);
                     const f2 DY = f2_fma(f2_lds(&s_y[wid][k]), NEG, YI);
                     const f2 DZ = f2_fma(f2_lds(&s_z[wid][k]), NEG, ZI);
@@ -1577,9 +1614,9 @@ gravity_kernel(const GravityArgs a) {
                 paz = -(R)(az2.x + az2.y);
                 ppt = -(R)(pt2.x + pt2.y);
                 pet = (R)(et2.x + et2.y);
-            } else if (tpi == 1 && n == 32) {
+            } else if (tpi == 1 && n == JT) {
 #pragma unroll 8
-                for (int k = 0; k < 32; ++k) pair(k);
+                for (int k = 0; k < JT; ++k) pair(k);
             } else {
                 for (int k = sub; k < n; k += tpi) pair(k);
             }
@@ -1589,9 +1626,9 @@ gravity_kernel(const GravityArgs a) {
             pt.add(ppt);
             et.add(pet);
             __syncwarp();
-            if (qfill >= 32) {
+            while (qfill >= 32) {
                 run_quad(32);
-                qhead ^= 32;
+                qhead = (qhead + 32) & (QR - 1);
                 qfill -= 32;
             }
         }

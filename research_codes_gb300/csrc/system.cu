@@ -1621,7 +1621,9 @@ int gravity_phase(sph_system *s) {
     a.s_quad = q64 ? s->quad.p : nullptr;
     a.f_sq0 = q32 ? s->fq0.p : nullptr;
     a.f_sq1 = q32 ? s->fq1.p : nullptr;
-    sphrt::launch_gravity(a, ctx->prm.precision, ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st);
+    const int jt = (ctx->prm.precision == SPH_PREC_FP32C && s->prm.gravity_jtile == 64) ? 64 : 32;
+    sphrt::launch_gravity(a, ctx->prm.precision,
+                          jt == 64 ? ctx->grid_g64 : ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st, jt);
     cudaEventRecord(s->ev[EV_GK_E], st);
     gravity_writeback<<<grid_for(n), 256, 0, st>>>(n, s->prm.G, s->r_acc.p, s->r_pot.p, s->r_eta.p, s->ksr[0].p,
                                                    s->grdh.p, s->dens.p, s->accg2.p, s->pot.p, s->eta.p,
@@ -1832,6 +1834,7 @@ extern "C" void sph_system_params_default(sph_system_params *p) {
     p->heavy_classes = SPH_HEAVY_CLASSES;
     p->density_list_slack = NBR_SLACK;
     p->hydro_signal_skip = 1;
+    p->gravity_jtile = 32;
 }
 
 // update_dt halves the step until it is below the limit or at dt_min: that
@@ -1849,7 +1852,8 @@ extern "C" int sph_system_create(sph_context *ctx, int64_t n, const sph_system_p
     s->n = (int)n;
     if (p) s->prm = *p; else sph_system_params_default(&s->prm);
     if (s->prm.n_group < 1 || s->prm.n_leaf < 1 || s->prm.n_leaf > sphtree::MAX_LEAF || !(s->prm.theta > 0.0) ||
-        s->prm.density_list_slack > MAX_NBR_SLACK || !dt_range_ok(s->prm)) {
+        s->prm.density_list_slack > MAX_NBR_SLACK || !dt_range_ok(s->prm) ||
+        (s->prm.gravity_jtile != 32 && s->prm.gravity_jtile != 64)) {
         delete s;
         return SPH_ERR_INVALID_ARGUMENT;
     }
@@ -2103,6 +2107,8 @@ extern "C" int sph_system_set_params(sph_system *s, const sph_system_params *p) 
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "density_list_slack above %g", (double)MAX_NBR_SLACK);
     if (!dt_range_ok(*p))
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "need 0 < dt_min <= dt_max < infinity");
+    if (p->gravity_jtile != 32 && p->gravity_jtile != 64)
+        return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT, "gravity_jtile must be 32 or 64");
     if (p->quadrupole && !s->prm.quadrupole)
         return sphrt::set_error(s->ctx, SPH_ERR_INVALID_ARGUMENT,
                                 "quadrupole needs a system created with it (node moment buffers)");

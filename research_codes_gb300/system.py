@@ -36,7 +36,7 @@ class SystemParams(ctypes.Structure):
                 ("alphu_max", _D), ("alphu_min", _D), ("ksr_max_mode", _I32),
                 ("max_density_iterations", _I32), ("use_graph", _I32), ("quadrupole", _I32),
                 ("item_split_nj", _I32), ("heavy_classes", _I32), ("density_list_slack", ctypes.c_float),
-                ("hydro_signal_skip", _I32)]
+                ("hydro_signal_skip", _I32), ("gravity_jtile", _I32)]
 
 
 class SystemStats(ctypes.Structure):

@@ -26,20 +26,20 @@ class FakeSystem:
 
     def phase_times(self):
         p = self.params
-        return {"force_total": self.cost(p.n_group, p.item_split_nj, p.heavy_classes)}
+        return {"force_total": self.cost(p.n_group, p.item_split_nj, p.heavy_classes, p.gravity_jtile)}
 
 
-START = dict(n_group=256, item_split_nj=1 << 30, heavy_classes=0)
+START = dict(n_group=256, item_split_nj=1 << 30, heavy_classes=0, gravity_jtile=32)
 
 
-def _separable(g, s, h):
-    return 1.0 + abs(g - 128) / 64 + abs(s - 4096) / 4096 + 0.1 * abs(h - 2)
+def _separable(g, s, h, jt):
+    return 1.0 + abs(g - 128) / 64 + abs(s - 4096) / 4096 + 0.1 * abs(h - 2) + (0.05 if jt == 32 else 0.0)
 
 
 def test_coordinate_descent_finds_the_minimum_of_a_separable_cost():
     ps = FakeSystem(_separable, **START)
     best, table = autotune.autotune(ps, reps=3)
-    assert best == dict(n_group=128, item_split_nj=4096, heavy_classes=2)
+    assert best == dict(n_group=128, item_split_nj=4096, heavy_classes=2, gravity_jtile=64)
     # the system keeps the best parameters and its graph setting
     assert {k: getattr(ps.params, k) for k in best} == best
     assert ps.params.use_graph == 1 and ps.graph_calls[-1] is True
@@ -61,8 +61,8 @@ def test_apply_false_restores_the_original_parameters():
 
 def test_result_is_a_coordinate_minimum_of_a_coupled_cost():
     # n_group and item_split_nj interact: the best split depends on the group size
-    def coupled(g, s, h):
-        return 1.0 + ((g / 128.0) * (s / 4096.0) - 1.0) ** 2 + abs(g - 256) / 1024 + 0.01 * h
+    def coupled(g, s, h, jt):
+        return 1.0 + ((g / 128.0) * (s / 4096.0) - 1.0) ** 2 + abs(g - 256) / 1024 + 0.01 * h + 0.001 * jt
     ps = FakeSystem(coupled, **START)
     best, table = autotune.autotune(ps, reps=1, sweeps=3)
     t_best = coupled(*best.values())
@@ -70,10 +70,10 @@ def test_result_is_a_coordinate_minimum_of_a_coupled_cost():
     for k, vals in autotune.CANDIDATES.items():
         for v in vals:
             p = dict(best, **{k: v})
-            assert coupled(p["n_group"], p["item_split_nj"], p["heavy_classes"]) >= t_best
+            assert coupled(p["n_group"], p["item_split_nj"], p["heavy_classes"], p["gravity_jtile"]) >= t_best
 
 
 def test_grid_enumerates_every_combination():
     g = autotune.grid({"a": (1, 2), "b": (3, 4, 5)})
     assert len(g) == 6 and {"a": 2, "b": 5} in g
-    assert len(autotune.grid()) == 4 * 4 * 4
+    assert len(autotune.grid()) == 4 * 4 * 4 * 2

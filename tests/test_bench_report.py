@@ -107,6 +107,7 @@ def test_reference_arm_prints_one_contract_line(tmp_path):
               "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in r, k
     assert r["impl"] == "reference" and r["value"] > 0 and r["warmup"] >= 3
+    assert r["unit"] == "s/step" and r["higher_is_better"] is False
     assert r["cpu_baseline"]["kind"] == "port" and r["cpu_baseline"]["value"] == r["value"]
     assert r["e2e"] == {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert r["config"]["workload"].startswith("c0: single n=1.5 polytrope")

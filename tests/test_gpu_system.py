@@ -144,11 +144,13 @@ def test_hydro_matches_oracle_on_engine_lists(evaluated):
         for k, v in worst.items():
             assert v < 1e-11, (k, v)
         return
-    assert_cancelling_field(f["acch"][gi], ref["acch"], "acch")
-    assert_cancelling_field(f["accg1"][gi], G * ref["accg"], "accg", FLOOR_DERIV)
-    assert_cancelling_field(f["udot"][gi], ref["udot"], "udot")
-    assert_cancelling_field(f["diffu"][gi], ref["diffu"], "diffu", FLOOR_DERIV)
-    assert err(f["vsmx"][gi], ref["vsmx"]) < 1e-5
+    # per particle: the cancelling sums are double-float in FP32C
+    worst = {"acch": err(f["acch"][gi], ref["acch"]), "accg": err(f["accg1"][gi], G * ref["accg"]),
+             "udot": err(f["udot"][gi], ref["udot"]), "vsmx": err(f["vsmx"][gi], ref["vsmx"])}
+    for k, v in worst.items():
+        assert v < 1e-5, (k, v)
+    # diffu keeps FP32 terms (a conduction signal; it cancels as div v does)
+    assert err(f["diffu"][gi], ref["diffu"], FLOOR_DERIV) < 1e-4
 
 
 @pytest.mark.parametrize("prec", ["fp32c", "fp64"])
@@ -523,3 +525,25 @@ def test_graph_replay_recovers_from_list_overflow():
         sys.compute_forces()
         assert sys.stats()["last_status"] == 0
         sys.close()
+
+
+def test_gravity_jtile_64_matches_32():
+    """The autotuner's j-tile choice (entries staged and summed per pass in
+    the FP32C gravity kernel) changes only the FP32 partial sums: both tiles
+    agree to 1e-5 (the 32-entry tile is the one checked against the oracle
+    above), with and without quadrupoles; other tiles are refused."""
+    s = _two_stars(n=6000, seed=12)
+    for quad in (0, 1):
+        out = {}
+        for jt in (32, 64):
+            with functors.Context(precision="fp32c", eta=1.18) as ctx:
+                sys = ParticleSystem(ctx, len(s["mass"]), n_group=64, use_graph=0, quadrupole=quad, gravity_jtile=jt)
+                sys.upload(s)
+                sys.compute_forces()
+                out[jt] = {k: sys.download(k) for k in ("accg2", "pot", "eta")}
+                if jt == 64:
+                    with pytest.raises(abi.SPHError):
+                        sys.set_params(gravity_jtile=48)
+                sys.close()
+        for k in ("accg2", "pot", "eta"):
+            assert err(out[64][k], out[32][k]) < 1e-5, (quad, k)
