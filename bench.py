@@ -112,7 +112,7 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU oracle
-def oracle_rates(samples, nthreads, warm=True):
+def oracle_rates(samples, nthreads, warm=True, ksr_max=0.0):
     """Times the oracle's walk-batched functors on host-built EPI/EPJ samples.
 
     samples: {"density": (epi, epj, i_off, j_off), "hydro": ..., "gravity": ...}
@@ -121,7 +121,8 @@ def oracle_rates(samples, nthreads, warm=True):
     out, res = {}, {}
     for phase, (epi, epj, io, jo) in samples.items():
         pairs = int(np.sum(np.diff(io) * np.diff(jo)))
-        fn = {"density": lambda: orc.density_walks(io, jo, epi, epj, eta=ETA, nthreads=nthreads),
+        fn = {"density": lambda: orc.density_walks(io, jo, epi, epj, eta=ETA, ksr_max=ksr_max,
+                                                       nthreads=nthreads),
               "hydro": lambda: orc.hydro_walks(io, jo, epi, epj, nthreads=nthreads),
               "gravity": lambda: orc.gravity_walks(io, jo, epi, epj, nthreads=nthreads)}[phase]
         if warm:
@@ -196,16 +197,24 @@ def combined_rate(rates, mix):
     return sum(mix.values()) / t
 
 
-def samples_from_engine(ps, rng, frac):
+def samples_from_engine(ps, rng, frac, ksr_first):
     """EPI/EPJ arrays of a random subset of the engine's own walks, and per
-    phase the sorted-order indices of their i-particles."""
+    phase the sorted-order indices of their i-particles.  ksr_first: the
+    smoothing lengths the evaluation started from (upload order), the density
+    functor's first guess and search radius 1.1 ksr (hdr_density.hpp:376-379);
+    the other phases take the evaluation's final fields."""
     from research_codes_gb300 import abi, units, walks
     n = ps.n
     f = {k: ps.download(k, sorted_order=True) for k in
          ("pos", "vel", "mass", "id", "ksr", "pres", "grdh", "dens", "bswt", "vsnd", "alph", "alphu", "uene",
           "eta")}
     f["id"] = f["id"].astype(np.int64)
-    f["rs"] = 1.1 * f["ksr"]
+    # upload index of every sorted slot, through the (unique) particle ids
+    up_id = ps.download("id").astype(np.int64)
+    order = np.argsort(up_id, kind="stable")
+    slot = order[np.searchsorted(up_id[order], f["id"])]
+    fd = dict(f, ksr=np.asarray(ksr_first)[slot])
+    fd["rs"] = 1.1 * fd["ksr"]
     out, idx = {}, {}
     for kind, phase in ((0, "density"), (1, "hydro"), (2, "gravity")):
         i_first, i_count, j_off, j_idx = ps.lists(kind)
@@ -217,7 +226,7 @@ def samples_from_engine(ps, rng, frac):
             gi = np.arange(i_first[w], i_first[w] + i_count[w])
             gj = j_idx[j_off[w]:j_off[w + 1]]
             if phase == "density":
-                items.append((walks.density_epi(gi, f), walks.density_epj(gj, f)))
+                items.append((walks.density_epi(gi, fd), walks.density_epj(gj, fd)))
             elif phase == "hydro":
                 items.append((walks.hydro_epi(gi, f), walks.hydro_epj(gj, f)))
             else:
@@ -319,31 +328,40 @@ def run_ours(args):
     ps.set_graph(True)
     phases = {k: v / args.steps for k, v in acc_t.items()}
     st_k = ps.stats()
-    kern = {"density": phases["density_kernel"], "hydro": phases["hydro_kernel"],
-            "gravity": phases["gravity_kernel"]}
+    # the four pair kernels and the algorithmic work of one launch: pairs x
+    # flop per pair counted from the reference's GPU kernels (density 132 per
+    # listed pair of the first walk, gravity 29; the hydro signal velocity 20
+    # per listed pair, hdr_hydro.hpp:368-372, taken over every j of a list;
+    # the rest of the hydro pair formula, 109 per pair, on the marked pairs
+    # inside a support, which the double-float pass evaluates)
+    kern = {"density": phases["density_kernel"], "gravity": phases["gravity_kernel"],
+            "hydro_signal": phases["hydro_signal"], "hydro_df": phases["hydro_df"]}
     dom = max(kern, key=kern.get)
     peak = ctx.probe_fp32_peak()
-    # the density kernel time is that of the first walk: pair it with that walk's pairs
-    pairs_k = {"density": st_k["pairs_density_first"], "hydro": st_k["pairs_hydro"],
-               "gravity": st_k["pairs_gravity"]}
-    achieved = (pairs_k[dom] * FLOP_PER_PAIR[dom] / (kern[dom] * 1e-3) / 1e12) if pairs_k[dom] else None
+    work = {"density": (st_k["pairs_density_first"], FLOP_PER_PAIR["density"]),
+            "gravity": (st_k["pairs_gravity"], FLOP_PER_PAIR["gravity"]),
+            "hydro_signal": (st_k["pairs_hydro"], FLOP_HYDRO_FAR),
+            "hydro_df": (st_k["hydro_pairs_marked"], FLOP_PER_PAIR["hydro"])}
+    achieved = work[dom][0] * work[dom][1] / (kern[dom] * 1e-3) / 1e12 if work[dom][0] else None
     # work the kernels actually evaluated: the density and hydro kernels drop
     # list entries beyond every i-particle's kernel support before their pair
     # loops (those pairs contribute exactly zero); gravity evaluates all
     useful_d = float(ps.download("np").sum())
     flop_eval = {"density": st_k["evals_density_first"] * FLOP_DENS_PASS + st_k["evals_density_grad"] * FLOP_DENS_GRAD,
-                 "hydro": st_k["evals_hydro_near"] * FLOP_PER_PAIR["hydro"] + st_k["evals_hydro_far"] * FLOP_HYDRO_FAR,
-                 "gravity": pairs_k["gravity"] * FLOP_PER_PAIR["gravity"]}
+                 "gravity": st_k["pairs_gravity"] * FLOP_PER_PAIR["gravity"],
+                 "hydro_signal": (st_k["evals_hydro_near"] + st_k["evals_hydro_far"]) * FLOP_HYDRO_FAR,
+                 "hydro_df": st_k["hydro_pairs_marked"] * FLOP_PER_PAIR["hydro"]}
     per_kernel = {}
     for k in kern:
-        per_kernel[k] = {"ms": round(kern[k], 4), "pairs_listed": int(pairs_k[k]),
-                         "achieved_listed_tflops": pairs_k[k] * FLOP_PER_PAIR[k] / (kern[k] * 1e-3) / 1e12,
+        per_kernel[k] = {"ms": round(kern[k], 4), "pairs": int(work[k][0]), "flop_per_pair": work[k][1],
+                         "achieved_tflops": work[k][0] * work[k][1] / (kern[k] * 1e-3) / 1e12,
                          "achieved_evaluated_tflops": flop_eval[k] / (kern[k] * 1e-3) / 1e12}
     per_kernel["density"]["pair_evaluations"] = {"three_passes": int(st_k["evals_density_first"]),
                                                  "gradient_pass": int(st_k["evals_density_grad"]),
                                                  "useful_per_pass": int(useful_d)}
-    per_kernel["hydro"]["pair_evaluations"] = {"full": int(st_k["evals_hydro_near"]),
-                                               "signal_velocity_only": int(st_k["evals_hydro_far"])}
+    per_kernel["hydro_signal"]["pair_evaluations"] = {"near": int(st_k["evals_hydro_near"]),
+                                                      "signal_velocity_only": int(st_k["evals_hydro_far"])}
+    per_kernel["hydro_df"]["rows_overflowed"] = int(st_k["hydro_rows_overflowed"])
     traffic = None
     if os.path.exists(PROFILE_TRAFFIC):
         tr = json.load(open(PROFILE_TRAFFIC))
@@ -392,9 +410,10 @@ def run_ours(args):
                          "traffic": traffic,
                          "peak_source": "FP32 FMA probe on this GPU (sph_probe_fp32_peak); "
                                         "MEASURED_PEAKS.json holds no FP32 figure",
-                         "work": "achieved = listed pairs (sum n_i*n_j over the walk lists) x flop/pair "
-                                 "(132 density, 109 hydro, 29 gravity) / kernel time; the kernels skip "
-                                 "pairs beyond the kernel support, per_kernel gives the evaluated work",
+                         "work": "achieved = pairs of one launch x flop/pair / its CUDA-event time: listed "
+                                 "pairs (sum n_i*n_j) x 132 density, 29 gravity, 20 hydro signal velocity; "
+                                 "marked pairs x 109 for the hydro double-float pass; per_kernel gives every "
+                                 "kernel and the evaluated work",
                          "frac_evaluated": per_kernel[dom]["achieved_evaluated_tflops"] / peak,
                          "per_kernel": per_kernel},
             "tree_lists": tree_lists, "gpu_launches": None, "clocks": clk, "autotune": tuned,
@@ -402,7 +421,13 @@ def run_ours(args):
 
     # kernel launches in the timed region: the kernel nodes of the captured
     # step graph (CUB sort/scan kernels compiled into the library included)
-    line["gpu_launches"] = args.steps * ps.graph_kernels(step=True)
+    try:
+        line["gpu_launches"] = args.steps * ps.graph_kernels(step=True)
+    except Exception:
+        # the last step re-ran eagerly (its lists outgrew the captured
+        # buffers): the next step captures the graph again
+        ps.step(1)
+        line["gpu_launches"] = args.steps * ps.graph_kernels(step=True)
 
     if rank == 0 and not args.no_fp64:
         # ---- FP64 comparator: parity of one force evaluation of identical
@@ -493,12 +518,14 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu:
         # ---- CPU oracle (port) on the host cores, bounded sample of this workload's walks
         global NODES
+        ksr_first = ps.download("ksr")   # the density iteration's first guess
         ps.compute_forces()   # eager evaluation: every list is exported as used
         NODES = ps.nodes()
         rng = np.random.default_rng(1)
-        smp, idx = samples_from_engine(ps, rng, args.cpu_frac)
+        smp, idx = samples_from_engine(ps, rng, args.cpu_frac, ksr_first)
         nthreads = os.cpu_count() or 1
-        rates, outs = oracle_rates(smp, nthreads)
+        ksr_max = ps.stats()["ksr_max"]   # this evaluation's cap (the star separation for two stars)
+        rates, outs = oracle_rates(smp, nthreads, ksr_max=ksr_max if np.isfinite(ksr_max) else 0.0)
         cpu_rate = combined_rate(rates, {k: float(v) for k, v in pairs.items()})
         cpu_s = sum(float(pairs[p]) / (rates[p][0] / rates[p][1]) for p in pairs)   # this step's pairs
         if args.cpu_frac >= 1.0:
@@ -517,6 +544,26 @@ def run_ours(args):
 
 
 # ------------------------------------------------------------------ reference arm
+def tree_groups(keys, n_group):
+    """i-groups as FDPS forms them: the cells of an octree over the Morton
+    order (keys sorted) holding at most n_group particles, each a contiguous
+    index range; returns a list of index arrays in key order."""
+    keys = np.asarray(keys, np.uint64)
+    out, stack = [], [(0, len(keys), 0)]
+    while stack:
+        a, b, level = stack.pop()
+        if b - a <= n_group or level >= 21:
+            out.append((a, b))
+            continue
+        shift = 3 * (20 - level)
+        base = (int(keys[a]) >> (shift + 3)) << (shift + 3)
+        cuts = [a] + [a + int(np.searchsorted(keys[a:b], np.uint64(base | (o << shift)))) for o in range(1, 8)] + [b]
+        for o in range(7, -1, -1):
+            if cuts[o + 1] > cuts[o]:
+                stack.append((cuts[o], cuts[o + 1], level + 1))
+    return [np.arange(a, b) for a, b in sorted(out)]
+
+
 def host_walks_density(tree, s, groups, rs, active=None):
     """Gather lists (hdr_density.hpp:389-397; FDPS's Gather search): for each
     group with iterating particles, every j within the largest search radius
@@ -577,26 +624,34 @@ def host_walks_gravity(s, keys, groups, theta, nthreads):
     return walks.concat_walks(items)
 
 
-def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, timed=None):
+def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, cache=None):
     """One calcSPHKernel (main.cpp:300-358) on the host: the density with its
     search-radius re-walks (hdr_density.hpp:372-415), EOS and Balsara switch,
     tree gravity and the hydro force, every functor the oracle's (OpenMP over
     walks), every list the host's.  Updates s in place; returns the functor
-    seconds and listed pairs per phase."""
+    seconds and listed pairs per phase and the density walks.  `cache`
+    (a dict) keeps the walk arrays of the first call for later calls on the
+    same state, which then time the functors alone."""
     from scipy.spatial import cKDTree
 
     from oracle import oracle as orc
     from research_codes_gb300 import units
-    tree = cKDTree(s["pos"])
+    reuse = cache is not None and "density" in cache
+    tree = None if reuse else cKDTree(s["pos"])
     n = len(s["mass"])
     sec = {"density": 0.0, "gravity": 0.0, "hydro": 0.0}
     pairs = {"density": 0, "gravity": 0, "hydro": 0}
-    walks_d = 0
     h0 = s["ksr"].copy()
     rs = 1.1 * h0
     active = np.ones(n, bool)
+    walks_d = 0
     while active.any():
-        (epi, epj, io, jo), idx = host_walks_density(tree, dict(s, ksr=h0), groups, rs, active)
+        if reuse:
+            (epi, epj, io, jo), idx = cache["density"][walks_d]
+        else:
+            (epi, epj, io, jo), idx = host_walks_density(tree, dict(s, ksr=h0), groups, rs, active)
+            if cache is not None:
+                cache.setdefault("density_build", []).append(((epi, epj, io, jo), idx))
         t = time.perf_counter()
         out, _ = orc.density_walks(io, jo, epi, epj, eta=ETA, nthreads=nthreads)
         sec["density"] += time.perf_counter() - t
@@ -607,11 +662,18 @@ def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, timed=None):
             s[k][idx[done]] = out[k][done]
         active[idx[done]] = False
         rs[idx[~done]] *= 1.1
-        if walks_d >= 20:
+        if walks_d >= 20 or (reuse and walks_d >= len(cache["density"])):
             break
+    if cache is not None and not reuse:
+        cache["density"] = cache.pop("density_build", [])
     s["pres"], s["vsnd"] = orc.eos(s["dens"], s["uene"])
     s["bswt"] = orc.balsara(s["divv"], s["rotv"], s["vsnd"], s["ksr"])
-    epi, epj, io, jo = host_walks_gravity(s, keys, groups, theta, nthreads)
+    if reuse:
+        epi, epj, io, jo = cache["gravity"]
+    else:
+        epi, epj, io, jo = host_walks_gravity(s, keys, groups, theta, nthreads)
+        if cache is not None:
+            cache["gravity"] = (epi, epj, io, jo)
     t = time.perf_counter()
     gout, _ = orc.gravity_walks(io, jo, epi, epj, nthreads=nthreads)
     sec["gravity"] += time.perf_counter() - t
@@ -619,7 +681,12 @@ def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, timed=None):
     gi = np.concatenate(groups)
     s["eta"] = np.empty(n)
     s["eta"][gi] = s["ksr"][gi] ** 2 / units.KSRH ** 2 * s["grdh"][gi] / (3.0 * s["dens"][gi]) * gout["eta"]
-    epi, epj, io, jo = host_walks_hydro(tree, s, groups)
+    if reuse:
+        epi, epj, io, jo = cache["hydro"]
+    else:
+        epi, epj, io, jo = host_walks_hydro(tree, s, groups)
+        if cache is not None:
+            cache["hydro"] = (epi, epj, io, jo)
     t = time.perf_counter()
     orc.hydro_walks(io, jo, epi, epj, nthreads=nthreads)
     sec["hydro"] += time.perf_counter() - t
@@ -660,19 +727,24 @@ def run_reference(args):
     s = {k: (np.asarray(v)[order].copy() if np.ndim(v) > 0 and len(v) == n else v) for k, v in s.items()}
     for k in ("dens", "divv", "rotv", "grdh"):
         s[k] = np.zeros(n)
-    groups = [np.arange(k, min(k + args.n_group, n)) for k in range(0, n, args.n_group)]
+    groups = tree_groups(keys, args.n_group)
     nthreads = os.cpu_count() or 1
     t0 = time.perf_counter()
     host_force_evaluation(s, keys, groups, nthreads)   # from the initial guess of h
-    log(f"[bench/ref] set-up evaluation {time.perf_counter() - t0:.1f}s")
+    # the evaluation every step repeats: lists built once (not timed), the
+    # functors of every walk timed per step
+    cache = {}
+    host_force_evaluation({k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}, keys, groups,
+                          nthreads, cache=cache)
+    log(f"[bench/ref] set-up evaluations {time.perf_counter() - t0:.1f}s")
     for _ in range(args.warmup):
-        host_force_evaluation(dict(s), keys, groups, nthreads)
-    secs, rates = [], []
+        host_force_evaluation({k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}, keys,
+                              groups, nthreads, cache=cache)
+    secs = []
     for _ in range(args.steps):
         st = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in s.items()}
-        sec, pairs, walks_d = host_force_evaluation(st, keys, groups, nthreads)
+        sec, pairs, walks_d = host_force_evaluation(st, keys, groups, nthreads, cache=cache)
         secs.append(sum(sec.values()))
-        rates.append(sum(pairs.values()) / secs[-1])
     value = float(np.mean(secs))   # s/step
     ms_step = 1e3 * value
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s/step", "n_gpus": world,
@@ -680,11 +752,11 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
             "config": workload_config(args, n),
             "interactions_per_s": {"listed": float(sum(pairs.values()) / value)},
-            "pairs_per_step": {"listed": pairs}, "density_walks": walks_d,
+            "pairs_per_step": {"listed": pairs}, "density_walks": walks_d, "n_group": args.n_group,
             "phases_s": {k: round(v, 3) for k, v in sec.items()},
             "cpu_baseline": {"value": value, "unit": "s/step", "cores": nthreads, "kind": "port",
-                             "sample": f"every walk of one force evaluation per step ({len(groups)} groups of "
-                                       f"{args.n_group}; density {pairs['density']:.2e}, hydro "
+                             "sample": f"every walk of one force evaluation per step ({len(groups)} octree groups "
+                                       f"of <= {args.n_group}; density {pairs['density']:.2e}, hydro "
                                        f"{pairs['hydro']:.2e}, gravity {pairs['gravity']:.2e} pairs); scalar FP64 C "
                                        "restatement of the reference functors, OpenMP over walks; host-built "
                                        "lists (KD-tree gather/symmetric, octree theta = 0.5); list construction "
@@ -693,15 +765,15 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-METRIC = "s/step of the SPH interaction path (density+EOS+gravity+hydro), N=1M collision, FP32C"
+METRIC = "s/step of the SPH interaction path (density+EOS+gravity+hydro), N=1M collision"
 DATA = "synthetic seeded polytropes (ic.config_system)"
 
 
 def workload_config(args, n):
     """The config dict of both arms' lines (the workload, not the machine)."""
     big = n >= 500_000
-    return {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, n_group={args.n_group}, "
-                        f"theta=0.5, eta={ETA}", "n_particles": n,
+    return {"workload": f"{args.config}: {WORKLOADS.get(args.config, args.config)}, N={n}, theta=0.5, eta={ETA}",
+            "n_particles": n,
             "l2": ("inputs larger than L2 (particle state + lists ~2 kB per particle, 2 GB at N=1M)" if big else
                    "inputs smaller than L2 (a test-size configuration)")}
 
@@ -731,7 +803,6 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cpu-frac", type=float, default=1.0)
-    ap.add_argument("--ref-frac", type=float, default=0.03)
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 steps")

@@ -503,8 +503,11 @@ int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t
  * from CUDA events recorded on the context's stream (also inside a captured
  * step): [0] tree + groups, [1] density incl. lists and all walks,
  * [2] density pair kernel of the first walk, [3] gravity lists,
- * [4] gravity pair kernel, [5] hydro prep + lists, [6] hydro pair kernel,
- * [7] the whole force evaluation.  Returns the number of values written,
+ * [4] gravity pair kernel, [5] hydro prep + lists, [6] hydro pair kernels,
+ * [7] the whole force evaluation, [8] and [9] the two parts of [6] (FP32C:
+ * the signal-velocity / marking kernel and the double-float pass over the
+ * marked pairs; FP64: the pair kernel and nothing).  Returns the number of
+ * values written,
  * or minus a status code.  The events belong to eager evaluations
  * (sph_system_compute_forces and non-captured steps). */
 int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);

@@ -69,6 +69,9 @@ def autotune(ps, candidates=None, reps=3, sweeps=2, apply=True):
         if not improved:
             break
     ps.set_params(**(best if apply else original))
+    # one evaluation with the kept parameters sizes the system's list and
+    # task buffers for them before any graph is captured
+    ps.compute_forces()
     ps.set_graph(bool(use_graph))
     table = [(dict(zip(keys, key)), ms) for key, ms in sorted(tried.items(), key=lambda kv: kv[1])]
     return best, table

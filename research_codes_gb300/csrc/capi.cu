@@ -105,13 +105,17 @@ void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStr
 
 // FP32C: the signal-velocity / marking kernel, then the double-float pass
 // over the marked-pair rows and over the overflowed particles (a.df_novf
-// must be zero at launch; dfgrid: blocks for the two double-float kernels).
-void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid) {
+// must be zero at launch; dfgrid: resident blocks of the double-float pass).
+// mid (optional) is recorded between the two.
+void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid,
+                  cudaEvent_t mid) {
     if (precision == SPH_PREC_FP64) {
         sphk::hydro_kernel<true, HYDRO64_WARPS><<<grid, HYDRO64_WARPS * 32, 0, s>>>(a);
+        if (mid) cudaEventRecord(mid, s);
         return;
     }
     sphk::hydro_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
+    if (mid) cudaEventRecord(mid, s);
     if (a.n_i <= 0) return;
     const int need = (a.n_i + sphk::HYDRO_DF_THREADS - 1) / sphk::HYDRO_DF_THREADS;
     sphk::hydro_df_lists<<<std::max(1, std::min(need, dfgrid)), sphk::HYDRO_DF_THREADS, 0, s>>>(a);

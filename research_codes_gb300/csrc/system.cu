@@ -58,7 +58,7 @@ enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIR
 enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
 // phase events
 enum { EV_TREE_B = 0, EV_TREE_E, EV_DENS_B, EV_DENSK_B, EV_DENSK_E, EV_DENS_E, EV_GLIST_B, EV_GLIST_E, EV_GK_B,
-       EV_GK_E, EV_HLIST_B, EV_HK_B, EV_HK_E, EV_END, EV_N };
+       EV_GK_E, EV_HLIST_B, EV_HK_B, EV_HK_E, EV_END, EV_HK_MID, EV_N };
 
 inline int grid_for(long long n, int threads = 256) {
     long long b = (n + threads - 1) / threads;
@@ -1683,7 +1683,7 @@ int hydro_phase(sph_system *s, bool eager) {
         CUDA_TRY(cudaMemsetAsync(s->scal.p + S_HOVF, 0, sizeof(int), st));
     }
     sphrt::launch_hydro(a, ctx->prm.precision, ctx->grid[1][ctx->prm.precision == SPH_PREC_FP64], st,
-                        ctx->grid_df);
+                        ctx->grid_df, s->ev[EV_HK_MID]);
     cudaEventRecord(s->ev[EV_HK_E], st);
     AlphaParams ap{s->prm.alpha_max, s->prm.alpha_min, s->prm.alphu_max, s->prm.alphu_min};
     hydro_writeback<<<grid_for(n), 256, 0, st>>>(
@@ -2399,11 +2399,12 @@ extern "C" int sph_system_phase_times(sph_system *s, float *ms, int32_t n) {
     cudaSetDevice(s->ctx->prm.device);
     const cudaError_t se = cudaEventSynchronize(s->ev[EV_END]);
     if (se != cudaSuccess) return -sphrt::cuda_error(s->ctx, se, "cudaEventSynchronize");
-    const int pairs[8][2] = {{EV_TREE_B, EV_TREE_E}, {EV_DENS_B, EV_DENS_E}, {EV_DENSK_B, EV_DENSK_E},
-                             {EV_GLIST_B, EV_GLIST_E}, {EV_GK_B, EV_GK_E},   {EV_HLIST_B, EV_HK_B},
-                             {EV_HK_B, EV_HK_E},     {EV_TREE_B, EV_END}};
+    const int pairs[10][2] = {{EV_TREE_B, EV_TREE_E}, {EV_DENS_B, EV_DENS_E}, {EV_DENSK_B, EV_DENSK_E},
+                              {EV_GLIST_B, EV_GLIST_E}, {EV_GK_B, EV_GK_E},   {EV_HLIST_B, EV_HK_B},
+                              {EV_HK_B, EV_HK_E},     {EV_TREE_B, EV_END},   {EV_HK_B, EV_HK_MID},
+                              {EV_HK_MID, EV_HK_E}};
     int k = 0;
-    for (; k < n && k < 8; ++k) {
+    for (; k < n && k < 10; ++k) {
         float t = 0.0f;
         if (cudaEventElapsedTime(&t, s->ev[pairs[k][0]], s->ev[pairs[k][1]]) != cudaSuccess) {
             cudaGetLastError();

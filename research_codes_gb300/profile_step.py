@@ -32,6 +32,9 @@ def main():
     ap.add_argument("--precision", default="fp32c")
     ap.add_argument("--n-group", type=int, default=256)
     ap.add_argument("--quadrupole", type=int, default=0, help="1: quadrupole tree gravity")
+    ap.add_argument("--item-split-nj", type=int, default=4096)
+    ap.add_argument("--heavy-classes", type=int, default=2)
+    ap.add_argument("--gravity-jtile", type=int, default=32)
     ap.add_argument("--settle", type=int, default=4, help="force evaluations before the profiled one")
     ap.add_argument("--what", choices=("forces", "step"), default="forces",
                     help="profile one force evaluation or one whole step (after --settle steps)")
@@ -42,7 +45,9 @@ def main():
     s = state_from_ic(s)
     n = len(s["mass"])
     with functors.Context(precision=args.precision, eta=eta) as ctx:
-        ps = ParticleSystem(ctx, n, n_group=args.n_group, use_graph=0, quadrupole=args.quadrupole)
+        ps = ParticleSystem(ctx, n, n_group=args.n_group, use_graph=0, quadrupole=args.quadrupole,
+                            item_split_nj=args.item_split_nj, heavy_classes=args.heavy_classes,
+                            gravity_jtile=args.gravity_jtile)
         ps.upload(s)
         for _ in range(args.settle):
             if args.what == "step":

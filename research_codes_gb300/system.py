@@ -242,12 +242,12 @@ class ParticleSystem:
         return i_first[:nw.value], i_count[:nw.value], j_off, j_idx[:ne.value]
 
     PHASES = ("tree", "density", "density_kernel", "gravity_lists", "gravity_kernel", "hydro_lists",
-              "hydro_kernel", "force_total")
+              "hydro_kernel", "force_total", "hydro_signal", "hydro_df")
 
     def phase_times(self):
         """Device ms of the phases of the last force evaluation (CUDA events)."""
-        buf = (ctypes.c_float * 8)()
-        k = self.lib.sph_system_phase_times(self.handle, buf, 8)
+        buf = (ctypes.c_float * 10)()
+        k = self.lib.sph_system_phase_times(self.handle, buf, 10)
         if k < 0:
             check(-k, self.ctx.handle, "phase_times")
         return {name: float(buf[i]) for i, name in enumerate(self.PHASES[:k])}

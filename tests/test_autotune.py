@@ -49,7 +49,7 @@ def test_coordinate_descent_finds_the_minimum_of_a_separable_cost():
     keys = [tuple(sorted(p.items())) for p, _ in table]
     assert len(keys) == len(set(keys))
     # one warm-up plus `reps` evaluations per distinct combination
-    assert ps.evaluations == 4 * len(table)
+    assert ps.evaluations == 4 * len(table) + 1   # and one with the kept parameters
 
 
 def test_apply_false_restores_the_original_parameters():

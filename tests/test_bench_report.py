@@ -30,7 +30,7 @@ def test_tree_lists_rate_without_a_capture(tmp_path):
 
 def test_pair_kernel_traffic_entries():
     tr = json.load(open(bench.PROFILE_TRAFFIC))
-    for k in ("density", "hydro", "gravity"):
+    for k in ("density", "hydro_signal", "hydro_df", "gravity"):
         assert tr[k]["bytes_per_launch"] == round(tr[k]["read"] + tr[k]["write"])
         assert tr[k]["ncu_ms"] > 0
 
