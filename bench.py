@@ -564,41 +564,45 @@ def tree_groups(keys, n_group):
     return [np.arange(a, b) for a, b in sorted(out)]
 
 
-def host_walks_density(tree, s, groups, rs, active=None):
+def _group_ranges(groups):
+    gf = np.array([g[0] for g in groups], np.int64)
+    gc = np.array([len(g) for g in groups], np.int64)
+    return gf, gc
+
+
+def host_walks_density(s, keys, groups, rs, active, nthreads):
     """Gather lists (hdr_density.hpp:389-397; FDPS's Gather search): for each
     group with iterating particles, every j within the largest search radius
-    of those particles from the group's bounding box.  Returns EPI/EPJ walk
-    arrays and the i-particle indices, in walk order."""
+    of those particles from the group's bounding box (host octree,
+    oracle_neighbour_lists).  Returns EPI/EPJ walk arrays and the i-particle
+    indices, in walk order."""
+    from oracle import oracle as orc
     from research_codes_gb300 import walks
-    items, idx = [], []
-    for g in groups:
-        gi = g if active is None else g[active[g]]
-        if len(gi) == 0:
-            continue
-        lo, hi = s["pos"][g].min(0), s["pos"][g].max(0)
-        r = rs[gi].max()
-        cand = np.array(tree.query_ball_point(0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo) + r), dtype=np.int64)
-        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
-        items.append((walks.density_epi(gi, s, rs), walks.density_epj(np.sort(cand[(d * d).sum(1) <= r * r]), s)))
-        idx.append(gi)
-    return walks.concat_walks(items), np.concatenate(idx)
+    gf, gc = _group_ranges(groups)
+    owner = np.repeat(np.arange(len(groups)), gc)
+    gr = np.full(len(groups), -1.0)
+    np.maximum.at(gr, owner[active], rs[active])
+    off, idx = orc.neighbour_lists(keys, s["pos"], s["ksr"], gf, gc, gr, 0, 8, nthreads)
+    keep = gr >= 0.0
+    i_idx = np.flatnonzero(active)                       # group order = index order
+    i_off = np.concatenate([[0], np.cumsum(np.bincount(owner[active], minlength=len(groups))[keep])])
+    j_off = np.concatenate([[0], np.cumsum(np.diff(off)[keep])])
+    epi = walks.density_epi(i_idx, s, rs)
+    epj = walks.density_epj(idx, s)
+    return (epi, epj, i_off.astype(np.int64), j_off.astype(np.int64)), i_idx
 
 
-def host_walks_hydro(tree, s, groups):
+def host_walks_hydro(s, keys, groups, nthreads):
     """Symmetric lists (main.cpp:336-344; FDPS's Symmetry search): every j
     within max(max_{i in g} h_i, h_j) of the group's bounding box."""
+    from oracle import oracle as orc
     from research_codes_gb300 import walks
-    hmax = s["ksr"].max()
-    items = []
-    for g in groups:
-        lo, hi = s["pos"][g].min(0), s["pos"][g].max(0)
-        rg = s["ksr"][g].max()
-        cand = np.array(tree.query_ball_point(0.5 * (lo + hi), 0.5 * np.linalg.norm(hi - lo) + max(rg, hmax)),
-                        dtype=np.int64)
-        d = np.maximum(lo - s["pos"][cand], 0) + np.maximum(s["pos"][cand] - hi, 0)
-        rj = np.maximum(rg, s["ksr"][cand])
-        items.append((walks.hydro_epi(g, s), walks.hydro_epj(np.sort(cand[(d * d).sum(1) <= rj * rj]), s)))
-    return walks.concat_walks(items)
+    gf, gc = _group_ranges(groups)
+    gr = np.maximum.reduceat(s["ksr"], gf)
+    off, idx = orc.neighbour_lists(keys, s["pos"], s["ksr"], gf, gc, gr, 1, 8, nthreads)
+    i_off = np.concatenate([[0], np.cumsum(gc)])
+    epi = walks.hydro_epi(np.arange(len(s["mass"])), s)
+    return epi, walks.hydro_epj(idx, s), i_off.astype(np.int64), off.astype(np.int64)
 
 
 def host_walks_gravity(s, keys, groups, theta, nthreads):
@@ -632,12 +636,9 @@ def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, cache=None):
     seconds and listed pairs per phase and the density walks.  `cache`
     (a dict) keeps the walk arrays of the first call for later calls on the
     same state, which then time the functors alone."""
-    from scipy.spatial import cKDTree
-
     from oracle import oracle as orc
     from research_codes_gb300 import units
     reuse = cache is not None and "density" in cache
-    tree = None if reuse else cKDTree(s["pos"])
     n = len(s["mass"])
     sec = {"density": 0.0, "gravity": 0.0, "hydro": 0.0}
     pairs = {"density": 0, "gravity": 0, "hydro": 0}
@@ -649,7 +650,7 @@ def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, cache=None):
         if reuse:
             (epi, epj, io, jo), idx = cache["density"][walks_d]
         else:
-            (epi, epj, io, jo), idx = host_walks_density(tree, dict(s, ksr=h0), groups, rs, active)
+            (epi, epj, io, jo), idx = host_walks_density(dict(s, ksr=h0), keys, groups, rs, active, nthreads)
             if cache is not None:
                 cache.setdefault("density_build", []).append(((epi, epj, io, jo), idx))
         t = time.perf_counter()
@@ -684,7 +685,7 @@ def host_force_evaluation(s, keys, groups, nthreads, theta=0.5, cache=None):
     if reuse:
         epi, epj, io, jo = cache["hydro"]
     else:
-        epi, epj, io, jo = host_walks_hydro(tree, s, groups)
+        epi, epj, io, jo = host_walks_hydro(s, keys, groups, nthreads)
         if cache is not None:
             cache["hydro"] = (epi, epj, io, jo)
     t = time.perf_counter()

@@ -89,6 +89,9 @@ def oracle_lib():
         lib.oracle_gravity_lists.argtypes = [ctypes.c_int64, _P, _P, _P, _P, ctypes.c_int32, _P, _P, _D,
                                              ctypes.c_int32, _P, _P, _P, _P, _P, _P, _I]
         lib.oracle_gravity_lists.restype = ctypes.c_int64
+        lib.oracle_neighbour_lists.argtypes = [ctypes.c_int64, _P, _P, _P, ctypes.c_int32, _P, _P, _P,
+                                               ctypes.c_int32, ctypes.c_int32, _P, _P, _I]
+        lib.oracle_neighbour_lists.restype = None
         _oracle = lib
     return _oracle
 
@@ -361,3 +364,23 @@ def gravity_tree_lists(keys, pos, mass, eps2, gfirst, gcount, theta=0.5, n_leaf=
     neps2 = np.zeros(nn)
     lib.oracle_gravity_lists(*args, _ptr(ep_idx), _ptr(sp_idx), _ptr(mom), _ptr(neps2), nthreads)
     return ep_off, ep_idx, sp_off, sp_idx, mom, neps2
+
+
+def neighbour_lists(keys, pos, h, gfirst, gcount, gr, mode, n_leaf=8, nthreads=0):
+    """Host octree neighbour lists (oracle_neighbour_lists): per group g the
+    particles within gr[g] of its bounding box (mode 0, gather) or within
+    max(gr[g], h_j) (mode 1, symmetric), ascending; gr < 0 gives an empty
+    list.  Returns (off, idx).  keys must be sorted, pos and h in that order."""
+    lib = oracle_lib()
+    keys = np.ascontiguousarray(keys, np.uint64)
+    pos, h, gr = _f64(pos), _f64(h), _f64(gr)
+    gfirst = np.ascontiguousarray(gfirst, np.int64)
+    gcount = np.ascontiguousarray(gcount, np.int64)
+    ng = len(gfirst)
+    off = np.zeros(ng + 1, np.int64)
+    args = (len(h), _ptr(keys), _ptr(pos), _ptr(h), ng, _ptr(gfirst), _ptr(gcount), _ptr(gr), int(mode), n_leaf,
+            _ptr(off))
+    lib.oracle_neighbour_lists(*args, None, nthreads)
+    idx = np.zeros(max(int(off[-1]), 1), np.int32)
+    lib.oracle_neighbour_lists(*args, _ptr(idx), nthreads)
+    return off, idx[:int(off[-1])]

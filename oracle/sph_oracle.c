@@ -456,6 +456,7 @@ typedef struct {
     int64_t first, count;
     int32_t child0, nchild;   /* children: consecutive node indices */
     double com[3], mass, eps2, size;
+    double lo[3], hi[3], hmax; /* particle bounding box, largest h (neighbour lists) */
 } otree_node;
 
 typedef struct {
@@ -487,6 +488,7 @@ static void otree_build(otree *t, int64_t v, const uint64_t *keys, const double 
     otree_node nd = t->nodes[v];
     double m = 0.0, c[3] = {0.0, 0.0, 0.0}, e = 0.0, lo[3], hi[3];
     for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+    nd.hmax = 0.0;
     for (int64_t i = nd.first; i < nd.first + nd.count; ++i) {
         m += mass[i];
         e += mass[i] * eps2[i];
@@ -502,6 +504,8 @@ static void otree_build(otree *t, int64_t v, const uint64_t *keys, const double 
     nd.size = 0.0;
     for (int k = 0; k < 3; ++k) {
         nd.com[k] = c[k] / m;
+        nd.lo[k] = lo[k];
+        nd.hi[k] = hi[k];
         if (hi[k] - lo[k] > nd.size) nd.size = hi[k] - lo[k];
     }
     nd.child0 = -1;
@@ -617,4 +621,98 @@ int64_t oracle_gravity_lists(int64_t n, const uint64_t *keys, const double *pos,
     const int64_t nn = t.n_nodes;
     free(t.nodes);
     return nn;
+}
+
+/* Largest h of every node (children before parents: children have larger
+ * indices than their parent). */
+static void otree_hmax(otree *t, const double *h) {
+    for (int64_t v = t->n_nodes - 1; v >= 0; --v) {
+        otree_node *nd = &t->nodes[v];
+        double m = 0.0;
+        if (nd->nchild == 0) {
+            for (int64_t i = nd->first; i < nd->first + nd->count; ++i)
+                if (h[i] > m) m = h[i];
+        } else {
+            for (int32_t u = nd->child0; u < nd->child0 + nd->nchild; ++u)
+                if (t->nodes[u].hmax > m) m = t->nodes[u].hmax;
+        }
+        nd->hmax = m;
+    }
+}
+
+static double box_d2(const double *alo, const double *ahi, const double *blo, const double *bhi) {
+    double d2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        double d = 0.0;
+        if (blo[k] > ahi[k]) d = blo[k] - ahi[k];
+        else if (alo[k] > bhi[k]) d = alo[k] - bhi[k];
+        d2 += d * d;
+    }
+    return d2;
+}
+
+/* Gather and symmetric neighbour lists of groups (the roles of FDPS's
+ * Gather search for the density, hdr_density.hpp:389-397, and its Symmetry
+ * search for the hydro force, main.cpp:336-344), on the host octree above.
+ * Group g covers particles [gfirst[g], gfirst[g] + gcount[g]) with bounding
+ * box B_g and radius gr[g] (gr < 0: the group gets an empty list).
+ *   mode 0: every particle j with dist(x_j, B_g) <= gr[g];
+ *   mode 1: every particle j with dist(x_j, B_g) <= max(gr[g], h[j]).
+ * Entries come in ascending particle order.  Fills off (ng + 1) and, when idx
+ * is non-null, the lists (call once with idx null to size them). */
+void oracle_neighbour_lists(int64_t n, const uint64_t *keys, const double *pos, const double *h, int32_t ng,
+                            const int64_t *gfirst, const int64_t *gcount, const double *gr, int32_t mode,
+                            int32_t n_leaf, int64_t *off, int32_t *idx, int nthreads) {
+    set_threads(nthreads);
+    double *unit = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    for (int64_t i = 0; i < n; ++i) unit[i] = 1.0;
+    otree t = {0, 0, 0, 0};
+    const int64_t root = otree_push(&t);
+    t.nodes[root].first = 0;
+    t.nodes[root].count = n;
+    otree_build(&t, root, keys, pos, unit, unit, 0, n_leaf);
+    otree_hmax(&t, h);
+    free(unit);
+    const int fill = idx != NULL;
+#pragma omp parallel
+    {
+        int32_t *stack = (int32_t *)malloc(sizeof(int32_t) * (size_t)(8 * 22 + 64));
+#pragma omp for schedule(dynamic, 4)
+        for (int32_t g = 0; g < ng; ++g) {
+            int64_t ne = 0;
+            if (gr[g] >= 0.0 && gcount[g] > 0) {
+                double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+                for (int64_t i = gfirst[g]; i < gfirst[g] + gcount[g]; ++i)
+                    for (int k = 0; k < 3; ++k) {
+                        if (pos[3 * i + k] < lo[k]) lo[k] = pos[3 * i + k];
+                        if (pos[3 * i + k] > hi[k]) hi[k] = pos[3 * i + k];
+                    }
+                int32_t *out = fill ? idx + off[g] : NULL;
+                int64_t top = 0;
+                stack[top++] = 0;
+                while (top > 0) {
+                    const otree_node *nd = &t.nodes[stack[--top]];
+                    const double r = (mode == 1 && nd->hmax > gr[g]) ? nd->hmax : gr[g];
+                    if (box_d2(lo, hi, nd->lo, nd->hi) > r * r) continue;
+                    if (nd->nchild == 0) {
+                        for (int64_t i = nd->first; i < nd->first + nd->count; ++i) {
+                            const double ri = (mode == 1 && h[i] > gr[g]) ? h[i] : gr[g];
+                            if (box_d2(lo, hi, pos + 3 * i, pos + 3 * i) > ri * ri) continue;
+                            if (out) out[ne] = (int32_t)i;
+                            ++ne;
+                        }
+                    } else {
+                        for (int32_t u = nd->child0 + nd->nchild - 1; u >= nd->child0; --u) stack[top++] = u;
+                    }
+                }
+            }
+            if (!fill) off[g + 1] = ne;
+        }
+        free(stack);
+    }
+    if (!fill) {
+        off[0] = 0;
+        for (int32_t g = 0; g < ng; ++g) off[g + 1] += off[g];
+    }
+    free(t.nodes);
 }

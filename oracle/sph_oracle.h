@@ -122,6 +122,9 @@ int64_t oracle_gravity_lists(int64_t n, const uint64_t *keys, const double *pos,
                              double theta, int32_t n_leaf, int64_t *ep_off, int64_t *sp_off,
                              int32_t *ep_idx, int32_t *sp_idx, double *node_mom, double *node_eps2,
                              int nthreads);
+void oracle_neighbour_lists(int64_t n, const uint64_t *keys, const double *pos, const double *h, int32_t ng,
+                            const int64_t *gfirst, const int64_t *gcount, const double *gr, int32_t mode,
+                            int32_t n_leaf, int64_t *off, int32_t *idx, int nthreads);
 
 #ifdef __cplusplus
 }

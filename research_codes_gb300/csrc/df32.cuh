@@ -20,6 +20,9 @@
 #pragma once
 
 #include <cmath>
+#include <cstring>
+
+#include <vector_types.h>
 
 #if defined(__CUDACC__)
 #define DF_HD __host__ __device__ __forceinline__
@@ -29,9 +32,12 @@
 
 namespace dfk {
 
-struct df {
-    float h, l;
+// hi + lo over a lane type T (float; on the device also pk, below)
+template <class T>
+struct dv {
+    T h, l;
 };
+using df = dv<float>;
 
 DF_HD float add(float a, float b) {
 #if defined(__CUDA_ARCH__)
@@ -166,6 +172,183 @@ DF_HD double to_double(df x) { return (double)x.h + (double)x.l; }
 DF_HD df split(double v) {
     const float h = (float)v;
     return df{h, (float)(v - (double)h)};
+}
+
+// ---------------------------------------------------------------------------
+// Lean double-float operations, generic over the lane type T: float, or on
+// the device pk, two FP32 lanes in one 64-bit register pair that the packed
+// f32x2 instructions of sm_100 and later process at once (each half rounded
+// exactly as the scalar instruction would round it).  Two independent
+// double-float computations then share every instruction.
+//
+// The results are left unnormalised: the closing Fast2Sum of Dekker's
+// operations is dropped, so |l| may reach a few ulps of h instead of half
+// an ulp (the operands must themselves have |l| << |h|; diff_t, whose lo
+// inputs may carry the whole difference, normalises).  Every error-free transformation is kept (TwoSum of the hi parts,
+// the FMA product error), so the relative error stays ~2^-44, while a
+// multiplication costs 4 operations instead of 7 and an addition 8 instead
+// of 11.  Callers that need a normalised value (shuffles, the final sums)
+// use the operations above.
+
+DF_HD float fms(float a, float b, float c) {   // a b - c, one rounding
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, -c);
+#else
+    return std::fma(a, b, -c);
+#endif
+}
+template <class T>
+DF_HD T cst(float c);
+template <>
+DF_HD float cst<float>(float c) { return c; }
+
+// Packed operations: the f32x2 instructions on the device; the host
+// versions apply the scalar operation per half (same results).
+struct pk {
+    unsigned long long v;
+};
+DF_HD pk pack(float a, float b) {
+    pk r;
+#if defined(__CUDA_ARCH__)
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+#else
+    unsigned int ua, ub;
+    memcpy(&ua, &a, 4);
+    memcpy(&ub, &b, 4);
+    r.v = (unsigned long long)ua | ((unsigned long long)ub << 32);
+#endif
+    return r;
+}
+DF_HD float2 unpack(pk x) {
+    float2 r;
+#if defined(__CUDA_ARCH__)
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(x.v));
+#else
+    const unsigned int ua = (unsigned int)x.v, ub = (unsigned int)(x.v >> 32);
+    memcpy(&r.x, &ua, 4);
+    memcpy(&r.y, &ub, 4);
+#endif
+    return r;
+}
+template <>
+DF_HD pk cst<pk>(float c) { return pack(c, c); }
+#if defined(__CUDA_ARCH__)
+#define DF_PK2(name, op)                                                        \
+    DF_HD pk name(pk a, pk b) {                                                 \
+        pk r;                                                                   \
+        asm(op ".rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));     \
+        return r;                                                               \
+    }
+DF_PK2(add, "add")
+DF_PK2(sub, "sub")
+DF_PK2(mul, "mul")
+#undef DF_PK2
+DF_HD pk fma(pk a, pk b, pk c) {
+    pk r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+#else
+DF_HD pk add(pk a, pk b) {
+    const float2 x = unpack(a), y = unpack(b);
+    return pack(add(x.x, y.x), add(x.y, y.y));
+}
+DF_HD pk sub(pk a, pk b) {
+    const float2 x = unpack(a), y = unpack(b);
+    return pack(sub(x.x, y.x), sub(x.y, y.y));
+}
+DF_HD pk mul(pk a, pk b) {
+    const float2 x = unpack(a), y = unpack(b);
+    return pack(mul(x.x, y.x), mul(x.y, y.y));
+}
+DF_HD pk fma(pk a, pk b, pk c) {
+    const float2 x = unpack(a), y = unpack(b), z = unpack(c);
+    return pack(fma(x.x, y.x, z.x), fma(x.y, y.y, z.y));
+}
+#endif
+DF_HD pk fms(pk a, pk b, pk c) {   // a b - c: the sign bits of c flipped
+    pk nc;
+    nc.v = c.v ^ 0x8000000080000000ull;
+    return fma(a, b, nc);
+}
+
+// Knuth TwoSum and TwoDiff (s + e = a +- b exactly).
+template <class T>
+DF_HD dv<T> two_sum_t(T a, T b) {
+    const T s = add(a, b);
+    const T bb = sub(s, a);
+    return dv<T>{s, add(sub(a, sub(s, bb)), sub(b, bb))};
+}
+template <class T>
+DF_HD dv<T> two_diff_t(T a, T b) {
+    const T s = sub(a, b);
+    const T bb = sub(s, a);
+    return dv<T>{s, sub(sub(a, sub(s, bb)), add(b, bb))};
+}
+template <class T>
+DF_HD dv<T> add_t(dv<T> x, dv<T> y) {
+    const dv<T> s = two_sum_t(x.h, y.h);
+    return dv<T>{s.h, add(s.l, add(x.l, y.l))};
+}
+template <class T>
+DF_HD dv<T> add_t(dv<T> x, T b) {
+    const dv<T> s = two_sum_t(x.h, b);
+    return dv<T>{s.h, add(s.l, x.l)};
+}
+template <class T>
+DF_HD dv<T> mul_t(dv<T> x, dv<T> y) {
+    const T p = mul(x.h, y.h);
+    return dv<T>{p, fma(x.l, y.h, fma(x.h, y.l, fms(x.h, y.h, p)))};
+}
+template <class T>
+DF_HD dv<T> mul_t(dv<T> x, T b) {
+    const T p = mul(x.h, b);
+    return dv<T>{p, fma(x.l, b, fms(x.h, b, p))};
+}
+template <class T>
+DF_HD dv<T> sqr_t(dv<T> x) {
+    const T p = mul(x.h, x.h);
+    return dv<T>{p, fma(add(x.h, x.h), x.l, fms(x.h, x.h, p))};
+}
+// (ah + al) - (bh + bl) for hi/lo splits of two FP64 values, normalised
+// (Fast2Sum): when the hi parts are equal or nearly so (close particles far
+// from the origin) the lo difference is the whole result, not a correction.
+template <class T>
+DF_HD dv<T> diff_t(T ah, T al, T bh, T bl) {
+    const dv<T> s = two_diff_t(ah, bh);
+    const T l = add(s.l, sub(al, bl));
+    const T h = add(s.h, l);
+    return dv<T>{h, sub(l, sub(h, s.h))};
+}
+// s += x (the hi parts by TwoSum, the rest gathered in s.l)
+template <class T>
+DF_HD void accumulate_t(dv<T> &s, dv<T> x) {
+    const dv<T> t = two_sum_t(s.h, x.h);
+    s.l = add(s.l, add(t.l, x.l));
+    s.h = t.h;
+}
+template <class T>
+DF_HD void accumulate_t(dv<T> &s, T x) {
+    const dv<T> t = two_sum_t(s.h, x);
+    s.l = add(s.l, t.l);
+    s.h = t.h;
+}
+DF_HD float rsqrt_seed_t(float x) { return rsqrt_seed(x); }
+DF_HD pk rsqrt_seed_t(pk x) {
+    const float2 v = unpack(x);
+    return pack(rsqrt_seed(v.x), rsqrt_seed(v.y));
+}
+// 1/sqrt(x), x > 0: the Newton step of rsqrt above, its result left as the
+// pair (seed, correction)
+template <class T>
+DF_HD dv<T> rsqrt_t(dv<T> x) {
+    const T y = rsqrt_seed_t(x.h);
+    const T th = mul(y, y);
+    const T tl = fms(y, y, th);
+    const T m = mul(x.h, th);
+    const T me = fma(x.l, th, fma(x.h, tl, fms(x.h, th, m)));
+    const T e = sub(sub(cst<T>(1.0f), m), me);
+    return dv<T>{y, mul(mul(e, y), fma(cst<T>(0.375f), e, cst<T>(0.5f)))};
 }
 
 }  // namespace dfk

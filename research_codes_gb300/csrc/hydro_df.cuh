@@ -11,18 +11,26 @@
 // formed with double-float operands and accumulators (~44 bits, df32.cuh):
 // separations from the hi/lo particle records, 1/r by one Newton step,
 // q and u in double-float, P Omega / rho^2 and h^-1, h^-4 from double-float
-// splits of their FP64 values.  The artificial-viscosity part of the
+// splits of their FP64 values, the masses as hi/lo pairs (an FP32 mass
+// alone would scale every term of a star's equal-mass particles by the same
+// rounding, ~4e-8).  The artificial-viscosity part of the
 // pressure factor and of du/dt, the signal velocities and diffu stay FP32:
 // they do not cancel at that level.  The kernel constant -5 c1 common to
 // every term (W1(q) = c1 u^3 (u - 1 - 4q) = -5 c1 q u^3 with u = 1 - q,
 // hdr_kernel.hpp:251-257) is applied to the finished sums in FP64.
+//
+// The pair formula is written once over a lane type T (df32.cuh): float for
+// one pair at a time, pk for two pairs of the same i-particle in the two
+// halves of packed f32x2 instructions.  It uses the lean (unnormalised)
+// double-float operations: ~2^-44 relative error per term, far below the
+// ~10^-9 that a condition number of 10^3 and a 10^-5 target leave.
 //
 // The pair set is the one the signal-velocity kernel marks (every j inside
 // the support of i or j, plus a few just beyond both, whose terms are
 // exactly zero: u = max(1 - q, 0) = 0), without self pairs (equal ids,
 // hdr_hydro.hpp:356).  That kernel writes each i-particle's marked j indices
 // into a fixed-capacity row; an i-particle whose row overflowed is summed by
-// one warp over its walk's whole list instead.
+// one block over its walk's whole list instead.
 #pragma once
 
 #include <vector_types.h>
@@ -32,118 +40,186 @@
 namespace sphk {
 
 // FP32C hydro records of one particle (FP32C mode of hydro_kernel):
-//   phi (x_hi, y_hi, z_hi, mass)      plo (x_lo, y_lo, z_lo, -)
+//   phi (x_hi, y_hi, z_hi, mass_hi)   plo (x_lo, y_lo, z_lo, mass_lo)
 //   vhi (vx_hi, vy_hi, vz_hi, 1/h)    vlo (vx_lo, vy_lo, vz_lo, h^-4)
 //   g1  (P_hi, P_lo, presc_hi, bswt/2) g2 (dens, vsnd, alph, alphu)
 //   g3  (thrm_hi, thrm_lo, eta, presc_lo)
 //   g4  (1/h hi, 1/h lo, h^-4 hi, h^-4 lo)
-struct HydroDFI {
-    float xh, yh, zh, xl, yl, zl;
-    float vxh, vyh, vzh, vxl, vyl, vzl;
-    dfk::df presc, hinv, h4;
-    float eta, dens, vsnd, bswt, alph, alphu, ph, pl, th, tl;
+// as the fields the pair formula reads, over lane type T.
+template <class T>
+struct HydroDFP {
+    T xh, yh, zh, xl, yl, zl;
+    dfk::dv<T> m;
+    T vxh, vyh, vzh, vxl, vyl, vzl;
+    dfk::dv<T> presc, hinv, h4;
+    T eta, dens, vsnd, bswt, alph, alphu, ph, pl, th, tl;
 };
+
+DF_HD HydroDFP<float> hydro_df_rec(float4 phi, float4 plo, float4 vhi, float4 vlo, float4 g1, float4 g2, float4 g3,
+                                   float4 g4) {
+    HydroDFP<float> p;
+    p.xh = phi.x; p.yh = phi.y; p.zh = phi.z; p.m = dfk::dv<float>{phi.w, plo.w};
+    p.xl = plo.x; p.yl = plo.y; p.zl = plo.z;
+    p.vxh = vhi.x; p.vyh = vhi.y; p.vzh = vhi.z;
+    p.vxl = vlo.x; p.vyl = vlo.y; p.vzl = vlo.z;
+    p.presc = dfk::dv<float>{g1.z, g3.w};
+    p.hinv = dfk::dv<float>{g4.x, g4.y};
+    p.h4 = dfk::dv<float>{g4.z, g4.w};
+    p.eta = g3.z; p.dens = g2.x; p.vsnd = g2.y; p.bswt = g1.w; p.alph = g2.z; p.alphu = g2.w;
+    p.ph = g1.x; p.pl = g1.y; p.th = g3.x; p.tl = g3.y;
+    return p;
+}
 
 // Sums over j: acceleration a, softening correction g, the pressure part
 // of du/dt without its factor P_i Omega_i / rho_i^2 (ud: sum ka w), the
 // viscous part (uv: sum ka visc, FP32 terms) and diffu (dif).
+template <class T>
 struct HydroDFAcc {
-    dfk::df ax, ay, az, gx, gy, gz, ud, uv, dif;
+    dfk::dv<T> ax, ay, az, gx, gy, gz, ud, uv, dif;
 };
 
-DF_HD HydroDFI hydro_df_i(float4 phi, float4 plo, float4 vhi, float4 vlo, float4 g1, float4 g2, float4 g3,
-                          float4 g4) {
-    HydroDFI i;
-    i.xh = phi.x; i.yh = phi.y; i.zh = phi.z;
-    i.xl = plo.x; i.yl = plo.y; i.zl = plo.z;
-    i.vxh = vhi.x; i.vyh = vhi.y; i.vzh = vhi.z;
-    i.vxl = vlo.x; i.vyl = vlo.y; i.vzl = vlo.z;
-    i.presc = dfk::make(g1.z, g3.w);
-    i.hinv = dfk::make(g4.x, g4.y);
-    i.h4 = dfk::make(g4.z, g4.w);
-    i.eta = g3.z; i.dens = g2.x; i.vsnd = g2.y; i.bswt = g1.w; i.alph = g2.z; i.alphu = g2.w;
-    i.ph = g1.x; i.pl = g1.y; i.th = g3.x; i.tl = g3.y;
-    return i;
+template <class T>
+DF_HD HydroDFAcc<T> hydro_df_zero() {
+    const dfk::dv<T> z{dfk::cst<T>(0.0f), dfk::cst<T>(0.0f)};
+    return HydroDFAcc<T>{z, z, z, z, z, z, z, z, z};
 }
 
-DF_HD HydroDFAcc hydro_df_zero() {
-    const dfk::df z = dfk::make(0.0f, 0.0f);
-    return HydroDFAcc{z, z, z, z, z, z, z, z, z};
+// Per-lane operations that have no packed instruction.
+DF_HD float lane_min0(float x) { return x < 0.0f ? x : 0.0f; }
+DF_HD float lane_rcp(float x) { return 1.0f / x; }
+DF_HD float lane_sqrt0(float x) { return x > 0.0f ? sqrtf(x) : 0.0f; }
+DF_HD float lane_abs(float x) { return fabsf(x); }
+// u, or exactly zero where u.h <= 0 (beyond the support)
+DF_HD dfk::dv<float> lane_pos(dfk::dv<float> u) {
+    return (u.h > 0.0f) ? u : dfk::dv<float>{0.0f, 0.0f};
+}
+DF_HD dfk::pk lane_min0(dfk::pk x) {
+    const float2 v = dfk::unpack(x);
+    return dfk::pack(lane_min0(v.x), lane_min0(v.y));
+}
+DF_HD dfk::pk lane_rcp(dfk::pk x) {
+    const float2 v = dfk::unpack(x);
+    return dfk::pack(1.0f / v.x, 1.0f / v.y);
+}
+DF_HD dfk::pk lane_sqrt0(dfk::pk x) {
+    const float2 v = dfk::unpack(x);
+    return dfk::pack(lane_sqrt0(v.x), lane_sqrt0(v.y));
+}
+DF_HD dfk::pk lane_abs(dfk::pk x) {
+    dfk::pk r;
+    r.v = x.v & 0x7fffffff7fffffffull;
+    return r;
+}
+DF_HD dfk::dv<dfk::pk> lane_pos(dfk::dv<dfk::pk> u) {
+    const float2 h = dfk::unpack(u.h), l = dfk::unpack(u.l);
+    const bool a = h.x > 0.0f, b = h.y > 0.0f;
+    return dfk::dv<dfk::pk>{dfk::pack(a ? h.x : 0.0f, b ? h.y : 0.0f), dfk::pack(a ? l.x : 0.0f, b ? l.y : 0.0f)};
+}
+// two particles' records in the two lanes, and one particle's in both
+DF_HD dfk::dv<dfk::pk> pack_dv(dfk::dv<float> a, dfk::dv<float> b) {
+    return dfk::dv<dfk::pk>{dfk::pack(a.h, b.h), dfk::pack(a.l, b.l)};
+}
+DF_HD HydroDFP<dfk::pk> hydro_df_pack(const HydroDFP<float> &a, const HydroDFP<float> &b) {
+    using dfk::pack;
+    HydroDFP<dfk::pk> p;
+    p.xh = pack(a.xh, b.xh); p.yh = pack(a.yh, b.yh); p.zh = pack(a.zh, b.zh);
+    p.xl = pack(a.xl, b.xl); p.yl = pack(a.yl, b.yl); p.zl = pack(a.zl, b.zl);
+    p.m = pack_dv(a.m, b.m);
+    p.vxh = pack(a.vxh, b.vxh); p.vyh = pack(a.vyh, b.vyh); p.vzh = pack(a.vzh, b.vzh);
+    p.vxl = pack(a.vxl, b.vxl); p.vyl = pack(a.vyl, b.vyl); p.vzl = pack(a.vzl, b.vzl);
+    p.presc = pack_dv(a.presc, b.presc);
+    p.hinv = pack_dv(a.hinv, b.hinv);
+    p.h4 = pack_dv(a.h4, b.h4);
+    p.eta = pack(a.eta, b.eta); p.dens = pack(a.dens, b.dens); p.vsnd = pack(a.vsnd, b.vsnd);
+    p.bswt = pack(a.bswt, b.bswt); p.alph = pack(a.alph, b.alph); p.alphu = pack(a.alphu, b.alphu);
+    p.ph = pack(a.ph, b.ph); p.pl = pack(a.pl, b.pl); p.th = pack(a.th, b.th); p.tl = pack(a.tl, b.tl);
+    return p;
+}
+// lane 0 and lane 1 of a packed double-float
+DF_HD dfk::df lane0(dfk::dv<dfk::pk> x) {
+    return dfk::df{dfk::unpack(x.h).x, dfk::unpack(x.l).x};
+}
+DF_HD dfk::df lane1(dfk::dv<dfk::pk> x) {
+    return dfk::df{dfk::unpack(x.h).y, dfk::unpack(x.l).y};
 }
 
 // q u^3 h^-4 with q = r / h, u = max(1 - q, 0): the kernel-gradient factor
 // W1(q) h^-4 / (-5 c1) (hdr_kernel.hpp:251-257), exactly zero for q >= 1.
-DF_HD dfk::df hydro_df_grad(dfk::df r, dfk::df hinv, dfk::df h4) {
+template <class T>
+DF_HD dfk::dv<T> hydro_df_grad(dfk::dv<T> r, dfk::dv<T> hinv, dfk::dv<T> h4) {
     using namespace dfk;
-    const df q = mul(r, hinv);
-    // 1 - q.h is exact for q.h in [1/2, 2] and Fast2Sum-exact below; beyond,
-    // u < 0 and the factor is zero
-    const df s = fast_two_sum(1.0f, -q.h);
-    const df u = fast_two_sum(s.h, sub(s.l, q.l));
-    if (!(u.h > 0.0f)) return make(0.0f, 0.0f);
-    return mul(mul(q, mul(sqr(u), u)), h4);
+    const dv<T> q = mul_t(r, hinv);
+    // u = 1 - q: Fast2Sum of 1 and -q.h (its error term exact for q.h <= 1;
+    // beyond, u <= 0 and the factor is zero), then q's lo part
+    const T one = cst<T>(1.0f);
+    const T uh = sub(one, q.h);
+    const dv<T> u = lane_pos(dv<T>{uh, sub(sub(sub(one, uh), q.h), q.l)});
+    return mul_t(mul_t(q, mul_t(sqr_t(u), u)), h4);
 }
 
-// One pair (i, j) of calcHydro (hdr_hydro.hpp:349-398) added to acc; j given
-// by its records.  The pair must not be a self pair.
-DF_HD void hydro_df_pair(const HydroDFI &i, float4 phi, float4 plo, float4 vhi, float4 vlo, float4 g1, float4 g2,
-                         float4 g3, float4 g4, HydroDFAcc &acc) {
+// One pair (i, j) of calcHydro (hdr_hydro.hpp:349-398) added to acc.  The
+// pair must not be a self pair.
+template <class T>
+DF_HD void hydro_df_pair(const HydroDFP<T> &i, const HydroDFP<T> &j, HydroDFAcc<T> &acc) {
     using namespace dfk;
-    const df dx = diff(i.xh, i.xl, phi.x, plo.x);
-    const df dy = diff(i.yh, i.yl, phi.y, plo.y);
-    const df dz = diff(i.zh, i.zl, phi.z, plo.z);
-    const df r2 = add(add(sqr(dx), sqr(dy)), sqr(dz));
-    const df ri = rsqrt(r2);
-    const df r = mul(r2, ri);
-    const df dwi = hydro_df_grad(r, i.hinv, i.h4);
-    const df dwj = hydro_df_grad(r, make(g4.x, g4.y), make(g4.z, g4.w));
-    const df ka = mul(add(dwi, dwj), phi.w);   // (dW_i + dW_j) m_j / (-5 c1)
+    const dv<T> dx = diff_t(i.xh, i.xl, j.xh, j.xl);
+    const dv<T> dy = diff_t(i.yh, i.yl, j.yh, j.yl);
+    const dv<T> dz = diff_t(i.zh, i.zl, j.zh, j.zl);
+    const dv<T> r2 = add_t(add_t(sqr_t(dx), sqr_t(dy)), sqr_t(dz));
+    const dv<T> ri = rsqrt_t(r2);
+    const dv<T> r = mul_t(r2, ri);
+    const dv<T> dwi = hydro_df_grad(r, i.hinv, i.h4);
+    const dv<T> dwj = hydro_df_grad(r, j.hinv, j.h4);
+    const dv<T> ka = mul_t(add_t(dwi, dwj), j.m);   // (dW_i + dW_j) m_j / (-5 c1)
     // velocity projection w = v_ij . r_ij / r, and the viscosity (FP32)
-    const df ux = diff(i.vxh, i.vxl, vhi.x, vlo.x);
-    const df uy = diff(i.vyh, i.vyl, vhi.y, vlo.y);
-    const df uz = diff(i.vzh, i.vzl, vhi.z, vlo.z);
-    const df w = mul(add(add(mul(dx, ux), mul(dy, uy)), mul(dz, uz)), ri);
-    const float wneg = w.h < 0.0f ? w.h : 0.0f;
-    const float vs = i.vsnd + g2.y - 3.0f * wneg;
-    const float rhi = 1.0f / (i.dens + g2.x);
-    const float av = (i.bswt + g1.w) * (i.alph + g2.z) * vs * wneg;
+    const dv<T> ux = diff_t(i.vxh, i.vxl, j.vxh, j.vxl);
+    const dv<T> uy = diff_t(i.vyh, i.vyl, j.vyh, j.vyl);
+    const dv<T> uz = diff_t(i.vzh, i.vzl, j.vzh, j.vzl);
+    const dv<T> w = mul_t(add_t(add_t(mul_t(dx, ux), mul_t(dy, uy)), mul_t(dz, uz)), ri);
+    // FP32 values of the unnormalised w, ka and 1/r for the FP32 terms (h
+    // alone may be a few ulps off)
+    const T wneg = lane_min0(add(w.h, w.l));
+    const T vs = dfk::fma(cst<T>(-3.0f), wneg, add(i.vsnd, j.vsnd));
+    const T rhi = lane_rcp(add(i.dens, j.dens));
+    const T av = mul(mul(mul(add(i.bswt, j.bswt), add(i.alph, j.alph)), vs), wneg);
     // pressure gradient with the viscous pressure, :378-382
-    const df pf = add(add(i.presc, make(g1.z, g3.w)), -0.5f * av * rhi);
-    const df fa = mul(mul(pf, ka), ri);
-    accumulate(acc.ax, mul(fa, dx));
-    accumulate(acc.ay, mul(fa, dy));
-    accumulate(acc.az, mul(fa, dz));
+    const dv<T> pf = add_t(add_t(i.presc, j.presc), mul(mul(cst<T>(-0.5f), av), rhi));
+    const dv<T> fa = mul_t(mul_t(pf, ka), ri);
+    accumulate_t(acc.ax, mul_t(fa, dx));
+    accumulate_t(acc.ay, mul_t(fa, dy));
+    accumulate_t(acc.az, mul_t(fa, dz));
     // energy equation with conduction, :384-393: ka (P_i Omega_i / rho_i^2 w
     // - visc), the first part summed without its constant factor
-    const float du = (i.th - g3.x) + (i.tl - g3.y);
-    const float dp = (i.ph - g1.x) + (i.pl - g1.y);
-    const float vsu2 = fabsf(dp) * rhi * 2.0f;
-    const float vsu = vsu2 > 0.0f ? sqrtf(vsu2) : 0.0f;
-    const float visc = rhi * (0.25f * av * wneg - (i.alphu + g2.w) * vsu * du);
-    accumulate(acc.ud, mul(ka, w));
-    accumulate(acc.uv, ka.h * visc);
-    accumulate(acc.dif, rhi * du * ka.h * ri.h);
+    const T du = add(sub(i.th, j.th), sub(i.tl, j.tl));
+    const T dp = add(sub(i.ph, j.ph), sub(i.pl, j.pl));
+    const T vsu = lane_sqrt0(mul(mul(lane_abs(dp), rhi), cst<T>(2.0f)));
+    const T xneg = mul(mul(add(i.alphu, j.alphu), vsu), cst<T>(-1.0f));
+    const T visc = mul(rhi, dfk::fma(xneg, du, mul(mul(cst<T>(0.25f), av), wneg)));
+    accumulate_t(acc.ud, mul_t(ka, w));
+    accumulate_t(acc.uv, mul_t(ka, visc));
+    accumulate_t(acc.dif, mul(mul(mul(rhi, du), add(ka.h, ka.l)), add(ri.h, ri.l)));
     // softening correction, :395-398
-    const df dg = mul(mul(add(mul(dwi, i.eta), mul(dwj, g3.z)), ri), phi.w);
-    accumulate(acc.gx, mul(dg, dx));
-    accumulate(acc.gy, mul(dg, dy));
-    accumulate(acc.gz, mul(dg, dz));
+    const dv<T> dg = mul_t(mul_t(add_t(mul_t(dwi, i.eta), mul_t(dwj, j.eta)), ri), j.m);
+    accumulate_t(acc.gx, mul_t(dg, dx));
+    accumulate_t(acc.gy, mul_t(dg, dy));
+    accumulate_t(acc.gz, mul_t(dg, dz));
 }
 
 // The reference's outputs from the sums: acch = 0.5 sum(-fa dx),
 // accg = 0.5 sum(dg dx), udot = 0.5 sum(...), diffu = 2 sum(...)
 // (hdr_hydro.hpp:401-421), with the factor -5 c1 of every term.
-DF_HD void hydro_df_finish(const HydroDFAcc &a, const HydroDFI &i, double c1, double *acch, double *accg,
-                           double *udot, double *diffu) {
+DF_HD void hydro_df_finish(const HydroDFAcc<float> &a, dfk::dv<float> presc, double c1, double *acch,
+                           double *accg, double *udot, double *diffu) {
+    auto dbl = [](dfk::dv<float> x) { return (double)x.h + (double)x.l; };
     const double k = -5.0 * c1;
-    acch[0] = -0.5 * k * dfk::to_double(a.ax);
-    acch[1] = -0.5 * k * dfk::to_double(a.ay);
-    acch[2] = -0.5 * k * dfk::to_double(a.az);
-    accg[0] = 0.5 * k * dfk::to_double(a.gx);
-    accg[1] = 0.5 * k * dfk::to_double(a.gy);
-    accg[2] = 0.5 * k * dfk::to_double(a.gz);
-    *udot = 0.5 * k * (dfk::to_double(i.presc) * dfk::to_double(a.ud) - dfk::to_double(a.uv));
-    *diffu = 2.0 * k * dfk::to_double(a.dif);
+    acch[0] = -0.5 * k * dbl(a.ax);
+    acch[1] = -0.5 * k * dbl(a.ay);
+    acch[2] = -0.5 * k * dbl(a.az);
+    accg[0] = 0.5 * k * dbl(a.gx);
+    accg[1] = 0.5 * k * dbl(a.gy);
+    accg[2] = 0.5 * k * dbl(a.gz);
+    *udot = 0.5 * k * (dbl(presc) * dbl(a.ud) - dbl(a.uv));
+    *diffu = 2.0 * k * dbl(a.dif);
 }
 
 }  // namespace sphk

@@ -46,6 +46,10 @@
 #ifndef SPH_HYDRO_MARK_UNROLL
 #define SPH_HYDRO_MARK_UNROLL 8
 #endif
+// The double-float hydro pass (128 threads): 3 blocks per SM, 168 registers.
+#ifndef SPH_HYDRO_DF_MIN_BLOCKS
+#define SPH_HYDRO_DF_MIN_BLOCKS 3
+#endif
 #ifndef SPH_HYDRO_MIN_BLOCKS
 #define SPH_HYDRO_MIN_BLOCKS 4
 #endif
@@ -753,6 +757,7 @@ struct HydroArgs {
 // (~50-60 marked pairs are typical; a particle whose row overflows is summed
 // over its walk's whole list instead).
 constexpr int HYDRO_LIST_CAP = 128;
+static_assert(HYDRO_LIST_CAP % 4 == 0, "rows of marked pairs start 16-byte aligned");
 
 template <bool F64, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, F64 ? 1 : SPH_HYDRO_MIN_BLOCKS)
@@ -921,9 +926,12 @@ hydro_kernel(const HydroArgs a) {
             ri = (idi != s_id[wid][k]) ? rsqrt_r(r2) : (R)0;
         };
         // Every near entry: the signal velocity (hdr_hydro.hpp:368-372) and
-        // a mark when the pair is inside either support (r^2 min(1/h_i^2,
-        // 1/h_j^2) below 1 + 2e-5, so every pair with q_i < 1 or q_j < 1 is
-        // marked).  Unmarked pairs add exactly zero to every sum.
+        // a mark when the pair is inside either support (FP64: r^2
+        // min(1/h_i^2, 1/h_j^2) below 1 + 2e-5, so every pair with q_i < 1 or
+        // q_j < 1 is marked; FP32C: the test of mark_only below, so that a
+        // particle's row holds the same pairs whether or not its tiles skip
+        // their signal-velocity terms).  Unmarked pairs add exactly zero to
+        // every sum.
         auto signal = [&](int k, unsigned &msk) {
             R dx, dy, dz, ux, uy, uz, r2, ri;
             diffs(k, dx, dy, dz, ux, uy, uz, r2, ri);
@@ -931,9 +939,16 @@ hydro_kernel(const HydroArgs a) {
             const R wneg = w < (R)0 ? w : (R)0;
             const R vs = cs_i + s_p2[wid][k].w - (R)3 * wneg;
             vsmx = vs > vsmx ? vs : vsmx;
-            const R hj = s_p1[wid][k].w;
-            const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
-            if (!(r2 * hmin2 >= (R)1.00002)) msk |= 1u << (k & 31);
+            if constexpr (F64) {
+                const R hj = s_p1[wid][k].w;
+                const R hmin2 = hi2_i < hj * hj ? hi2_i : hj * hj;
+                if (!(r2 * hmin2 >= (R)1.00002)) msk |= 1u << (k & 31);
+            } else {
+                const float4 M = s_m[wid][k];
+                const float ex = xc - M.x, ey = yc - M.y, ez = zc - M.z;
+                const float lim = h2m_i > M.w ? h2m_i : M.w;
+                if (!(ex * ex + ey * ey + ez * ez >= lim)) msk |= 1u << (k & 31);
+            }
         };
         // the mark alone (tiles whose signal-velocity terms are skipped).
         // FP32C tests r^2 < max(h_i, h_j)^2 (1 + 2e-4) on the one-float item
@@ -1246,31 +1261,52 @@ hydro_kernel(const HydroArgs a) {
 
 // FP32C hydro, double-float pass over the marked-pair rows: one thread per
 // i-particle (particles in index order, so a warp's particles share most of
-// their neighbours in L1).  Rows that overflowed are left to hydro_df_sweep.
+// their neighbours in L1), two row entries at a time in the two halves of
+// packed f32x2 instructions (even and odd entries summed apart and combined
+// at the end), an odd last entry alone.  Rows that overflowed are left to
+// hydro_df_sweep.
 constexpr int HYDRO_DF_THREADS = 128;
-__global__ inline void __launch_bounds__(HYDRO_DF_THREADS) hydro_df_lists(const HydroArgs a) {
+__device__ __forceinline__ HydroDFP<float> hydro_df_load(const F32Part &f, const float4 *g1, const float4 *g2,
+                                                         const float4 *g3, const float4 *g4, int j) {
+    return hydro_df_rec(f.phi[j], f.plo[j], f.vhi[j], f.vlo[j], g1[j], g2[j], g3[j], g4[j]);
+}
+__device__ __forceinline__ void hydro_df_store(const HydroArgs &a, int p, const HydroDFAcc<float> &acc,
+                                               dfk::df presc) {
+    double h[3], g[3], ud, dif;
+    hydro_df_finish(acc, presc, CEFF1, h, g, &ud, &dif);
+    a.o_acch[3 * p + 0] = h[0];
+    a.o_acch[3 * p + 1] = h[1];
+    a.o_acch[3 * p + 2] = h[2];
+    a.o_accg[3 * p + 0] = g[0];
+    a.o_accg[3 * p + 1] = g[1];
+    a.o_accg[3 * p + 2] = g[2];
+    a.o_udot[p] = ud;
+    a.o_diffu[p] = dif;
+}
+__global__ inline void __launch_bounds__(HYDRO_DF_THREADS, SPH_HYDRO_DF_MIN_BLOCKS) hydro_df_lists(const HydroArgs a) {
+    using dfk::pk;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n_i; p += gridDim.x * blockDim.x) {
         const int c = a.df_cnt[p];
         if (c > a.df_cap) continue;
-        const HydroDFI I = hydro_df_i(a.fi.phi[p], a.fi.plo[p], a.fi.vhi[p], a.fi.vlo[p], a.fi_g1[p], a.fi_g2[p],
-                                      a.fi_g3[p], a.fi_g4[p]);
-        HydroDFAcc acc = hydro_df_zero();
+        const HydroDFP<float> I = hydro_df_load(a.fi, a.fi_g1, a.fi_g2, a.fi_g3, a.fi_g4, p);
+        const HydroDFP<pk> I2 = hydro_df_pack(I, I);
+        HydroDFAcc<pk> acc2 = hydro_df_zero<pk>();
+        HydroDFAcc<float> acc = hydro_df_zero<float>();
         const int *row = a.df_list + (size_t)p * a.df_cap;
-        for (int k = 0; k < c; ++k) {
-            const int j = row[k];
-            hydro_df_pair(I, a.fj.phi[j], a.fj.plo[j], a.fj.vhi[j], a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j],
-                          a.fj_g3[j], a.fj_g4[j], acc);
+        int k = 0;
+        for (; k + 1 < c; k += 2) {
+            const HydroDFP<float> J0 = hydro_df_load(a.fj, a.fj_g1, a.fj_g2, a.fj_g3, a.fj_g4, row[k]);
+            const HydroDFP<float> J1 = hydro_df_load(a.fj, a.fj_g1, a.fj_g2, a.fj_g3, a.fj_g4, row[k + 1]);
+            hydro_df_pair(I2, hydro_df_pack(J0, J1), acc2);
         }
-        double h[3], g[3], ud, dif;
-        hydro_df_finish(acc, I, CEFF1, h, g, &ud, &dif);
-        a.o_acch[3 * p + 0] = h[0];
-        a.o_acch[3 * p + 1] = h[1];
-        a.o_acch[3 * p + 2] = h[2];
-        a.o_accg[3 * p + 0] = g[0];
-        a.o_accg[3 * p + 1] = g[1];
-        a.o_accg[3 * p + 2] = g[2];
-        a.o_udot[p] = ud;
-        a.o_diffu[p] = dif;
+        if (k < c) hydro_df_pair(I, hydro_df_load(a.fj, a.fj_g1, a.fj_g2, a.fj_g3, a.fj_g4, row[k]), acc);
+        // (even + odd) + last, each addition renormalised
+        dfk::df *v[9] = {&acc.ax, &acc.ay, &acc.az, &acc.gx, &acc.gy, &acc.gz, &acc.ud, &acc.uv, &acc.dif};
+        const dfk::dv<pk> *w[9] = {&acc2.ax, &acc2.ay, &acc2.az, &acc2.gx, &acc2.gy, &acc2.gz,
+                                   &acc2.ud, &acc2.uv, &acc2.dif};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) *v[q] = dfk::add(dfk::add(lane0(*w[q]), lane1(*w[q])), *v[q]);
+        hydro_df_store(a, p, acc, I.presc);
     }
 }
 
@@ -1297,9 +1333,8 @@ __global__ inline void __launch_bounds__(HYDRO_SWEEP_THREADS) hydro_df_sweep(con
         const int p = ent.x, w = ent.y;
         const int jb = a.j_off[w], je = a.j_off[w + 1];
         const long long idi = a.i_id[p];
-        const HydroDFI I = hydro_df_i(a.fi.phi[p], a.fi.plo[p], a.fi.vhi[p], a.fi.vlo[p], a.fi_g1[p], a.fi_g2[p],
-                                      a.fi_g3[p], a.fi_g4[p]);
-        HydroDFAcc acc = hydro_df_zero();
+        const HydroDFP<float> I = hydro_df_load(a.fi, a.fi_g1, a.fi_g2, a.fi_g3, a.fi_g4, p);
+        HydroDFAcc<float> acc = hydro_df_zero<float>();
         const float hi2 = 1.0f / (I.hinv.h * I.hinv.h);
         for (int k = jb + threadIdx.x; k < je; k += HYDRO_SWEEP_THREADS) {
             const int j = a.j_idx ? a.j_idx[k] : k;
@@ -1311,7 +1346,8 @@ __global__ inline void __launch_bounds__(HYDRO_SWEEP_THREADS) hydro_df_sweep(con
             const float dz = (I.zh - ph.z) + (I.zl - pl.z);
             const float hj2 = 1.0f / (vh.w * vh.w);
             if (dx * dx + dy * dy + dz * dz > fmaxf(hi2, hj2) * 1.001f) continue;
-            hydro_df_pair(I, ph, pl, vh, a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j], a.fj_g3[j], a.fj_g4[j], acc);
+            hydro_df_pair(I, hydro_df_rec(ph, pl, vh, a.fj.vlo[j], a.fj_g1[j], a.fj_g2[j], a.fj_g3[j], a.fj_g4[j]),
+                          acc);
         }
         dfk::df *v[9] = {&acc.ax, &acc.ay, &acc.az, &acc.gx, &acc.gy, &acc.gz, &acc.ud, &acc.uv, &acc.dif};
 #pragma unroll
@@ -1327,14 +1363,7 @@ __global__ inline void __launch_bounds__(HYDRO_SWEEP_THREADS) hydro_df_sweep(con
                 for (int u = 1; u < NW; ++u) t = dfk::add(t, part[q][u]);
                 *v[q] = t;
             }
-            double h[3], g[3], ud, dif;
-            hydro_df_finish(acc, I, CEFF1, h, g, &ud, &dif);
-            for (int c = 0; c < 3; ++c) {
-                a.o_acch[3 * p + c] = h[c];
-                a.o_accg[3 * p + c] = g[c];
-            }
-            a.o_udot[p] = ud;
-            a.o_diffu[p] = dif;
+            hydro_df_store(a, p, acc, I.presc);
         }
         __syncthreads();   // part[] is rewritten by the next particle
     }
@@ -1705,9 +1734,9 @@ __global__ inline void make_hydro_records(int n, const dbl4 *pm, const dbl4 *vel
         const float2 u = df_split(v.x), w = df_split(v.y), s = df_split(v.z);
         const float2 P = df_split(a.y), T = df_split(c.x), Q = df_split(a.z);
         const double h4d = (a.x * a.x) * (a.x * a.x);
-        const float2 H = df_split(a.x), H4 = df_split(h4d);
-        phi[k] = make_float4(x.x, y.x, z.x, (float)p.w);
-        plo[k] = make_float4(x.y, y.y, z.y, 0.0f);
+        const float2 H = df_split(a.x), H4 = df_split(h4d), M = df_split(p.w);
+        phi[k] = make_float4(x.x, y.x, z.x, M.x);
+        plo[k] = make_float4(x.y, y.y, z.y, M.y);
         vhi[k] = make_float4(u.x, w.x, s.x, H.x);
         vlo[k] = make_float4(u.y, w.y, s.y, H4.x);
         g1[k] = make_float4(P.x, P.y, Q.x, (float)a.w);
