@@ -303,6 +303,8 @@ def run_ours(args):
     replicas.barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+    # phases of the last timed step, from the event-record nodes of its graph
+    phases_graph = ps.phase_times()
     st = ps.stats()
     pairs = {"density": st["pairs_density"], "hydro": st["pairs_hydro"], "gravity": st["pairs_gravity"]}
     # energy drift of the timed steps (FP64 sums of m (v^2/2 + u + pot/2))
@@ -405,6 +407,7 @@ def run_ours(args):
             "density_walks": st["density_iterations"],
             "parallelism": "replicas" if world > 1 else "single GPU",
             "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+            "phases_ms_step_graph": {k: round(v, 4) for k, v in phases_graph.items()},
             "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
                          "traffic": traffic,

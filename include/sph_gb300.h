@@ -507,9 +507,11 @@ int sph_system_get_lists(sph_system *sys, int32_t kind, int32_t *n_walk, int64_t
  * [7] the whole force evaluation, [8] and [9] the two parts of [6] (FP32C:
  * the signal-velocity / marking kernel and the double-float pass over the
  * marked pairs; FP64: the pair kernel and nothing).  Returns the number of
- * values written,
- * or minus a status code.  The events belong to eager evaluations
- * (sph_system_compute_forces and non-captured steps). */
+ * values written, or minus a status code.  Eager evaluations record the
+ * events directly; captured graphs (force evaluation and step) hold them as
+ * external event-record nodes, so the values after a graph replay are that
+ * replay's.  [3] runs on a second stream in captured graphs, overlapping
+ * [1]. */
 int sph_system_phase_times(sph_system *sys, float *ms, int32_t n);
 
 /* Kernel launches per replay of the captured graph: step = 1 for the

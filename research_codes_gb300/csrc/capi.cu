@@ -106,16 +106,20 @@ void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStr
 // FP32C: the signal-velocity / marking kernel, then the double-float pass
 // over the marked-pair rows and over the overflowed particles (a.df_novf
 // must be zero at launch; dfgrid: resident blocks of the double-float pass).
-// mid (optional) is recorded between the two.
+// mid (optional) is recorded between the two (as an external record node
+// when mid_external: inside a stream capture).
 void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid,
-                  cudaEvent_t mid) {
+                  cudaEvent_t mid, bool mid_external) {
+    auto record_mid = [&]() {
+        if (mid) cudaEventRecordWithFlags(mid, s, mid_external ? cudaEventRecordExternal : cudaEventRecordDefault);
+    };
     if (precision == SPH_PREC_FP64) {
         sphk::hydro_kernel<true, HYDRO64_WARPS><<<grid, HYDRO64_WARPS * 32, 0, s>>>(a);
-        if (mid) cudaEventRecord(mid, s);
+        record_mid();
         return;
     }
     sphk::hydro_kernel<false, PAIR_WARPS><<<grid, PAIR_WARPS * 32, 0, s>>>(a);
-    if (mid) cudaEventRecord(mid, s);
+    record_mid();
     if (a.n_i <= 0) return;
     const int need = (a.n_i + sphk::HYDRO_DF_THREADS - 1) / sphk::HYDRO_DF_THREADS;
     sphk::hydro_df_lists<<<std::max(1, std::min(need, dfgrid)), sphk::HYDRO_DF_THREADS, 0, s>>>(a);

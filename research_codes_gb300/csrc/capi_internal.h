@@ -167,6 +167,6 @@ int cuda_error(sph_context *ctx, cudaError_t e, const char *what);
 int pair_grid(const sph_context *ctx, int kind, int precision, int n_items);
 void launch_density(const sphk::DensityArgs &a, int precision, int grid, cudaStream_t s);
 void launch_hydro(const sphk::HydroArgs &a, int precision, int grid, cudaStream_t s, int dfgrid,
-                  cudaEvent_t mid = nullptr);
+                  cudaEvent_t mid = nullptr, bool mid_external = false);
 void launch_gravity(const sphk::GravityArgs &a, int precision, int grid, cudaStream_t s, int jtile);
 }  // namespace sphrt

@@ -654,44 +654,6 @@ __global__ void gravity_writeback(int n, double G, const double *acc, const doub
 }
 
 // HydroEPI/EPJ::copyFromFP, hdr_hydro.hpp:45-62 / 95-113 (umin = 0)
-// Largest sound speed over each hydro walk's j-list (one block per walk, -inf
-// for an empty list).  The signal velocity of every i-particle of the walk,
-// a maximum of cs_i + cs_j - 3 min(w, 0) over the list (hdr_hydro.hpp:368-372),
-// is at least its own sound speed plus this.
-constexpr int CSMAX_THREADS = 256;
-__global__ void __launch_bounds__(CSMAX_THREADS) walk_csmax(const int *n_walks, const int *j_off, const int *j_idx,
-                                                            const float4 *f_g2, const dbl4 *h2, double *out,
-                                                            const int *scal) {
-    __shared__ double red[CSMAX_THREADS / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (scal[S_ERROR] & (E_LISTCAP | E_STACK)) return;   // the lists overflowed (no hydro items either)
-    const int nw = *n_walks;
-    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
-        double m = -INFINITY;
-        const int e = j_off[w + 1];
-        // four entries per thread and round: their loads are in flight together
-        for (int k = j_off[w] + threadIdx.x; k < e; k += 4 * CSMAX_THREADS) {
-            int j[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int kk = k + u * CSMAX_THREADS;
-                j[u] = kk < e ? (j_idx ? j_idx[kk] : kk) : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (j[u] >= 0) m = fmax(m, f_g2 ? (double)f_g2[j[u]].y : h2[j[u]].y);   // NaN never raises it
-        }
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) red[warp] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int k = 1; k < CSMAX_THREADS / 32; ++k) m = fmax(m, red[k]);
-            out[w] = m;
-        }
-        __syncthreads();
-    }
-}
-
 __global__ void hydro_prep(int n, const double *ksr, const double *pres, const double *grdh,
                            const double *dens, const double *bswt, const double *vsnd, const double *alph,
                            const double *alphu, const double *uene, const double *eta, dbl4 *h1, dbl4 *h2,
@@ -1017,6 +979,16 @@ struct sph_system {
 
 namespace {
 
+// Phase event k on stream st.  Inside a capture it becomes an external
+// event-record node, so that every replay of the graph times its phases as
+// well (sph_system_phase_times after a captured step or evaluation).
+void phase_event(sph_system *s, int k, cudaStream_t st) {
+    if (s->capturing >= 0)
+        cudaEventRecordWithFlags(s->ev[k], st, cudaEventRecordExternal);
+    else
+        cudaEventRecord(s->ev[k], st);
+}
+
 int alloc_all(sph_system *s) {
     const size_t n = (size_t)s->n;
     const size_t nn = 2 * n;
@@ -1144,7 +1116,7 @@ int build_tree(sph_system *s) {
     int r0 = SPH_OK;
     const int n = s->n;
     cudaStream_t st = s->st();
-    cudaEventRecord(s->ev[EV_TREE_B], st);
+    phase_event(s, EV_TREE_B, st);
     bbox_stage1<<<RED_BLOCKS, RED_THREADS, 0, st>>>(s->pos[0].p, n, s->partial.p);
     bbox_stage2<<<1, 32 * 6, 0, st>>>(s->partial.p, RED_BLOCKS, s->box.p);
     sphtree::morton_keys<<<grid_for(n), 256, 0, st>>>(s->pos[0].p, n, s->box.p, s->keys[0].p, s->perm[0].p);
@@ -1183,7 +1155,7 @@ int build_tree(sph_system *s) {
     if (r) return r;
     compact_groups<<<grid_for(n), 256, 0, st>>>(n, s->gflag.p, s->gscan.p, s->groot.p, t, s->group_node.p,
                                                 s->group_first.p, s->group_count.p, s->scal.p);
-    cudaEventRecord(s->ev[EV_TREE_E], st);
+    phase_event(s, EV_TREE_E, st);
     return SPH_OK;
 }
 
@@ -1238,9 +1210,12 @@ __global__ void pool_usage(int *scal) {
 // Builds the lists of `kind` over the walks (group nodes + radii) and the
 // matching work items.  In eager mode (no capture) the list capacity grows to
 // the counted total first.
+// csmax (symmetric lists, optional): the largest sound speed over each
+// walk's list (cs_f4[j].y or cs_d4[j].y), taken while the lists are copied.
 int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const double *walk_r, bool eager,
                           long long *pairs, const int *item_first = nullptr, const int *item_count = nullptr,
-                          int chunk = 32) {
+                          int chunk = 32, double *csmax = nullptr, const float4 *cs_f4 = nullptr,
+                          const dbl4 *cs_d4 = nullptr) {
     const int n = s->n;
     cudaStream_t st = s->st();
     const int builder = kind == 2 ? 1 : 0;
@@ -1346,6 +1321,12 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // 3. the chunks to their list offsets
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
+    if (csmax) {
+        CUDA_TRY(cudaMemsetAsync(csmax, 0, sizeof(double) * (size_t)n, st));   // +0.0
+        a.csmax_bits = reinterpret_cast<unsigned long long *>(csmax);
+        a.cs_f4 = cs_f4;
+        a.cs_d4 = cs_d4;
+    }
     sphtree::copy_lists<<<s->ctx->sm_count * 8, sphtree::COPY_THREADS, 0, st>>>(a);
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
@@ -1433,9 +1414,9 @@ int density_walk(sph_system *s, int it, bool eager, cudaGraphConditionalHandle c
     a.amb_cap = s->amb_cap;
     a.amb_tol = sphrt::AMB_TOL;
     if (f32) CUDA_TRY(cudaMemsetAsync(s->scal.p + S_AMB, 0, sizeof(int), st));
-    if (first) cudaEventRecord(s->ev[EV_DENSK_B], st);
+    if (first) phase_event(s, EV_DENSK_B, st);
     sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
-    if (first) cudaEventRecord(s->ev[EV_DENSK_E], st);
+    if (first) phase_event(s, EV_DENSK_E, st);
     if (f32) {
         // FP64 recomputation of decision-ambiguous particles (same lists)
         sphk::make_fixup_items<<<8, 256, 0, st>>>(s->scal.p + S_AMB, s->amb_w.p, s->amb_cap, s->fitems.p,
@@ -1515,7 +1496,7 @@ int density_phase(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
-    cudaEventRecord(s->ev[EV_DENS_B], st);
+    phase_event(s, EV_DENS_B, st);
     const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
     if (f32)
         sphk::make_density_records<<<grid_for(n), 256, 0, st>>>(n, s->pos[0].p, s->vel[0].p, s->f_phi.p,
@@ -1553,7 +1534,7 @@ int density_phase(sph_system *s, bool eager) {
             return rr;
         }
     }
-    cudaEventRecord(s->ev[EV_DENS_E], st);
+    phase_event(s, EV_DENS_E, st);
     return SPH_OK;
 }
 
@@ -1577,12 +1558,12 @@ int gravity_lists(sph_system *s, bool eager) {
         s->st_override = s->side_stream;
     }
     const cudaStream_t st = s->st();
-    cudaEventRecord(s->ev[EV_GLIST_B], st);
+    phase_event(s, EV_GLIST_B, st);
     int r = SPH_OK;
     const cudaError_t em = cudaMemsetAsync(s->ls[1].sc, 0, sizeof(int) * S_NI, st);
     if (em != cudaSuccess) r = sphrt::cuda_error(s->ctx, em, "cudaMemsetAsync");
     if (!r) r = build_lists_and_items(s, 2, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_G);
-    cudaEventRecord(s->ev[EV_GLIST_E], st);
+    phase_event(s, EV_GLIST_E, st);
     if (s->glist_forked) {
         const cudaError_t ej = cudaEventRecord(s->ev_join, s->side_stream);
         s->st_override = prev;
@@ -1604,7 +1585,7 @@ int gravity_phase(sph_system *s) {
                                                                           s->f_shi.p, s->f_slo.p);
     }
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
-    cudaEventRecord(s->ev[EV_GK_B], st);
+    phase_event(s, EV_GK_B, st);
     sphk::GravityArgs a{};
     a.i_pe = s->pe.p;
     a.j_pm = s->pos[0].p; a.j_eps2 = s->eps2.p;
@@ -1624,7 +1605,7 @@ int gravity_phase(sph_system *s) {
     const int jt = (ctx->prm.precision == SPH_PREC_FP32C && s->prm.gravity_jtile == 64) ? 64 : 32;
     sphrt::launch_gravity(a, ctx->prm.precision,
                           jt == 64 ? ctx->grid_g64 : ctx->grid[2][ctx->prm.precision == SPH_PREC_FP64], st, jt);
-    cudaEventRecord(s->ev[EV_GK_E], st);
+    phase_event(s, EV_GK_E, st);
     gravity_writeback<<<grid_for(n), 256, 0, st>>>(n, s->prm.G, s->r_acc.p, s->r_pot.p, s->r_eta.p, s->ksr[0].p,
                                                    s->grdh.p, s->dens.p, s->accg2.p, s->pot.p, s->eta.p,
                                                    ctx->prm.precision == SPH_PREC_FP32C);
@@ -1635,7 +1616,7 @@ int hydro_phase(sph_system *s, bool eager) {
     const int n = s->n;
     cudaStream_t st = s->st();
     sph_context *ctx = s->ctx;
-    cudaEventRecord(s->ev[EV_HLIST_B], st);
+    phase_event(s, EV_HLIST_B, st);
     hydro_prep<<<grid_for(n), 256, 0, st>>>(n, s->ksr[0].p, s->pres.p, s->grdh.p, s->dens.p, s->bswt.p,
                                             s->vsnd.p, s->alph[0].p, s->alphu[0].p, s->uene[0].p, s->eta.p,
                                             s->h1.p, s->h2.p, s->h3.p, ctx->prm.precision == SPH_PREC_FP32C);
@@ -1644,15 +1625,16 @@ int hydro_phase(sph_system *s, bool eager) {
                                                               s->h3.p, s->f_phi.p, s->f_plo.p, s->f_vhi.p,
                                                               s->f_vlo.p, s->f_g1.p, s->f_g2.p, s->f_g3.p,
                                                               s->f_g4.p);
-    int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
-    if (r) return r;
     const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
     const bool skip = s->prm.hydro_signal_skip != 0;
-    if (skip)
-        walk_csmax<<<ctx->sm_count * 8, CSMAX_THREADS, 0, st>>>(s->walk_num[1], s->loff[1].p, s->jidx[1].p,
-                                                     f32 ? s->f_g2.p : nullptr, s->h2.p, s->w_csmax.p, s->scal.p);
+    // with the skip, the largest sound speed of every walk's list is taken
+    // as the lists are copied: the signal velocity of each i-particle of the
+    // walk is at least its own sound speed plus it (hdr_hydro.hpp:368-372)
+    int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H, nullptr, nullptr,
+                                  32, skip ? s->w_csmax.p : nullptr, f32 ? s->f_g2.p : nullptr, s->h2.p);
+    if (r) return r;
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
-    cudaEventRecord(s->ev[EV_HK_B], st);
+    phase_event(s, EV_HK_B, st);
     sphk::HydroArgs a{};
     a.n_eval_near = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HN);
     a.n_eval_far = reinterpret_cast<unsigned long long *>(s->lscal.p + L_EVAL_HF);
@@ -1683,8 +1665,8 @@ int hydro_phase(sph_system *s, bool eager) {
         CUDA_TRY(cudaMemsetAsync(s->scal.p + S_HOVF, 0, sizeof(int), st));
     }
     sphrt::launch_hydro(a, ctx->prm.precision, ctx->grid[1][ctx->prm.precision == SPH_PREC_FP64], st,
-                        ctx->grid_df, s->ev[EV_HK_MID]);
-    cudaEventRecord(s->ev[EV_HK_E], st);
+                        ctx->grid_df, s->ev[EV_HK_MID], s->capturing >= 0);
+    phase_event(s, EV_HK_E, st);
     AlphaParams ap{s->prm.alpha_max, s->prm.alpha_min, s->prm.alphu_max, s->prm.alphu_min};
     hydro_writeback<<<grid_for(n), 256, 0, st>>>(
         n, s->prm.G, s->r_acch.p, s->r_accg.p, s->r_udot.p, s->r_vsmx.p, s->r_diffu.p, s->acch.p, s->accg1.p,
@@ -1734,7 +1716,7 @@ int force_body(sph_system *s, bool eager, bool energy = true) {
         fe.pos = s->pos[0].p; fe.vel = s->vel[0].p; fe.uene = s->uene[0].p; fe.pot = s->pot.p;
         reduce(s, fe, s->dscal.p + D_EKIN);
     }
-    cudaEventRecord(s->ev[EV_END], st);
+    phase_event(s, EV_END, st);
     return SPH_OK;
 }
 

@@ -262,6 +262,27 @@ def test_graph_replay_equals_eager_steps():
     assert out[0][3]["time"] == out[1][3]["time"]
 
 
+def test_phase_times_of_a_captured_step():
+    """The phase events are record nodes of the captured graphs: after a
+    replay every phase has a positive device time and the parts fit inside
+    the whole force evaluation; the step graph's own events are timed."""
+    s = _two_stars(n=3000)
+    with functors.Context(eta=1.18) as ctx:
+        sys = ParticleSystem(ctx, len(s["mass"]), n_group=64, use_graph=1)
+        sys.upload(s)
+        sys.compute_forces()
+        sys.step(3)
+        ph = sys.phase_times()
+        assert sys.graph_kernels(step=True) > 0
+        assert all(v > 0.0 for v in ph.values()), ph
+        total = ph["force_total"]
+        for k in ("tree", "density", "gravity_kernel", "hydro_lists", "hydro_kernel"):
+            assert ph[k] <= total, (k, ph)
+        assert ph["density_kernel"] <= ph["density"]
+        assert abs(ph["hydro_signal"] + ph["hydro_df"] - ph["hydro_kernel"]) <= 0.05 * ph["hydro_kernel"] + 1e-3
+        sys.close()
+
+
 @pytest.mark.parametrize("prec", ["fp32c", "fp64"])
 def test_energy_conservation_short_run(prec):
     s = _star(n=3000, seed=4, spin=False)
