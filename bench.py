@@ -502,16 +502,16 @@ def run_ours(args):
         ps.upload(pin)
         ps.compute_forces()            # captures the force-evaluation graph
         torch.cuda.synchronize()
-        pairs_e = 0
         t = time.perf_counter()
         for _ in range(ke):
             ps.upload(pin)
             ps.compute_forces()
             ps.download("acc", out=out_acc)
             ps.download("udot", out=out_udot)
-            ste = ps.stats()
-            pairs_e += ste["pairs_density"] + ste["pairs_hydro"] + ste["pairs_gravity"]
         el = time.perf_counter() - t
+        # every timed evaluation is of the same uploaded state: its pairs
+        ste = ps.stats()
+        pairs_e = ke * (ste["pairs_density"] + ste["pairs_hydro"] + ste["pairs_gravity"])
         line["e2e"] = {"value": el / ke, "unit": "s/step", "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * el / ke,
                        "interactions_per_s": pairs_e / el,

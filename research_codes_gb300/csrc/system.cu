@@ -653,6 +653,44 @@ __global__ void gravity_writeback(int n, double G, const double *acc, const doub
     }
 }
 
+// Largest sound speed over each hydro walk's j-list (one block per walk, -inf
+// for an empty list).  The signal velocity of every i-particle of the walk,
+// a maximum of cs_i + cs_j - 3 min(w, 0) over the list (hdr_hydro.hpp:368-372),
+// is at least its own sound speed plus this.
+constexpr int CSMAX_THREADS = 256;
+__global__ void __launch_bounds__(CSMAX_THREADS) walk_csmax(const int *n_walks, const int *j_off, const int *j_idx,
+                                                            const float4 *f_g2, const dbl4 *h2, double *out,
+                                                            const int *scal) {
+    __shared__ double red[CSMAX_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (scal[S_ERROR] & (E_LISTCAP | E_STACK)) return;   // the lists overflowed (no hydro items either)
+    const int nw = *n_walks;
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+        double m = -INFINITY;
+        const int e = j_off[w + 1];
+        // four entries per thread and round: their loads are in flight together
+        for (int k = j_off[w] + threadIdx.x; k < e; k += 4 * CSMAX_THREADS) {
+            int j[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int kk = k + u * CSMAX_THREADS;
+                j[u] = kk < e ? (j_idx ? j_idx[kk] : kk) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j[u] >= 0) m = fmax(m, f_g2 ? (double)f_g2[j[u]].y : h2[j[u]].y);   // NaN never raises it
+        }
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) red[warp] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 1; k < CSMAX_THREADS / 32; ++k) m = fmax(m, red[k]);
+            out[w] = m;
+        }
+        __syncthreads();
+    }
+}
+
 // HydroEPI/EPJ::copyFromFP, hdr_hydro.hpp:45-62 / 95-113 (umin = 0)
 __global__ void hydro_prep(int n, const double *ksr, const double *pres, const double *grdh,
                            const double *dens, const double *bswt, const double *vsnd, const double *alph,
@@ -1210,12 +1248,9 @@ __global__ void pool_usage(int *scal) {
 // Builds the lists of `kind` over the walks (group nodes + radii) and the
 // matching work items.  In eager mode (no capture) the list capacity grows to
 // the counted total first.
-// csmax (symmetric lists, optional): the largest sound speed over each
-// walk's list (cs_f4[j].y or cs_d4[j].y), taken while the lists are copied.
 int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const double *walk_r, bool eager,
                           long long *pairs, const int *item_first = nullptr, const int *item_count = nullptr,
-                          int chunk = 32, double *csmax = nullptr, const float4 *cs_f4 = nullptr,
-                          const dbl4 *cs_d4 = nullptr) {
+                          int chunk = 32) {
     const int n = s->n;
     cudaStream_t st = s->st();
     const int builder = kind == 2 ? 1 : 0;
@@ -1321,12 +1356,6 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     // 3. the chunks to their list offsets
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
-    if (csmax) {
-        CUDA_TRY(cudaMemsetAsync(csmax, 0, sizeof(double) * (size_t)n, st));   // +0.0
-        a.csmax_bits = reinterpret_cast<unsigned long long *>(csmax);
-        a.cs_f4 = cs_f4;
-        a.cs_d4 = cs_d4;
-    }
     sphtree::copy_lists<<<s->ctx->sm_count * 8, sphtree::COPY_THREADS, 0, st>>>(a);
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
@@ -1625,14 +1654,13 @@ int hydro_phase(sph_system *s, bool eager) {
                                                               s->h3.p, s->f_phi.p, s->f_plo.p, s->f_vhi.p,
                                                               s->f_vlo.p, s->f_g1.p, s->f_g2.p, s->f_g3.p,
                                                               s->f_g4.p);
+    int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H);
+    if (r) return r;
     const bool f32 = ctx->prm.precision == SPH_PREC_FP32C;
     const bool skip = s->prm.hydro_signal_skip != 0;
-    // with the skip, the largest sound speed of every walk's list is taken
-    // as the lists are copied: the signal velocity of each i-particle of the
-    // walk is at least its own sound speed plus it (hdr_hydro.hpp:368-372)
-    int r = build_lists_and_items(s, 1, s->group_node.p, nullptr, eager, s->lscal.p + L_PAIRS_H, nullptr, nullptr,
-                                  32, skip ? s->w_csmax.p : nullptr, f32 ? s->f_g2.p : nullptr, s->h2.p);
-    if (r) return r;
+    if (skip)
+        walk_csmax<<<ctx->sm_count * 8, CSMAX_THREADS, 0, st>>>(s->walk_num[1], s->loff[1].p, s->jidx[1].p,
+                                                     f32 ? s->f_g2.p : nullptr, s->h2.p, s->w_csmax.p, s->scal.p);
     CUDA_TRY(cudaMemsetAsync(s->scal.p + S_QUEUE, 0, sizeof(int), st));
     phase_event(s, EV_HK_B, st);
     sphk::HydroArgs a{};

@@ -536,13 +536,6 @@ struct ListArgs {
     int *chain;
     int chain_max;
     int *pool_error;
-    // symmetric lists, optional: the largest sound speed over each group's
-    // list, taken while copy_lists moves it (cs_f4[j].y in FP32C, cs_d4[j].y
-    // in FP64), into csmax_bits[group] as the bits of a non-negative double
-    // (atomicMax; zeroed before the copy)
-    const float4 *cs_f4 = nullptr;
-    const dbl4 *cs_d4 = nullptr;
-    unsigned long long *csmax_bits = nullptr;
 };
 
 constexpr int LIST_CHUNK = 128;   // entries per pool chunk (a multiple of 32)
@@ -907,30 +900,15 @@ __global__ void __launch_bounds__(COPY_THREADS) copy_lists(ListArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.error, 2);
         return;
     }
-    __shared__ double red[COPY_THREADS / 32];
     for (int task = blockIdx.x; task < n_tasks; task += gridDim.x) {
         const int total = a.count_out[task];
         const long long off = a.offset[task];
         const int *chain = a.chain + (size_t)task * a.chain_max;
-        double m = 0.0;
         for (int k = threadIdx.x; k < total; k += COPY_THREADS) {
             const int ch = chain[k / LIST_CHUNK];
             const long long w = off + k;
-            const int j = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
-            if (w >= 0 && w < a.capacity) a.j_idx[w] = j;
+            if (w >= 0 && w < a.capacity) a.j_idx[w] = a.pool[(size_t)ch * LIST_CHUNK + (k % LIST_CHUNK)];
             else atomicOr(a.error, 2);
-            if (a.csmax_bits && j >= 0 && j < a.n)
-                m = fmax(m, a.cs_f4 ? (double)a.cs_f4[j].y : a.cs_d4[j].y);   // NaN never raises it
-        }
-        if (a.csmax_bits) {
-            for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(FULL, m, o));
-            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int q = 1; q < COPY_THREADS / 32; ++q) m = fmax(m, red[q]);
-                atomicMax(&a.csmax_bits[a.tasks[task].x], (unsigned long long)__double_as_longlong(m));
-            }
-            __syncthreads();
         }
     }
 }
