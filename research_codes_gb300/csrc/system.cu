@@ -47,7 +47,7 @@ constexpr int MAX_RED = 8;
 constexpr long long MAX_POOL_CHUNKS = 0x7fffffffLL / sphtree::LIST_CHUNK;
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_POOLMAX, S_HOVF, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
+       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_TQUEUE, S_POOLMAX, S_HOVF, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -1292,6 +1292,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.offset = L.tloff.p;
     a.pool_next = sc + S_POOL;
     a.pool_error = sc + S_POOLERR;
+    a.task_queue = sc + S_TQUEUE;
     // one traversal: counts per task and the entries into pool chunks; in
     // eager mode the pool and the chains grow until they hold the lists with
     // a quarter of headroom (graph replays cannot allocate)
@@ -1301,7 +1302,7 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
         a.chain = L.lchain.p;
         a.chain_max = L.lchain_max;
         CUDA_TRY(cudaMemsetAsync(L.tlcnt.p, 0, sizeof(int) * (size_t)(L.task_cap + 1), st));
-        CUDA_TRY(cudaMemsetAsync(sc + S_POOL, 0, 2 * sizeof(int), st));
+        CUDA_TRY(cudaMemsetAsync(sc + S_POOL, 0, 3 * sizeof(int), st));   // pool, pool error, task queue
         launch_lists(mode, tgrid, a, st);
         pool_usage<<<1, 1, 0, st>>>(sc);
         if (!eager) break;

@@ -536,6 +536,7 @@ struct ListArgs {
     int *chain;
     int chain_max;
     int *pool_error;
+    int *task_queue;        // next task to traverse (0 at launch): warps take tasks as they finish
 };
 
 constexpr int LIST_CHUNK = 128;   // entries per pool chunk (a multiple of 32)
@@ -726,9 +727,15 @@ __global__ void __launch_bounds__(TRAV_WARPS * 32) build_lists(ListArgs a) {
     const int wid = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int n_tasks = *a.n_tasks;
-    const int warps = gridDim.x * TRAV_WARPS;
     const float slack = coord_slack(a.box);
-    for (int task = blockIdx.x * TRAV_WARPS + wid; task < n_tasks; task += warps) {
+    // tasks differ in length: each warp takes the next one when it is done
+    // (the lists do not depend on the order, each task writing its own chunks)
+    auto next_task = [&]() {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(a.task_queue, 1);
+        return __shfl_sync(FULL, t, 0);
+    };
+    for (int task = next_task(); task < n_tasks; task = next_task()) {
         const int2 tk = a.tasks[task];
         const int g = tk.x;
         const int gn = a.group_node[g];
