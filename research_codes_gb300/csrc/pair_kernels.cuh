@@ -690,6 +690,201 @@ density_kernel(const DensityArgs a) {
     }
 }
 
+// Re-walks of few particles (the search-radius loop of hdr_density.hpp:
+// 382-414 late in its course: typically a handful of particles whose h
+// grew past 1.1^k times its first guess).  density_kernel gives such a walk
+// one warp, which streams the walk's list 32 entries at a time and waits on
+// every chunk's loads; here one block takes a walk and evaluates its
+// iterating particles one after another, every pass spreading the whole
+// list over the block's threads.  Same pair terms, per-particle updates,
+// search-radius decision, ambiguity queue and outputs as density_kernel
+// (for a one-particle item: positions relative to the particle itself);
+// each thread sums its entries (FP32C: Kahan) and the block adds the
+// threads' sums in FP64.  Runs only when *small is set (the caller then
+// leaves density_kernel no items).
+constexpr int REWALK_THREADS = 256;
+template <int N>
+__device__ __forceinline__ void block_sum(double (&v)[N], double (*red)[REWALK_THREADS / 32]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(FULL, v[q], o);
+        if (lane == 0) red[q][wid] = v[q];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+        double t = 0.0;
+        for (int u = 0; u < REWALK_THREADS / 32; ++u) t += red[q][u];
+        v[q] = t;
+    }
+    __syncthreads();
+}
+template <bool F64>
+__global__ void __launch_bounds__(REWALK_THREADS) density_rewalk_blocks(const DensityArgs a, const int *n_walks,
+                                                                       const int *seg_first, const int *seg_count,
+                                                                       const int *small) {
+    typedef typename Real<F64>::T R;
+    __shared__ double red[6][REWALK_THREADS / 32];
+    if (!*small) return;
+    const int nw = *n_walks;
+    const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
+    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+        const int jb = a.j_off[w], je = a.j_off[w + 1];
+        for (int s = 0; s < seg_count[w]; ++s) {
+            const int ii = a.i_list[seg_first[w] + s];
+            float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
+            dbl4 ci = make_dbl4(0, 0, 0, 0);
+            if (F64) ci = a.i_pm[ii];
+            else { cph = a.fi.phi[ii]; cpl = a.fi.plo[ii]; }
+            // position of j relative to i (FP32C) or absolute (FP64), and its mass
+            auto rel = [&](int j, R &dx, R &dy, R &dz) -> R {
+                if constexpr (F64) {
+                    const dbl4 p = a.j_pm[j];
+                    dx = (R)ci.x - (R)p.x; dy = (R)ci.y - (R)p.y; dz = (R)ci.z - (R)p.z;
+                    return (R)p.w;
+                } else {
+                    const float4 ph = a.fj.phi[j], pl = a.fj.plo[j];
+                    dx = -df_diff(ph.x, pl.x, cph.x, cpl.x);
+                    dy = -df_diff(ph.y, pl.y, cph.y, cpl.y);
+                    dz = -df_diff(ph.z, pl.z, cph.z, cpl.z);
+                    return (R)ph.w;
+                }
+            };
+            double h = a.i_ksr[ii];
+            const double mi = a.i_pm[ii].w;
+            R rho = 0;
+            long long np = 0;
+            // three fixed-point passes, hdr_density.hpp:264-302
+            for (int pass = 0; pass < 3; ++pass) {
+                const R hinv = (R)1 / (R)h;
+                const R hinv2 = hinv * hinv;
+                Acc<F64> acc;
+                long long cnt = 0;
+                for (int k = jb + threadIdx.x; k < je; k += REWALK_THREADS) {
+                    const int j = a.j_idx ? a.j_idx[k] : k;
+                    R dx, dy, dz;
+                    const R m = rel(j, dx, dy, dz);
+                    const R q = sqrt_q(dx * dx + dy * dy + dz * dz, hinv2);
+                    const R u = max0((R)1 - q);
+                    const R u2 = u * u;
+                    if (pass == 2) cnt += (q < (R)1) ? 1 : 0;
+                    acc.add(m * (u2 * u2 * ((R)1 + (R)4 * q)));
+                }
+                double v[2] = {acc.value(), (double)cnt};
+                block_sum(v, red);
+                double hn;
+                if (F64) {
+                    const double hinv_d = 1.0 / h;
+                    rho = (R)(CEFF0 * hinv_d * hinv_d * hinv_d * v[0]);
+                    hn = a.eta_ksrh * cbrt(mi / (double)rho);
+                } else {
+                    const float hinv_f = (float)hinv;
+                    const float rho_f = (float)CEFF0 * hinv_f * hinv_f * hinv_f * (float)v[0];
+                    rho = (R)rho_f;
+                    hn = (double)((float)a.eta_ksrh * cbrtf((float)mi / rho_f));
+                }
+                hn = (hn < ksr_max) ? hn : ksr_max;
+                np = (long long)v[1];
+                h = hn;
+            }
+            // the search-radius decision of the last pass (hdr_density.hpp:299)
+            const double rs_i = a.i_rs[ii];
+            const bool itr = h > rs_i;
+            if (!F64 && a.amb_count && threadIdx.x == 0 && fabs(h - rs_i) <= (double)a.amb_tol * rs_i) {
+                const int q = atomicAdd(a.amb_count, 1);
+                if (q < a.amb_cap) {
+                    a.amb_i[q] = ii;
+                    a.amb_w[q] = w;
+                }
+            }
+            // gradient pass with the final h, hdr_density.hpp:304-349
+            const long long idi = a.i_id[ii];
+            R vxi, vyi, vzi;
+            float lxi = 0.0f, lyi = 0.0f, lzi = 0.0f;
+            if (F64) {
+                const dbl4 vv = a.i_vel[ii];
+                vxi = (R)vv.x; vyi = (R)vv.y; vzi = (R)vv.z;
+            } else {
+                const float4 vh = a.fi.vhi[ii], vl = a.fi.vlo[ii];
+                vxi = vh.x; vyi = vh.y; vzi = vh.z;
+                lxi = vl.x; lyi = vl.y; lzi = vl.z;
+            }
+            const R hinv = (R)1 / (R)h;
+            Acc<F64> g_acc, d_acc, rx_acc, ry_acc, rz_acc;
+            for (int k = jb + threadIdx.x; k < je; k += REWALK_THREADS) {
+                const int j = a.j_idx ? a.j_idx[k] : k;
+                R dx, dy, dz;
+                const R m = rel(j, dx, dy, dz);
+                R ux, uy, uz;
+                if constexpr (F64) {
+                    const dbl4 vv = a.j_vel[j];
+                    ux = vxi - (R)vv.x; uy = vyi - (R)vv.y; uz = vzi - (R)vv.z;
+                } else {
+                    const float4 vh = a.fj.vhi[j], vl = a.fj.vlo[j];
+                    ux = vxi - vh.x; uy = vyi - vh.y; uz = vzi - vh.z;
+                    ux += (R)(lxi - vl.x);
+                    uy += (R)(lyi - vl.y);
+                    uz += (R)(lzi - vl.z);
+                }
+                const R r2 = dx * dx + dy * dy + dz * dz;
+                const R ri = (idi != a.j_id[j]) ? rsqrt_r(r2) : (R)0;
+                const R q = r2 * ri * hinv;
+                const R u = max0((R)1 - q);
+                const R u2 = u * u;
+                const R u3 = u2 * u;
+                const R p14 = (R)1 + (R)4 * q;
+                const R w0 = u2 * u2 * p14;
+                const R w1 = w1_term(q, u, u2, u3, p14);
+                g_acc.add(m * ((R)(3.0 * CEFF0) * w0 + (R)CEFF1 * q * w1));
+                const R dw = m * w1 * ri;
+                d_acc.add((ux * dx + uy * dy + uz * dz) * dw);
+                rx_acc.add((uy * dz - uz * dy) * dw);
+                ry_acc.add((uz * dx - ux * dz) * dw);
+                rz_acc.add((ux * dy - uy * dx) * dw);
+            }
+            double v[5] = {g_acc.value(), d_acc.value(), rx_acc.value(), ry_acc.value(), rz_acc.value()};
+            block_sum(v, red);
+            if (threadIdx.x == 0) {
+                const double sg = v[0], sd = v[1], sx = v[2], sy = v[3], sz = v[4];
+                double divv, rotv, omega;
+                if (F64) {
+                    const double hinv_d = 1.0 / h;
+                    const double hinv4 = hinv_d * hinv_d * hinv_d * hinv_d;
+                    const double grdh = -hinv4 * sg;
+                    const double rx = CEFF1 * hinv4 * sx, ry = CEFF1 * hinv4 * sy, rz = CEFF1 * hinv4 * sz;
+                    const double rhoinv = 1.0 / (double)rho;
+                    omega = 1.0 / (1.0 + h * rhoinv * grdh / 3.0);
+                    const double rot2 = rx * rx + ry * ry + rz * rz;
+                    const double rot = (rot2 != 0.0) ? sqrt(rot2) : 0.0;
+                    divv = -CEFF1 * hinv4 * sd * rhoinv * omega;
+                    rotv = rot * rhoinv * omega;
+                } else {
+                    const float hf = (float)h;
+                    const float hinv_f = 1.0f / hf;
+                    const float hinv4 = hinv_f * hinv_f * hinv_f * hinv_f;
+                    const float rinv = 1.0f / (float)rho;
+                    const float g = -hinv4 * (float)sg;
+                    const float xf = (float)CEFF1 * hinv4 * (float)sx, yf = (float)CEFF1 * hinv4 * (float)sy,
+                                zf = (float)CEFF1 * hinv4 * (float)sz;
+                    const float om = 1.0f / (1.0f + hf * rinv * g / 3.0f);
+                    const float rot2 = xf * xf + yf * yf + zf * zf;
+                    omega = om;
+                    divv = -(float)CEFF1 * hinv4 * (float)sd * rinv * om;
+                    rotv = ((rot2 != 0.0f) ? sqrtf(rot2) : 0.0f) * rinv * om;
+                }
+                a.o_dens[ii] = (double)rho;
+                a.o_divv[ii] = divv;
+                a.o_rotv[ii] = rotv;
+                a.o_grdh[ii] = omega;
+                a.o_ksr[ii] = h;
+                a.o_np[ii] = np;
+                a.o_itr[ii] = itr ? 1 : 0;
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------- hydro
 struct HydroArgs {
     // FP64 mode records

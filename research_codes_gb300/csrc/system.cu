@@ -47,7 +47,8 @@ constexpr int MAX_RED = 8;
 constexpr long long MAX_POOL_CHUNKS = 0x7fffffffLL / sphtree::LIST_CHUNK;
 constexpr int NBKT = 32;   // cost classes of work items (log2 of the estimated cost)
 enum { S_NGROUPS = 0, S_NACTIVE, S_NITEMS, S_QUEUE, S_ERROR, S_UNCONV, S_TOTAL, S_ITERS, S_AMB, S_NFIX, S_AMBTOT,
-       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_TQUEUE, S_POOLMAX, S_HOVF, S_BKT, S_NI = S_BKT + 2 * NBKT + 2 };
+       S_NTASKS, S_NROOTS, S_POOL, S_POOLERR, S_TQUEUE, S_POOLMAX, S_HOVF, S_SMALL, S_BKT,
+       S_NI = S_BKT + 2 * NBKT + 2 };
 // double scalars
 enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN, D_ETHM, D_EPOT,
        D_R2, D_DN, D_NI };
@@ -524,6 +525,17 @@ __global__ void scatter_list(int n, const int *flag, const int *scan, int *list)
     GRID_STRIDE(p, n) {
         if (flag[p]) list[scan[p]] = p;
     }
+}
+
+// Re-walks with at most REWALK_SMALL iterating particles run on
+// density_rewalk_blocks (a block per walk) instead of density_kernel.
+constexpr int REWALK_SMALL = 1024;
+__global__ void rewalk_small(int n, const int *flag, const int *scan, int *scal) {
+    const int total = scan[n - 1] + flag[n - 1];
+    scal[S_SMALL] = (total <= REWALK_SMALL) ? 1 : 0;
+}
+__global__ void drop_items_if_small(int *scal) {
+    if (scal[S_SMALL]) scal[S_NITEMS] = 0;
 }
 
 // the index-list segment of each active walk
@@ -1412,6 +1424,7 @@ int density_walk(sph_system *s, int it, bool eager, cudaGraphConditionalHandle c
     scatter_list<<<grid_for(n), 256, 0, st>>>(n, s->uflag.p, s->uscan.p, s->ulist.p);
     walk_segments<<<grid_for(n), 256, 0, st>>>(n, s->scal.p, s->a_first.p, s->a_count.p, s->uflag.p,
                                                s->uscan.p, s->a_sfirst.p, s->a_scount.p);
+    if (!first) rewalk_small<<<1, 1, 0, st>>>(n, s->uflag.p, s->uscan.p, s->scal.p);
     const int kind = first ? 0 : 3;
     r = build_lists_and_items(s, kind, s->a_node.p, s->a_r.p, eager, s->lscal.p + (first ? L_PAIRS_D1 : L_PAIRS_D),
                               s->a_sfirst.p, s->a_scount.p, first ? 32 : 8);
@@ -1445,7 +1458,18 @@ int density_walk(sph_system *s, int it, bool eager, cudaGraphConditionalHandle c
     a.amb_tol = sphrt::AMB_TOL;
     if (f32) CUDA_TRY(cudaMemsetAsync(s->scal.p + S_AMB, 0, sizeof(int), st));
     if (first) phase_event(s, EV_DENSK_B, st);
+    if (!first) drop_items_if_small<<<1, 1, 0, st>>>(s->scal.p);
     sphrt::launch_density(a, ctx->prm.precision, ctx->grid[0][ctx->prm.precision == SPH_PREC_FP64], st);
+    if (!first) {
+        // few iterating particles: a block per walk instead (see density_rewalk_blocks)
+        const int rg = ctx->sm_count * 4;
+        if (f32)
+            sphk::density_rewalk_blocks<false><<<rg, sphk::REWALK_THREADS, 0, st>>>(
+                a, s->scal.p + S_NACTIVE, s->a_sfirst.p, s->a_scount.p, s->scal.p + S_SMALL);
+        else
+            sphk::density_rewalk_blocks<true><<<rg, sphk::REWALK_THREADS, 0, st>>>(
+                a, s->scal.p + S_NACTIVE, s->a_sfirst.p, s->a_scount.p, s->scal.p + S_SMALL);
+    }
     if (first) phase_event(s, EV_DENSK_E, st);
     if (f32) {
         // FP64 recomputation of decision-ambiguous particles (same lists)
