@@ -514,7 +514,7 @@ def run_ours(args):
         pairs_e = ke * (ste["pairs_density"] + ste["pairs_hydro"] + ste["pairs_gravity"])
         line["e2e"] = {"value": el / ke, "unit": "s/step", "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * el / ke,
-                       "interactions_per_s": pairs_e / el,
+                       "interactions_per_s": pairs_e / el, "density_walks": ste["density_iterations"],
                        "path": "sph_system_upload -> sph_system_compute_forces -> sph_system_download "
                                "(pinned host buffers, converged state)"}
 

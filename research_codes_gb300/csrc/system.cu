@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -263,6 +264,19 @@ struct StarComs : SumOp {    // both stars' centres (calcSystemSize, hdr_util.hp
 };
 
 // ---------------------------------------------------------------- small kernels
+// Run parameters the reference derives from the initial state
+// (hdr_hgas.hpp:961-970, 1335): ksrmax = the distance between the two stars'
+// centres of mass (c: their mass-weighted sums and masses; the largest double
+// for a single star), epsu = 1e-4 of the smallest u (already in dsc).
+__global__ void upload_scalars(const double *c, double *dsc) {
+    double ksrmax = DBL_MAX;
+    if (c[3] > 0.0 && c[7] > 0.0) {
+        const double dx = c[0] / c[3] - c[4] / c[7], dy = c[1] / c[3] - c[5] / c[7], dz = c[2] / c[3] - c[6] / c[7];
+        ksrmax = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    dsc[D_KSRMAX] = ksrmax;
+    dsc[D_EPSU] *= 1e-4;
+}
 __global__ void bbox_stage1(const dbl4 *pos, int n, double *partial) {
     __shared__ double sh[6][RED_THREADS];
     double b[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
@@ -2025,19 +2039,8 @@ extern "C" int sph_system_upload(sph_system *s, double t0, const int64_t *id, co
     fc.pos = s->pos[0].p;
     fc.istar = s->istar[0].p;
     reduce(s, fc, s->box.p);
-    double c[8], eu;
-    CUDA_TRY(cudaMemcpyAsync(c, s->box.p, sizeof(c), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(&eu, s->dscal.p + D_EPSU, sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    double ksrmax = std::numeric_limits<double>::max();
-    if (c[3] > 0.0 && c[7] > 0.0) {
-        const double dx = c[0] / c[3] - c[4] / c[7], dy = c[1] / c[3] - c[5] / c[7], dz = c[2] / c[3] - c[6] / c[7];
-        ksrmax = std::sqrt(dx * dx + dy * dy + dz * dz);
-    }
-    eu *= 1e-4;
-    CUDA_TRY(cudaMemcpyAsync(s->dscal.p + D_KSRMAX, &ksrmax, sizeof(double), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(s->dscal.p + D_EPSU, &eu, sizeof(double), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    upload_scalars<<<1, 1, 0, st>>>(s->box.p, s->dscal.p);
+    CUDA_TRY(cudaStreamSynchronize(st));   // the caller's host arrays are free again
     s->steps = 0;
     return SPH_OK;
 }
