@@ -1,7 +1,9 @@
 """Autotuner of the run parameters that shape the GPU work, not the physics.
 
 Tuned by coordinate descent on the device time of a force evaluation of the
-system's current state (CUDA events of eager evaluations, median of `reps`):
+system's current state, as the captured steps run it: CUDA events of
+replays of the captured force-evaluation graph (gravity lists on the second
+stream, no host round trips), median of `reps`:
 
 * n_group — the most i-particles a walk (i-group) may hold, which sets the
   list lengths and the pairs per step (the reference's FDPS setting is 256,
@@ -28,9 +30,9 @@ CANDIDATES = {"n_group": (64, 128, 256, 512), "item_split_nj": (2048, 4096, 8192
 
 
 def time_forces(ps, reps=3):
-    """Median device time (ms) of `reps` eager force evaluations after one
-    warm-up evaluation."""
-    ps.set_graph(False)
+    """Median device time (ms) of `reps` replays of the captured
+    force-evaluation graph, after the evaluation that captures it."""
+    ps.set_graph(True)
     ps.compute_forces()
     t = []
     for _ in range(reps):
