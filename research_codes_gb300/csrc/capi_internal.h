@@ -32,6 +32,15 @@ struct DevBuf {
             p = nullptr;
             return 1;
         }
+        // no buffer is ever read before it is written, but a field that a
+        // caller leaves unset (e.g. the signal velocity before the first
+        // force evaluation) then holds zeros, not stale memory
+        if (cudaMemset(p, 0, want * sizeof(T)) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(p);
+            p = nullptr;
+            return 1;
+        }
         cap = want;
         return 0;
     }

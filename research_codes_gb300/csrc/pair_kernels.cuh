@@ -720,19 +720,38 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double (*red)[REWALK_T
     }
     __syncthreads();
 }
+// Error bits (scal[err_slot]): list_err_mask marks lists that cannot be
+// used (a failed build: nothing runs), bounds_bit is raised for an index
+// outside the particle or list arrays (that access is skipped).
+struct RewalkBounds {
+    int n;                 // particles
+    long long list_cap;    // entries of the walks' lists
+    int *err;              // error word
+    int list_err_mask;
+    int bounds_bit;
+};
 template <bool F64>
 __global__ void __launch_bounds__(REWALK_THREADS) density_rewalk_blocks(const DensityArgs a, const int *n_walks,
                                                                        const int *seg_first, const int *seg_count,
-                                                                       const int *small) {
+                                                                       const int *small, RewalkBounds bnd) {
     typedef typename Real<F64>::T R;
     __shared__ double red[6][REWALK_THREADS / 32];
-    if (!*small) return;
+    if (!*small || (*bnd.err & bnd.list_err_mask)) return;
     const int nw = *n_walks;
     const double ksr_max = a.ksr_max_dev ? *a.ksr_max_dev : a.ksr_max;
     for (int w = blockIdx.x; w < nw; w += gridDim.x) {
         const int jb = a.j_off[w], je = a.j_off[w + 1];
+        if (jb < 0 || je < jb || (long long)je > bnd.list_cap) {
+            if (threadIdx.x == 0) atomicOr(bnd.err, bnd.bounds_bit);
+            continue;   // block-uniform
+        }
         for (int s = 0; s < seg_count[w]; ++s) {
-            const int ii = a.i_list[seg_first[w] + s];
+            const int u = seg_first[w] + s;
+            const int ii = (u >= 0 && u < bnd.n) ? a.i_list[u] : -1;
+            if (ii < 0 || ii >= bnd.n) {
+                if (threadIdx.x == 0) atomicOr(bnd.err, bnd.bounds_bit);
+                continue;   // block-uniform
+            }
             float4 cph = make_float4(0, 0, 0, 0), cpl = cph;
             dbl4 ci = make_dbl4(0, 0, 0, 0);
             if (F64) ci = a.i_pm[ii];
@@ -763,6 +782,10 @@ __global__ void __launch_bounds__(REWALK_THREADS) density_rewalk_blocks(const De
                 long long cnt = 0;
                 for (int k = jb + threadIdx.x; k < je; k += REWALK_THREADS) {
                     const int j = a.j_idx ? a.j_idx[k] : k;
+                    if (j < 0 || j >= bnd.n) {
+                        atomicOr(bnd.err, bnd.bounds_bit);
+                        continue;
+                    }
                     R dx, dy, dz;
                     const R m = rel(j, dx, dy, dz);
                     const R q = sqrt_q(dx * dx + dy * dy + dz * dz, hinv2);
@@ -814,6 +837,10 @@ __global__ void __launch_bounds__(REWALK_THREADS) density_rewalk_blocks(const De
             Acc<F64> g_acc, d_acc, rx_acc, ry_acc, rz_acc;
             for (int k = jb + threadIdx.x; k < je; k += REWALK_THREADS) {
                 const int j = a.j_idx ? a.j_idx[k] : k;
+                if (j < 0 || j >= bnd.n) {
+                    atomicOr(bnd.err, bnd.bounds_bit);
+                    continue;
+                }
                 R dx, dy, dz;
                 const R m = rel(j, dx, dy, dz);
                 R ux, uy, uz;

@@ -57,7 +57,7 @@ enum { D_TIME = 0, D_DT, D_KSRMAX, D_EPSU, D_DTC, D_XC, D_YC, D_ZC, D_MC, D_EKIN
 enum { L_PAIRS_D = 0, L_PAIRS_H, L_PAIRS_G, L_LIST_D, L_LIST_H, L_LIST_G, L_PAIRS_D1, L_LIST_R, L_EVAL_D1,
        L_EVAL_DG1, L_EVAL_HN, L_EVAL_HF, L_DLISTED, L_DSWEPT, L_HSKIP, L_HTILES, L_HMARK, L_HSLOTS, L_NI };
 // error bits
-enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8 };
+enum { E_STACK = 1, E_LISTCAP = 2, E_NOTCONV = 4, E_DTMIN = 8, E_BOUNDS = 16 };
 // phase events
 enum { EV_TREE_B = 0, EV_TREE_E, EV_DENS_B, EV_DENSK_B, EV_DENSK_E, EV_DENS_E, EV_GLIST_B, EV_GLIST_E, EV_GK_B,
        EV_GK_E, EV_HLIST_B, EV_HK_B, EV_HK_E, EV_END, EV_HK_MID, EV_N };
@@ -1321,7 +1321,10 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.task_queue = sc + S_TQUEUE;
     // one traversal: counts per task and the entries into pool chunks; in
     // eager mode the pool and the chains grow until they hold the lists with
-    // a quarter of headroom (graph replays cannot allocate)
+    // a quarter of headroom (graph replays cannot allocate).  A pool that
+    // held this traversal's lists but lacks headroom grows only after
+    // copy_lists has read it (growing frees the old buffer).
+    long long pool_grow_to = 0;
     for (;;) {
         a.pool = L.lpool.p;
         a.pool_chunks = L.lpool_chunks;
@@ -1345,9 +1348,14 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
                                     used, sphtree::LIST_CHUNK);
         if (used + used / 4 > L.lpool_chunks && L.lpool_chunks < MAX_POOL_CHUNKS) {
             const long long want = std::min(used + used / 2 + 1024, MAX_POOL_CHUNKS);
-            if (L.lpool.ensure((size_t)want * sphtree::LIST_CHUNK))
-                return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list pool allocation of %lld chunks failed", want);
-            L.lpool_chunks = std::min((long long)(L.lpool.cap / sphtree::LIST_CHUNK), MAX_POOL_CHUNKS);
+            if (!redo) {
+                pool_grow_to = want;   // this traversal's chunks are still in the pool
+            } else {
+                if (L.lpool.ensure((size_t)want * sphtree::LIST_CHUNK))
+                    return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list pool allocation of %lld chunks failed",
+                                            want);
+                L.lpool_chunks = std::min((long long)(L.lpool.cap / sphtree::LIST_CHUNK), MAX_POOL_CHUNKS);
+            }
         }
         if (pu[1] & 2) {
             L.lchain_max *= 2;
@@ -1384,6 +1392,14 @@ int build_lists_and_items(sph_system *s, int kind, const int *walk_node, const d
     a.j_idx = s->jidx[kind].p;
     a.capacity = s->lcap[kind];
     sphtree::copy_lists<<<s->ctx->sm_count * 8, sphtree::COPY_THREADS, 0, st>>>(a);
+    if (pool_grow_to > 0) {
+        // headroom for the next evaluations; the copy above has read the old
+        // pool (freeing it waits for the device)
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (L.lpool.ensure((size_t)pool_grow_to * sphtree::LIST_CHUNK))
+            return sphrt::set_error(s->ctx, SPH_ERR_CUDA, "list pool allocation of %lld chunks failed", pool_grow_to);
+        L.lpool_chunks = std::min((long long)(L.lpool.cap / sphtree::LIST_CHUNK), MAX_POOL_CHUNKS);
+    }
     // work items
     const int *ifirst = item_first ? item_first : s->walk_first[kind];
     const int *icount = item_count ? item_count : s->walk_count[kind];
@@ -1477,12 +1493,13 @@ int density_walk(sph_system *s, int it, bool eager, cudaGraphConditionalHandle c
     if (!first) {
         // few iterating particles: a block per walk instead (see density_rewalk_blocks)
         const int rg = ctx->sm_count * 4;
+        const sphk::RewalkBounds bnd{n, s->lcap[kind], s->scal.p + S_ERROR, E_LISTCAP | E_STACK, E_BOUNDS};
         if (f32)
             sphk::density_rewalk_blocks<false><<<rg, sphk::REWALK_THREADS, 0, st>>>(
-                a, s->scal.p + S_NACTIVE, s->a_sfirst.p, s->a_scount.p, s->scal.p + S_SMALL);
+                a, s->scal.p + S_NACTIVE, s->a_sfirst.p, s->a_scount.p, s->scal.p + S_SMALL, bnd);
         else
             sphk::density_rewalk_blocks<true><<<rg, sphk::REWALK_THREADS, 0, st>>>(
-                a, s->scal.p + S_NACTIVE, s->a_sfirst.p, s->a_scount.p, s->scal.p + S_SMALL);
+                a, s->scal.p + S_NACTIVE, s->a_sfirst.p, s->a_scount.p, s->scal.p + S_SMALL, bnd);
     }
     if (first) phase_event(s, EV_DENSK_E, st);
     if (f32) {
@@ -1823,6 +1840,7 @@ int check_errors(sph_system *s) {
         return sphrt::set_error(s->ctx, SPH_ERR_NOT_CONVERGED, "search radius still growing after %d walks",
                                 s->prm.max_density_iterations);
     if (e & E_DTMIN) return sphrt::set_error(s->ctx, SPH_ERR_NOT_CONVERGED, "time step below dt_min");
+    if (e & E_BOUNDS) return sphrt::set_error(s->ctx, SPH_ERR_STATE, "index out of range in a density re-walk");
     return SPH_OK;
 }
 
