@@ -8,7 +8,11 @@ first guess h0) finishes them.  The oracle replays both walks on the engine's ow
 lists (kind 0: the first walk; kind 3: the last re-walk) with the same first
 guess and search radii: every particle's final density, h, grad-h term,
 div v, |rot v| and neighbour count come from the walk in which it stopped
-iterating, and the set of particles re-walked is the oracle's."""
+iterating, and the set of particles re-walked is the oracle's.
+
+A second case starts only 24 particles from 0.85 x their converged h, so
+the re-walk has at most 1024 iterating particles and runs on the
+block-per-walk kernel (density_rewalk_blocks) instead of density_kernel."""
 import numpy as np
 import pytest
 
@@ -33,8 +37,9 @@ def _state():
     return s
 
 
+@pytest.mark.parametrize("few", [False, True])
 @pytest.mark.parametrize("prec", ["fp64", "fp32c"])
-def test_density_rewalk_matches_oracle_walk_by_walk(prec):
+def test_density_rewalk_matches_oracle_walk_by_walk(prec, few):
     s = _state()
     n = len(s["mass"])
     ctx = functors.Context(precision=prec, eta=1.18, ksr_max=0.0)
@@ -43,7 +48,12 @@ def test_density_rewalk_matches_oracle_walk_by_walk(prec):
         sys.upload(s)
         sys.compute_forces()
         sys.compute_forces()
-        s["ksr"] = 0.9 * sys.download("ksr")
+        if few:
+            s["ksr"] = sys.download("ksr")
+            pick = np.random.default_rng(7).choice(n, 24, replace=False)
+            s["ksr"][pick] *= 0.85
+        else:
+            s["ksr"] = 0.9 * sys.download("ksr")
         sys.upload(s)
         sys.compute_forces()
         st = sys.stats()
@@ -64,6 +74,8 @@ def test_density_rewalk_matches_oracle_walk_by_walk(prec):
                                   eta=1.18, ksr_max=0.0)
         again = out["itr"].astype(bool)
         assert 0 < again.sum() < n
+        if few:
+            assert again.sum() <= 1024     # the block-per-walk re-walk
 
         # walk 1: the groups holding iterating particles, rs = 1.21 h0, those particles only
         state["rs"] = 1.1 * 1.1 * h0
