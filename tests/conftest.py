@@ -55,9 +55,10 @@ def field_errors(a, b, floor_frac=1e-3):
 
 
 def assert_cancelling_field(a, b, name, floor_frac=1e-3):
-    """Acceptance for FP32 pair sums that cancel strongly (the SPH pressure
-    gradient and softening correction of a star near hydrostatic equilibrium,
-    where the pair terms are ~R/h times larger than their sum): the median and
-    the normwise error within 1e-5, the 99.9th percentile within 1e-4."""
+    """Acceptance for sums that cancel strongly (the SPH pressure gradient,
+    du/dt and softening correction of a star near hydrostatic equilibrium,
+    where the pair terms are ~R/h times larger than their sum) computed by
+    two engines from inputs that differ at rounding level: the median and the
+    normwise difference within 1e-5, the 99.9th percentile within 1e-4."""
     e = field_errors(a, b, floor_frac)
     assert e["median"] < 1e-5 and e["normwise"] < 1e-5 and e["p999"] < 1e-4, (name, e)

@@ -320,13 +320,18 @@ def test_fp32c_step_tracks_fp64_step():
 
 
 def test_fp32c_forces_match_fp64_on_same_state():
-    """North-star parity: rho, h, gravity acceleration and pot of the FP32C
-    engine against the plain FP64 engine on identical particle state, every
-    particle at 1e-5 relative (floor 1e-3 of the field maximum); the hydro
-    acceleration and du/dt, whose pair terms cancel to ~1/(R/h) of their size
-    near equilibrium, by median / normwise 1e-5 and 99.9th percentile 1e-4.  FP32C density results
-    whose search-radius decision lies within FP32 rounding of the threshold
-    are recomputed in FP64, so both precisions take the same walks."""
+    """The FP32C engine against the plain FP64 engine from identical particle
+    state: rho, h, gravity acceleration and pot within 1e-5 for every particle
+    (floor 1e-3 of the field maximum).  Each engine computes its own h, rho,
+    P and Balsara switch (equal to ~1e-7), and the hydro acceleration, du/dt
+    and the softening correction are sums whose pair terms cancel to
+    ~1/(R/h) of their size near equilibrium, so those input differences
+    reach them amplified: they are held to median / normwise 1e-5 and 99.9th
+    percentile 1e-4 here.  With identical inputs every particle is within
+    1e-5 (test_hydro_matches_oracle_on_engine_lists, against the FP64
+    oracle).  FP32C density results whose search-radius decision lies within
+    FP32 rounding of the threshold are recomputed in FP64, so both precisions
+    take the same walks."""
     s = _two_stars(n=12000, seed=21)
     res = {}
     with functors.Context(precision="fp64", eta=1.18) as ctx:
