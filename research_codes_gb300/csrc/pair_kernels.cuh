@@ -44,7 +44,7 @@
 #define SPH_DENSITY_UNROLL 4
 #endif
 #ifndef SPH_HYDRO_MARK_UNROLL
-#define SPH_HYDRO_MARK_UNROLL 8
+#define SPH_HYDRO_MARK_UNROLL 16
 #endif
 // The double-float hydro pass (128 threads): 3 blocks per SM, 168 registers.
 #ifndef SPH_HYDRO_DF_MIN_BLOCKS
