@@ -25,7 +25,7 @@ import itertools
 
 import numpy as np
 
-CANDIDATES = {"n_group": (64, 96, 128, 192, 256), "item_split_nj": (512, 1024, 2048, 4096, 8192, 1 << 30),
+CANDIDATES = {"n_group": (64, 80, 96, 128, 192, 256), "item_split_nj": (512, 1024, 2048, 4096, 8192, 1 << 30),
               "heavy_classes": (0, 1, 2, 4), "gravity_jtile": (32, 64)}
 
 

@@ -76,4 +76,4 @@ def test_result_is_a_coordinate_minimum_of_a_coupled_cost():
 def test_grid_enumerates_every_combination():
     g = autotune.grid({"a": (1, 2), "b": (3, 4, 5)})
     assert len(g) == 6 and {"a": 2, "b": 5} in g
-    assert len(autotune.grid()) == 5 * 6 * 4 * 2
+    assert len(autotune.grid()) == 6 * 6 * 4 * 2
