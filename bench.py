@@ -10,11 +10,14 @@ A step is one iteration of the reference's loop body — time step, predict,
 density with smoothing-length iteration, EOS, tree gravity, hydro force,
 correct — run by the device-resident engine as one CUDA graph.
 
-Metric: pair-interactions per second over the whole step (density + hydro +
-gravity pairs, each pair = one (i, j) evaluation in a walk's list), plus
-ms/step.  The line also carries the FP64 comparator, FP32C-vs-FP64 parity on
-the same state, the dominant kernel's roofline, the end-to-end rate through
-the C ABI with host buffers, and the CPU oracle's rate on the host cores.
+Metric: seconds per step (lower is better), after autotuning the work shape
+(n_group, item split, item order, gravity j-tile).  Beside it: pair
+interactions per second counted three ways (listed in the walks' lists, also
+at the reference's n_group = 256; evaluated by the kernels; inside a kernel
+support), every output's error against the FP64 oracle on the same walks and
+inputs, the energy drift per step, the FP64 comparator, the dominant
+kernel's roofline, the end-to-end time through the C ABI with host buffers,
+and the CPU oracle's time for the same step on the host cores.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
