@@ -77,3 +77,17 @@ def test_grid_enumerates_every_combination():
     g = autotune.grid({"a": (1, 2), "b": (3, 4, 5)})
     assert len(g) == 6 and {"a": 2, "b": 5} in g
     assert len(autotune.grid()) == 6 * 6 * 4 * 2
+
+
+def test_candidates_are_valid_system_parameters():
+    # the values sph_system_set_params accepts (include/sph_gb300.h):
+    # n_group >= 1, gravity_jtile 32 or 64; item_split_nj <= 0 means the
+    # default, so every candidate split is a positive length
+    c = autotune.CANDIDATES
+    assert set(c) == {"n_group", "item_split_nj", "heavy_classes", "gravity_jtile"}
+    assert all(isinstance(v, int) and v >= 1 for v in c["n_group"])
+    assert all(isinstance(v, int) and v > 0 for v in c["item_split_nj"])
+    assert all(isinstance(v, int) and v >= 0 for v in c["heavy_classes"])
+    assert set(c["gravity_jtile"]) <= {32, 64}
+    # the reference's own group size stays among the candidates (main.cpp:380)
+    assert 256 in c["n_group"]
